@@ -1,0 +1,241 @@
+/*
+ * stz_api.h -- C ABI of the GB300 shear-transformation-zone (STZ) kinetic Monte
+ * Carlo engine.
+ *
+ * Plain C types only: no CUDA, no C++ and no framework types cross this
+ * boundary. Every entry point returns an int status (STZ_OK == 0) and never
+ * aborts the process. The device owns all simulation state; host copies are
+ * produced only on request (stz_get_field / stz_get_scalars / stz_get_events).
+ *
+ * Reference interfaces replaced (paths inside the reference project
+ * "Mesoscale simulation STZ model/"):
+ *   stz_params_from_input_file  <- ReadInput(FILE*) + Init()        io.c:4-101, init.c:6-75
+ *   stz_create                  <- FFT_MPI_Init, Rand_Init, Alloc, Grad,
+ *                                  Energy_Init, DStrain, initial solve
+ *                                  init.c:77-206, init.c:225-479, elastic.c:6-142,
+ *                                  bmg.c:117-124
+ *   stz_run / stz_step          <- the driver loop body                bmg.c:138-411
+ *                                  (SofteningFactor init.c:711-739, ActEnergy
+ *                                  init.c:561-690, Q<0 test bmg.c:148-157,
+ *                                  athermal_plasticity evolution.c:47-100,
+ *                                  KMC evolution.c:102-363)
+ *   stz_solve                   <- InhomogeneousStressSolver / HomogeneousStressSolver
+ *                                  elastic.c:977-1066, elastic.c:779-903
+ *   stz_elastic_energy          <- ElasticEnergy()                     elastic.c:533-547
+ *   stz_destroy                 <- Free()                              init.c:482-559
+ * The reference-named entry points themselves (KMC, ActEnergy, ...) are
+ * declared in stz_refapi.h.
+ */
+#ifndef STZ_API_H
+#define STZ_API_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STZ_API_VERSION 1
+#define STZ_MODES 20           /* candidate modes per site (reference MODES, bmg.h:29) */
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  STZ_OK = 0,
+  STZ_ERR_INVALID = 1,      /* bad argument or parameter combination */
+  STZ_ERR_CUDA = 2,         /* CUDA runtime error (message in stz_last_error) */
+  STZ_ERR_NAN = 3,          /* non-finite value met in a field or in the total rate */
+  STZ_ERR_NO_EVENT = 4,     /* selection located no event (evolution.c:229-234) */
+  STZ_ERR_UNSUPPORTED = 5,  /* a flag combination this engine does not implement */
+  STZ_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+  STZ_ERR_IO = 7,           /* input file could not be read / parsed */
+  STZ_ERR_NOMEM = 8         /* device or host allocation failed */
+};
+
+/* ---- model, loading, precision ------------------------------------------ */
+enum {
+  STZ_MODEL_REF2D = 0,      /* the reference's own 2D model: per-site per-mode
+                               barriers and eigenstrains, re-drawn after each
+                               transformation (elastic.c:126-130, 508-512) */
+  STZ_MODEL_GLOBAL3D = 1    /* 3D: one table of STZ_MODES traceless modes shared
+                               by all sites, per-site barrier dF */
+};
+
+enum {                      /* bmgFlags.h:7-9 plus a stress-controlled mode */
+  STZ_LOAD_TENSION = 0,
+  STZ_LOAD_SHEAR = 1,
+  STZ_LOAD_COMPRESSION = 2,
+  STZ_LOAD_STRESS = 3       /* constant applied mean stress (applied_stress[]) */
+};
+
+enum {                      /* direction-softening schemes, bmgFlags.h:30-35 */
+  STZ_SF_LINEAR_FWD = 0,
+  STZ_SF_LINEAR_BWD = 1,
+  STZ_SF_EVEN = 2,
+  STZ_SF_SQUARE_FWD = 3,
+  STZ_SF_CUBIC_FWD = 4,
+  STZ_SF_GAUSS_FWD = 5
+};
+
+enum {
+  STZ_PREC_FP64 = 0,        /* "plain": FP64 throughout */
+  STZ_PREC_MIXED = 1        /* FP32 stress field, contraction and rates; FP64
+                               total rate, cumulative search, clock, eigenstrain
+                               and mean strain; periodic FP64 re-solve */
+};
+
+enum {
+  STZ_SOLVER_FFT = 0,       /* full Green's-function re-solve by FFT after every
+                               transformation (the reference's method) */
+  STZ_SOLVER_KERNEL = 1,    /* incremental: add the precomputed real-space
+                               response of one transformed voxel */
+  STZ_SOLVER_AUTO = 2       /* pick per grid size from the tuning table */
+};
+
+enum {                      /* barrier (dF) generators for STZ_MODEL_GLOBAL3D */
+  STZ_DF_TRUNC_NORMAL = 0,  /* iid Normal(q0_mean, q0_sd) truncated at +-q0_trunc sd */
+  STZ_DF_CORRELATED = 1     /* Gaussian random field, Gaussian covariance of
+                               length q0_corr_len voxels, clipped at +-q0_trunc sd */
+};
+
+/* Voigt component order. 3D: xx yy zz yz xz xy. 2D: xx yy xy (reference DE=3).
+ * x runs along the fastest grid axis n[2] (reference index j), y along n[1]
+ * (reference index i) and z along n[0] (1 in 2D). */
+enum { STZ_XX = 0, STZ_YY = 1, STZ_ZZ = 2, STZ_YZ = 3, STZ_XZ = 4, STZ_XY = 5 };
+
+typedef struct stz_params {
+  int32_t model;             /* STZ_MODEL_* */
+  int32_t n[3];              /* grid extents, slowest first; 2D: n[0] == 1 */
+  /* elastic medium (GPa) */
+  double  lambda, mu;        /* Lame constants of the homogeneous medium */
+  double  young, poisson;    /* E and nu as used by the loading formulas
+                                (reference: E from input, nu after LOW_T, init.c:26) */
+  /* kinetics */
+  double  temperature;       /* K */
+  double  trial_frequency;   /* s^-1 (reference TRIAL_FREQUENCY, bmg.h:42) */
+  double  voxel_volume;      /* nm^3 (reference VOXEL0, bmg.h:90) */
+  /* barriers and modes */
+  int32_t df_kind;           /* STZ_DF_* (GLOBAL3D) */
+  double  q0_mean, q0_sd, q0_trunc, q0_corr_len;
+  double  gamma0;            /* mode magnitude (reference GAMMA0 = 0.14, bmg.h:94) */
+  /* loading (evolution.c:262-358) */
+  int32_t loading;           /* STZ_LOAD_* */
+  double  strain_rate;       /* rate of the loaded tensor component, s^-1 */
+  double  strain_increment;  /* elastic-step increment; dt = increment / rate */
+  double  end_strain;        /* stop when |loaded mean strain| exceeds this */
+  double  applied_stress[6]; /* GPa, STZ_LOAD_STRESS only */
+  int32_t no_subtract_error; /* bmgFlags.h NO_SUBTRACT_ERROR */
+  int32_t shear_elastic_quirk; /* 1: elastic step adds strain_rate*1 to the mean
+                                  shear strain, as evolution.c:350 does */
+  /* softening / memory (init.c:59-68, 711-739; elastic.c:366-397) */
+  int32_t softening;         /* input "Softening Flag" */
+  int32_t sf_scheme;         /* STZ_SF_* */
+  double  perm_soft, temp_soft, perm_soft_cap, t_temp;
+  /* crystal-like MRO inputs (init.c:345-437). Only an all-glass map is run. */
+  double  xmro_frac, xq0amp, random_ratio;
+  int32_t init_mro;
+  /* bookkeeping */
+  int32_t print_period;      /* reference "Print period" */
+  uint64_t seed;             /* MT19937 seed; 0 maps to 4357 as GSL does */
+  /* engine controls */
+  int32_t precision;         /* STZ_PREC_* */
+  int32_t solver;            /* STZ_SOLVER_* */
+  int32_t resolve_period;    /* mixed: FP64 full re-solve every this many events (0 = never) */
+  int32_t device;            /* CUDA device ordinal */
+  int32_t reserved[8];
+} stz_params;
+
+/* kinds of stz_event */
+enum { STZ_EV_THERMAL = 0, STZ_EV_ATHERMAL = 1, STZ_EV_ELASTIC = 2 };
+
+typedef struct stz_event {
+  int64_t step;              /* driver-loop iteration, 1-based (reference 'step') */
+  int64_t site;              /* linear site index (i0*n1 + i1)*n2 + i2, -1 for elastic */
+  int32_t kind;              /* STZ_EV_* */
+  int32_t mode;              /* 0..STZ_MODES-1, -1 for elastic */
+  double  time;              /* simulation clock after the step, s */
+  double  dt;                /* clock advance of the step, s */
+  double  q;                 /* activation energy of the chosen (site, mode), eV */
+  double  total_rate;        /* summed rate over all (mode, site), s^-1 */
+} stz_event;
+
+/* scalars returned by stz_get_scalars */
+typedef struct stz_scalars {
+  double  time;              /* totime */
+  double  eps_avg[6];        /* mean strain EpsAvg (Voigt, tensor shear) */
+  double  stress[6];         /* mean stress Stress */
+  double  eps0_avg[6];       /* mean eigenstrain */
+  int64_t step, kstep, astep, estep;  /* bmg.h:350-354 counters */
+  int64_t n_print;
+  int64_t n_events_logged;
+  int32_t stopped;           /* 1: end strain reached, 2: unstable (bmg.c:382-409) */
+  int32_t status;            /* sticky device error status */
+  double  stress_err_max;    /* mixed: max relative stress error at the last FP64 re-solve */
+  double  stress_err_rms;
+  int64_t near_ties;         /* selections whose cumulative margin was below 1e-12 */
+  int64_t reserved[6];
+} stz_scalars;
+
+/* field selectors for stz_get_field / stz_set_field */
+enum {
+  STZ_FIELD_SIGMA = 0,       /* stress, comp 0..5 (0..2 in 2D) */
+  STZ_FIELD_EPS0 = 1,        /* accumulated eigenstrain */
+  STZ_FIELD_DF = 2,          /* barrier: GLOBAL3D dF (comp 0); REF2D Q0[mode] (comp = mode) */
+  STZ_FIELD_DEPS = 3,        /* REF2D mode eigenstrain: comp = mode*3 + voigt */
+  STZ_FIELD_TLAST = 4,
+  STZ_FIELD_PERM_SOFT = 5,
+  STZ_FIELD_TEMP_SOFT = 6,
+  STZ_FIELD_PREV_DEPS = 7,   /* eigenstrain increment of the site's last transformation */
+  STZ_FIELD_Q = 8            /* activation energy Q[mode] for the current stress */
+};
+
+typedef struct stz_ctx stz_ctx;
+
+/* ---- parameters ---------------------------------------------------------- */
+/* Fill defaults for a model (reference constants for REF2D, the 3D study
+ * constants for GLOBAL3D). */
+int stz_params_default(stz_params* p, int32_t model);
+
+/* Parse the reference's labelled 'input' file (io.c:4-101) and derive the
+ * moduli, clock and softening constants exactly as Init() does (init.c:6-75).
+ * Grid extents are left unchanged (the reference fixes them at compile time). */
+int stz_params_from_input_file(stz_params* p, const char* path);
+
+/* ---- lifecycle ----------------------------------------------------------- */
+int  stz_create(const stz_params* p, stz_ctx** out);
+void stz_destroy(stz_ctx* ctx);
+const char* stz_last_error(void);   /* thread-local message of the last failure */
+
+/* ---- stepping ------------------------------------------------------------ */
+/* Run driver-loop iterations until max_steps iterations or max_events thermal
+ * events have been done, or the run stops (end strain / instability). The
+ * event log keeps every thermal, athermal and elastic step of the run. */
+int stz_run(stz_ctx* ctx, int64_t max_steps, int64_t max_events);
+
+/* Re-solve the stress field from the accumulated eigenstrain in FP64 (the
+ * reference's elastic solve). */
+int stz_solve(stz_ctx* ctx);
+
+int stz_get_scalars(stz_ctx* ctx, stz_scalars* out);
+/* Copy out log entries [first, first+cap) ; *n receives the number copied. */
+int stz_get_events(stz_ctx* ctx, int64_t first, stz_event* out, int64_t cap, int64_t* n);
+int stz_get_field(stz_ctx* ctx, int32_t which, int32_t comp, double* host, int64_t count);
+int stz_set_field(stz_ctx* ctx, int32_t which, int32_t comp, const double* host, int64_t count);
+int stz_elastic_energy(stz_ctx* ctx, double* out);
+
+/* ---- timing and accounting (for benchmarks) ------------------------------ */
+int stz_sync(stz_ctx* ctx);
+int stz_timer_start(stz_ctx* ctx);
+int stz_timer_stop(stz_ctx* ctx, float* ms);       /* CUDA events on the ctx stream */
+int stz_flush_l2(stz_ctx* ctx);                      /* writes a buffer larger than L2 */
+int64_t stz_kernel_launches(stz_ctx* ctx);           /* kernels launched by this ctx so far */
+/* sizeof the ABI structs, for bindings: 0 stz_params, 1 stz_event, 2 stz_scalars */
+int64_t stz_sizeof(int32_t which);
+/* Average device time (ms) of the dominant per-event kernel over the last
+ * stz_run call, measured with CUDA events around its launches. */
+int stz_kernel_time(stz_ctx* ctx, int32_t which, double* ms_avg, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STZ_API_H */

@@ -1,0 +1,136 @@
+"""Workload configurations.
+
+ref2d(...)      the reference's own 2D model, built from a reference-format
+                input file (labels of io.c:4-101) at a chosen grid
+stress32()      32^3, FP64, constant applied pure shear stress 1 GPa, seed 0
+shear64(seed)   64^3, FP64, shear strain rate, seeds 0-3
+mixed128()      128^3, mixed form, periodic FP64 re-solve every 1000 events
+grf256()        256^3, mixed form, correlated barrier field
+replicas(...)   uneven 3D replicas (grids 32/48/64/96, T in [325, 585] K,
+                log-uniform strain rates), seeds 0-255
+
+Common 3D physics: mu = 35 GPa, nu = 0.35, nu0 = 1e13 /s, Omega0 = 1 nm^3,
+T = 455 K, dF ~ N(1.2, 0.1) eV truncated at 3 sd, 20 traceless modes of
+magnitude 0.1 with orientations uniform on SO(3). The shear loading applies
+the reference's SHEAR branch to the xy tensor component; an engineering shear
+strain (rate) gamma corresponds to a tensor strain (rate) gamma/2.
+"""
+import math
+import os
+
+import numpy as np
+
+from . import api
+
+INPUT_LABELS = [
+    ("Moduli(E, nu):", "{E} {nu}"),
+    ("Stress-free energy barrier:", "{q0amp}"),
+    ("Applied strain rate:", "{rate}"),
+    ("Strain increment:", "{inc}"),
+    ("Random seed:", "{seed}"),
+    ("Random ratio of fluctuation in energy barrier:", "{rr}"),
+    ("Print period:", "{pp}"),
+    ("End Strain:", "{end}"),
+    ("Softening Flag:", "{soft}"),
+    ("Relaxation Time:", "{relx}"),
+    ("Characteristic Xtal shear:", "{xs}"),
+    ("Barrier for Xtal shear:", "{xq}"),
+    ("Ratio for generating residual stress:", "{resi}"),
+    ("Residual stress data file:", "{resfile}"),
+    ("Volume fraction of crystal-like MRO:", "{xfrac}"),
+    ("Initialization condition for MRO:", "{initmro}"),
+    ("Stress-free energy barrier for crystal-like MRO:", "{xq0}"),
+]
+
+# values of the input file shipped with the reference
+SHIPPED_INPUT = dict(E="69.46", nu="0.365", q0amp="2.0", rate="1e-4", inc="1e-4", seed="123", rr="0.2",
+                     pp="5", end="0.06", soft="1", relx="0.", xs="0.04", xq="1.25", resi="0.06",
+                     resfile="NullSpaceBasis_128x128_Nullity254.out", xfrac="0.0", initmro="0", xq0="2.0")
+
+
+def write_input(path, **overrides):
+    """Write a reference-format 'input' file (the labelled layout of io.c)."""
+    v = dict(SHIPPED_INPUT)
+    v.update({k: str(x) for k, x in overrides.items()})
+    with open(path, "w") as f:
+        for label, fmt in INPUT_LABELS:
+            f.write(label + "\n" + fmt.format(**v) + "\n\n")
+    return path
+
+
+def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, **overrides):
+    p = api.default_params(api.MODEL_REF2D)
+    if input_path is None:
+        import tempfile
+        d = tempfile.mkdtemp(prefix="stz_in_")
+        input_path = write_input(os.path.join(d, "input"), **overrides)
+    api.params_from_input(input_path, p)
+    p.n[0], p.n[1], p.n[2] = 1, nx, ny
+    p.loading = loading
+    return p
+
+
+def _g3(n, seed=0):
+    p = api.default_params(api.MODEL_GLOBAL3D)
+    p.n[0] = p.n[1] = p.n[2] = n
+    p.seed = seed
+    return p
+
+
+def stress32(seed=0, n=32):
+    p = _g3(n, seed)
+    p.loading = api.LOAD_STRESS
+    p.applied_stress[api.XY] = 1.0
+    p.strain_rate = 0.0
+    return p
+
+
+def shear64(seed=0, n=64, eng_rate=1e-4, eng_end=0.05):
+    p = _g3(n, seed)
+    p.loading = api.LOAD_SHEAR
+    p.strain_rate = eng_rate / 2
+    p.end_strain = eng_end / 2
+    p.strain_increment = 1e-4
+    return p
+
+
+def mixed128(seed=0, n=128, resolve_period=1000):
+    p = shear64(seed, n)
+    p.precision = api.PREC_MIXED
+    p.solver = api.SOLVER_KERNEL
+    p.resolve_period = resolve_period
+    return p
+
+
+def plain128(seed=0, n=128):
+    return shear64(seed, n)
+
+
+def grf256(seed=0, n=256):
+    p = shear64(seed, n, eng_rate=1e-3, eng_end=0.08)
+    p.df_kind = api.DF_CORRELATED
+    p.q0_sd = 0.15
+    p.q0_corr_len = 4.0
+    p.precision = api.PREC_MIXED
+    p.solver = api.SOLVER_KERNEL
+    return p
+
+
+def replicas(count=256, seed_base=0, mixed=True, sizes=(32, 48, 64, 96)):
+    """Uneven replicas: grid uniform over `sizes`, T uniform in [325, 585] K,
+    engineering strain rate log-uniform in [1e-5, 1e-2] /s, seeds 0..count-1.
+    The draws come from numpy's PCG64 seeded with 2024 + seed_base."""
+    rng = np.random.default_rng(2024 + seed_base)
+    out = []
+    for i in range(count):
+        n = int(sizes[rng.integers(len(sizes))])
+        T = float(rng.uniform(325.0, 585.0))
+        rate = float(10 ** rng.uniform(-5, -2))
+        p = shear64(seed_base + i, n, eng_rate=rate)
+        p.temperature = T
+        p.t_temp = 1 / (p.trial_frequency * math.exp(-0.37 / (T * 1.380658e-23 / 1.60217733e-19)))
+        if mixed:
+            p.precision = api.PREC_MIXED
+            p.solver = api.SOLVER_KERNEL
+        out.append(p)
+    return out

@@ -1,0 +1,894 @@
+// engine.cu -- context lifecycle, initial state, step orchestration, C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "fft.cuh"
+#include "kmc.cuh"
+#include "stz_internal.h"
+
+namespace stz {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                __LINE__);                                                         \
+      return STZ_ERR_CUDA;                                                         \
+    }                                                                              \
+  } while (0)
+
+namespace {
+
+FFTPlan* plan_of(stz_ctx* c) { return reinterpret_cast<FFTPlan*>(c->fft); }
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+    return STZ_ERR_NOMEM;
+  }
+  cudaMemset(*p, 0, sizeof(T) * count);
+  return STZ_OK;
+}
+
+bool good_len(int n) {
+  if (n < 1) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+// Uniform random rotation from a point uniform on S^3 (Marsaglia 1972, two
+// points uniform in the unit disk): only +, *, / and sqrt, so every IEEE
+// host produces the same bits.
+void random_rotation(MT* r, double R[3][3]) {
+  double x1, x2, s1, x3, x4, s2;
+  do {
+    x1 = 2 * mt_uniform(r) - 1;
+    x2 = 2 * mt_uniform(r) - 1;
+    s1 = x1 * x1 + x2 * x2;
+  } while (s1 >= 1.0);
+  do {
+    x3 = 2 * mt_uniform(r) - 1;
+    x4 = 2 * mt_uniform(r) - 1;
+    s2 = x3 * x3 + x4 * x4;
+  } while (s2 >= 1.0 || s2 == 0.0);
+  const double t = std::sqrt((1 - s1) / s2);
+  const double w = x1, x = x2, y = x3 * t, z = x4 * t;
+  R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - z * w);     R[0][2] = 2 * (x * z + y * w);
+  R[1][0] = 2 * (x * y + z * w);     R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - x * w);
+  R[2][0] = 2 * (x * z - y * w);     R[2][1] = 2 * (y * z + x * w);     R[2][2] = 1 - 2 * (x * x + y * y);
+}
+
+void dev_coords(const double* s, double* d) {
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
+  d[0] = (s[0] - s[1]) * r2;
+  d[1] = (2.0 * s[2] - s[0] - s[1]) * r6;
+  d[2] = q2 * s[3];
+  d[3] = q2 * s[4];
+  d[4] = q2 * s[5];
+}
+
+void host_iso_inv(const KParams& kp, const double* s, double* e) {
+  const double lam = kp.lambda, mu = kp.mu;
+  if (kp.nc == 3) {
+    double tra = -lam / 2 / mu / (2 * lam + 2 * mu) * (s[0] + s[1]);
+    e[0] = tra + s[0] / 2 / mu;
+    e[1] = tra + s[1] / 2 / mu;
+    e[2] = s[2] / 2 / mu;
+  } else {
+    double tra = -lam / 2 / mu / (3 * lam + 2 * mu) * (s[0] + s[1] + s[2]);
+    for (int c = 0; c < 3; c++) e[c] = tra + s[c] / 2 / mu;
+    for (int c = 3; c < 6; c++) e[c] = s[c] / 2 / mu;
+  }
+}
+
+int upload(void* d, const void* h, size_t bytes, cudaStream_t st) {
+  CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
+  return STZ_OK;
+}
+
+// ------------------------------------------------------------- initial state
+int init_ref2d(stz_ctx* c, MT* rng) {
+  const stz_params& p = c->p;
+  const long long N = c->kp.N;
+  // Alloc(): MRO map (init.c:350-397), Energy_Init (init.c:181-198),
+  // DStrain glass branch (elastic.c:126-130); draw order is the reference's.
+  if (p.init_mro != 0) {
+    set_error("MRO initialisation from a structure file is not supported");
+    return STZ_ERR_UNSUPPORTED;
+  }
+  bool any_mro = false;
+  for (long long s = 0; s < N; s++) {
+    const double tmp = mt_uniform(rng);
+    if (tmp <= p.xmro_frac) {
+      any_mro = true;
+      (void)mt_uniform(rng);
+    }
+  }
+  if (any_mro) {
+    set_error("crystal-like MRO sites were drawn; only all-glass maps are supported");
+    return STZ_ERR_UNSUPPORTED;
+  }
+  std::vector<double> Q0((size_t)STZ_MODES * N), deps((size_t)STZ_MODES * 3 * N);
+  for (int m = 0; m < STZ_MODES; m++)
+    for (long long s = 0; s < N; s++) Q0[(size_t)m * N + s] = mt_gaussian(rng, p.q0_sd) + p.q0_mean;
+  for (int m = 0; m < STZ_MODES; m++)
+    for (long long s = 0; s < N; s++) {
+      double* d = deps.data() + (size_t)m * 3 * N;
+      d[s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
+      d[N + s] = -d[s];
+      d[2 * N + s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
+    }
+  int st;
+  if ((st = upload(c->f.Q0, Q0.data(), sizeof(double) * Q0.size(), c->stream))) return st;
+  if ((st = upload(c->f.deps, deps.data(), sizeof(double) * deps.size(), c->stream))) return st;
+  std::vector<double> tl((size_t)N, -100 * p.t_temp);
+  if ((st = upload(c->f.tlast, tl.data(), sizeof(double) * N, c->stream))) return st;
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+int init_global3d(stz_ctx* c, MT* rng) {
+  const stz_params& p = c->p;
+  KParams& kp = c->kp;
+  const long long N = kp.N;
+  for (int m = 0; m < STZ_MODES; m++) {
+    double R[3][3];
+    random_rotation(rng, R);
+    const double a[3] = {R[0][0], R[1][0], R[2][0]};
+    const double b[3] = {R[0][1], R[1][1], R[2][1]};
+    const double g = 0.5 * p.gamma0;
+    kp.modes[m][STZ_XX] = g * (2 * a[0] * b[0]);
+    kp.modes[m][STZ_YY] = g * (2 * a[1] * b[1]);
+    kp.modes[m][STZ_ZZ] = g * (2 * a[2] * b[2]);
+    kp.modes[m][STZ_YZ] = g * (a[1] * b[2] + a[2] * b[1]);
+    kp.modes[m][STZ_XZ] = g * (a[0] * b[2] + a[2] * b[0]);
+    kp.modes[m][STZ_XY] = g * (a[0] * b[1] + a[1] * b[0]);
+  }
+  std::vector<double> dF((size_t)N);
+  const double tr = p.q0_trunc;
+  if (p.df_kind == STZ_DF_TRUNC_NORMAL) {
+    for (long long s = 0; s < N; s++) {
+      double z;
+      do { z = mt_gaussian(rng, 1.0); } while (tr > 0 && std::fabs(z) > tr);
+      dF[s] = p.q0_mean + p.q0_sd * z;
+    }
+  } else if (p.df_kind == STZ_DF_CORRELATED) {
+    for (long long s = 0; s < N; s++) dF[s] = mt_gaussian(rng, 1.0);
+    int st;
+    if ((st = upload(c->f.dF, dF.data(), sizeof(double) * N, c->stream))) return st;
+    fft_filter_gaussian(*plan_of(c), c->f.dF, p.q0_corr_len, c->f.spec, c->stream);
+    CK(cudaMemcpyAsync(dF.data(), c->f.dF, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double ss = 0;
+    for (long long s = 0; s < N; s++) ss += dF[s] * dF[s];
+    const double sd = std::sqrt(ss / (double)N);
+    for (long long s = 0; s < N; s++) {
+      double z = dF[s] / sd;
+      if (tr > 0) z = std::min(tr, std::max(-tr, z));
+      dF[s] = p.q0_mean + p.q0_sd * z;
+    }
+  } else {
+    set_error("unknown barrier generator %d", p.df_kind);
+    return STZ_ERR_INVALID;
+  }
+  int st;
+  if ((st = upload(c->f.dF, dF.data(), sizeof(double) * N, c->stream))) return st;
+  if (c->f.dF32) launch_fill_f32(c->f.dF, c->f.dF32, N, c->stream);
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+// Mixed-form constants: deviatoric mode coordinates and rate scaling.
+void mixed_constants(stz_ctx* c) {
+  KParams& kp = c->kp;
+  const double cW = kp.V0 * 1e-18 * kJInEv;   // eV per (GPa * unit strain)
+  const double l2e = 1.4426950408889634074;
+  kp.q_ref = (float)c->p.q0_mean;
+  kp.a_scale = (float)(l2e / kp.kT);
+  kp.rate_scale = kp.vt * std::exp(-(double)kp.q_ref / kp.kT);
+  for (int m = 0; m < STZ_MODES; m++) {
+    double d[5];
+    dev_coords(kp.modes[m], d);
+    for (int k = 0; k < 5; k++) {
+      kp.mdev_raw[m][k] = (float)d[k];
+      kp.mdev[m][k] = (float)(d[k] * cW * 0.5 * l2e / kp.kT);
+    }
+  }
+}
+
+// ------------------------------------------------------------- solves
+int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
+  SolveArgs a{};
+  a.eps = c->f.eps0;
+  a.ebar = ebar;
+  a.lambda = c->kp.lambda;
+  a.mu = c->kp.mu;
+  a.gate = gate;
+  a.out = kOutSig64;
+  a.sig64 = c->f.sig;
+  a.spec = c->f.spec;
+  a.fp32 = 0;
+  return fft_solve(*plan_of(c), a, c->stream, &c->launches);
+}
+
+// FP64 re-solve into the FP32 deviatoric field (mixed form).
+int solve_dev(stz_ctx* c, const double* ebar, const double* uadd, double* err) {
+  SolveArgs a{};
+  a.eps = c->f.eps0;
+  a.ebar = ebar;
+  a.uadd = uadd;
+  a.lambda = c->kp.lambda;
+  a.mu = c->kp.mu;
+  a.out = kOutDev32;
+  a.sdev = c->f.sdev;
+  a.err = err;
+  a.spec = c->f.spec;
+  return fft_solve(*plan_of(c), a, c->stream, &c->launches);
+}
+
+double* ctl_field(stz_ctx* c, size_t offset) {
+  return reinterpret_cast<double*>(reinterpret_cast<char*>(c->f.ctl) + offset);
+}
+
+// The response of one voxel: five FP64 solves with a unit deviatoric
+// eigenstrain at the origin, projected on the deviatoric basis.
+int build_response_table(stz_ctx* c) {
+  KParams& kp = c->kp;
+  const long long N = kp.N;
+  const long long tn = (long long)kp.kt0 * kp.kt1 * kp.kt2;
+  int st;
+  if ((st = dalloc(&c->f.ktab, (size_t)15 * tn))) return st;
+  double *eps = nullptr, *sig = nullptr;
+  if ((st = dalloc(&eps, (size_t)6 * N))) return st;
+  if ((st = dalloc(&sig, (size_t)6 * N))) { cudaFree(eps); return st; }
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637;
+  const double basis[5][6] = {{r2, -r2, 0, 0, 0, 0},
+                              {-r6, -r6, 2 * r6, 0, 0, 0},
+                              {0, 0, 0, r2, 0, 0},
+                              {0, 0, 0, 0, r2, 0},
+                              {0, 0, 0, 0, 0, r2}};
+  for (int b = 0; b < 5; b++) {
+    for (int comp = 0; comp < 6; comp++)
+      CK(cudaMemcpyAsync(eps + (size_t)comp * N, &basis[b][comp], sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    SolveArgs a{};
+    a.eps = eps;
+    a.ebar = nullptr;
+    a.lambda = kp.lambda;
+    a.mu = kp.mu;
+    a.out = kOutSig64;
+    a.sig64 = sig;
+    a.spec = c->f.spec;
+    fft_solve(*plan_of(c), a, c->stream, &c->launches);
+    launch_ktab_column(kp, sig, c->f.ktab, b, c->stream);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(eps);
+  cudaFree(sig);
+  return STZ_OK;
+}
+
+// ------------------------------------------------------------- stepping
+// One driver-loop iteration of the FP64 forms, as a fixed kernel sequence.
+void enqueue_plain_step(stz_ctx* c) {
+  const KParams& kp = c->kp;
+  const Fields& f = c->f;
+  const int* gate = &f.ctl->solve_req;
+  const double* ebar = f.ctl->eps_avg;
+  launch_rate_fp64(kp, f, c->stream);
+  launch_athermal(kp, f, 0, c->stream);
+  solve_plain(c, gate, ebar);
+  launch_post_a(kp, f, c->stream);
+  solve_plain(c, gate, ebar);
+  launch_post_b(kp, f, c->stream);
+  c->launches += 1 + 2 + 2 + 1;
+}
+
+int sync_ctl(stz_ctx* c) {
+  CK(cudaMemcpyAsync(&c->host_ctl, c->f.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+int drain_log(stz_ctx* c) {
+  Ctl& h = c->host_ctl;
+  const long long cap = c->kp.log_cap;
+  long long from = h.log_base, to = h.nlog;
+  if (to > from) {
+    const size_t old = c->host_log.size();
+    c->host_log.resize(old + (size_t)(to - from));
+    long long i = from;
+    while (i < to) {
+      const long long slot = i % cap;
+      const long long n = std::min(to - i, cap - slot);
+      CK(cudaMemcpyAsync(c->host_log.data() + old + (i - from), c->f.log + slot, sizeof(stz_event) * n,
+                         cudaMemcpyDeviceToHost, c->stream));
+      i += n;
+    }
+    h.log_base = to;
+    CK(cudaMemcpyAsync(&c->f.ctl->log_base, &h.log_base, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return STZ_OK;
+}
+
+int set_targets(stz_ctx* c, long long max_kstep, long long max_step) {
+  Ctl& h = c->host_ctl;
+  h.max_kstep = max_kstep;
+  h.max_step = max_step;
+  h.halt = h.stopped ? 1 : 0;
+  h.halt_reason = h.stopped ? kHaltStop : kHaltNone;
+  CK(cudaMemcpyAsync(&c->f.ctl->max_kstep, &h.max_kstep, sizeof(long long) * 2, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(&c->f.ctl->halt, &h.halt, sizeof(int) * 2, cudaMemcpyHostToDevice, c->stream));
+  return STZ_OK;
+}
+
+int capture_plain_graph(stz_ctx* c, int steps) {
+  if (c->graph && c->graph_batch == steps) return STZ_OK;
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  cudaGraph_t g;
+  const int64_t l0 = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < steps; i++) {
+    if (c->kp.nc == 6 && c->f.sdev) launch_mixed(c->kp, c->f, 0, c->stream);
+    else enqueue_plain_step(c);
+  }
+  CK(cudaStreamEndCapture(c->stream, &g));
+  c->graph_launches = c->launches - l0;
+  c->launches = l0;
+  CK(cudaGraphInstantiate(&c->graph, g, 0));
+  cudaGraphDestroy(g);
+  c->graph_batch = steps;
+  return STZ_OK;
+}
+
+// Handle a halt of the mixed form between batches. Returns 1 when the run
+// must stop (target, stop condition or error).
+int mixed_service(stz_ctx* c, int* done) {
+  Ctl& h = c->host_ctl;
+  const KParams& kp = c->kp;
+  const Fields& f = c->f;
+  *done = 0;
+  if (h.status) { *done = 1; return STZ_OK; }
+  if (h.step_kind == kAthermal) {
+    // the avalanche, the reference's re-solve with the current mean strain,
+    // the athermal correction and the print check, then the stop checks
+    launch_athermal(kp, f, 1, c->stream);
+    solve_dev(c, f.ctl->eps_avg, nullptr, f.scratch);
+    launch_mixed_after_resolve(kp, f, 0, c->stream);
+    launch_post_a(kp, f, c->stream);
+    int st = sync_ctl(c);
+    if (st) return st;
+    if (h.print_done) {
+      solve_dev(c, f.ctl->eps_avg, nullptr, f.scratch);
+      launch_mixed_after_resolve(kp, f, 0, c->stream);
+    }
+    launch_post_b(kp, f, c->stream);
+    c->launches += 6;
+  } else {
+    if (kp.resolve_period > 0 && h.kstep >= h.next_resolve) {
+      // periodic FP64 re-solve: bring the FP32 field up to date, re-solve it
+      // in FP64 with the same mean strain and offsets, record the difference
+      launch_mixed(kp, f, 1, c->stream);
+      double zero[3] = {0, 0, 0};
+      CK(cudaMemcpyAsync(c->err_dev, zero, sizeof(zero), cudaMemcpyHostToDevice, c->stream));
+      solve_dev(c, f.ctl->eps_avg_applied, f.ctl->u, c->err_dev);
+      launch_mixed_after_resolve(kp, f, 1, c->stream);
+      double e[3];
+      CK(cudaMemcpyAsync(e, c->err_dev, sizeof(e), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      const double ref2 = std::max(e[2], 1e-300) / (double)kp.N;
+      c->err_max = std::sqrt(e[0] / ref2);
+      c->err_rms = std::sqrt((e[1] / (double)kp.N) / ref2);
+      h.next_resolve += kp.resolve_period;
+      CK(cudaMemcpyAsync(&f.ctl->next_resolve, &h.next_resolve, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+      c->launches += 2;
+    }
+    if (h.print_done) {
+      solve_dev(c, f.ctl->eps_avg, nullptr, f.scratch);
+      launch_mixed_after_resolve(kp, f, 0, c->stream);
+      launch_post_b(kp, f, c->stream);
+      c->launches += 2;
+    }
+  }
+  int st = sync_ctl(c);
+  if (st) return st;
+  if (h.stopped || h.status || h.halt_reason == kHaltTarget ||
+      (h.max_kstep >= 0 && h.kstep >= h.max_kstep) || (h.max_step >= 0 && h.step >= h.max_step)) {
+    *done = 1;
+    return STZ_OK;
+  }
+  // resume
+  h.halt = 0;
+  h.halt_reason = kHaltNone;
+  h.step_kind = kNone;
+  CK(cudaMemcpyAsync(&f.ctl->halt, &h.halt, sizeof(int) * 2, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(&f.ctl->step_kind, &h.step_kind, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  return STZ_OK;
+}
+
+}  // namespace
+}  // namespace stz
+
+using namespace stz;
+
+// ============================================================= C ABI
+extern "C" const char* stz_last_error(void) { return g_err; }
+
+extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
+  if (!pin || !out) return STZ_ERR_INVALID;
+  *out = nullptr;
+  const stz_params& p = *pin;
+  const bool ref2d = p.model == STZ_MODEL_REF2D;
+  if (p.model != STZ_MODEL_REF2D && p.model != STZ_MODEL_GLOBAL3D) { set_error("unknown model"); return STZ_ERR_INVALID; }
+  if ((ref2d && p.n[0] != 1) || !good_len(p.n[0]) || !good_len(p.n[1]) || !good_len(p.n[2]) || p.n[2] < 2 ||
+      p.n[2] % 2) {
+    set_error("grid %dx%dx%d not supported (extents 2^a 3^b, fastest even; 2D needs n[0] == 1)", p.n[0], p.n[1], p.n[2]);
+    return STZ_ERR_INVALID;
+  }
+  if (!(p.mu > 0) || !(p.temperature > 0)) { set_error("mu and temperature must be positive"); return STZ_ERR_INVALID; }
+  if (!ref2d && p.softening) { set_error("softening is implemented for the reference 2D model only"); return STZ_ERR_UNSUPPORTED; }
+  const bool mixed = p.precision == STZ_PREC_MIXED;
+  if (mixed && ref2d) { set_error("the mixed form is implemented for the 3D model"); return STZ_ERR_UNSUPPORTED; }
+  int solver = p.solver;
+  if (solver == STZ_SOLVER_AUTO) solver = mixed ? STZ_SOLVER_KERNEL : STZ_SOLVER_FFT;
+  if (mixed && solver != STZ_SOLVER_KERNEL) { set_error("the mixed form uses the incremental (kernel) solver"); return STZ_ERR_UNSUPPORTED; }
+  if (!mixed && solver != STZ_SOLVER_FFT) { set_error("the FP64 forms use the FFT solver"); return STZ_ERR_UNSUPPORTED; }
+
+  stz_ctx* c = new stz_ctx();
+  c->p = p;
+  c->p.solver = solver;
+  int st = STZ_OK;
+  KParams& kp = c->kp;
+  Fields& f = c->f;
+  if (cudaSetDevice(p.device) != cudaSuccess) { set_error("cudaSetDevice(%d) failed", p.device); delete c; return STZ_ERR_CUDA; }
+  cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  cudaEventCreate(&c->kev0);
+  cudaEventCreate(&c->kev1);
+
+  kp.model = p.model;
+  kp.nc = ref2d ? 3 : 6;
+  kp.n0 = p.n[0]; kp.n1 = p.n[1]; kp.n2 = p.n[2];
+  kp.nh = kp.n2 / 2 + 1;
+  kp.N = (long long)kp.n0 * kp.n1 * kp.n2;
+  kp.Nk = (long long)kp.n0 * kp.n1 * kp.nh;
+  const int spt = mixed ? 8 : 4;
+  kp.bsites = kRateThreads * spt;
+  kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
+  kp.loading = p.loading;
+  kp.softening = p.softening;
+  kp.sf_scheme = p.sf_scheme;
+  kp.no_subtract_error = p.no_subtract_error;
+  kp.shear_quirk = p.shear_elastic_quirk;
+  kp.lambda = p.lambda; kp.mu = p.mu; kp.young = p.young; kp.poisson = p.poisson;
+  kp.kT = p.temperature * kBoltz * kJInEv;
+  kp.vt = p.voxel_volume * p.trial_frequency;
+  kp.V0 = p.voxel_volume;
+  kp.dt = p.strain_rate > 0 ? p.strain_increment / p.strain_rate : INFINITY;
+  kp.gamma0 = p.gamma0;
+  kp.perm_soft = p.perm_soft; kp.temp_soft = p.temp_soft; kp.perm_soft_cap = p.perm_soft_cap; kp.t_temp = p.t_temp;
+  kp.end_strain = p.end_strain;
+  kp.strain_rate = p.strain_rate;
+  kp.strain_increment = p.strain_increment;
+  kp.print_thr = p.print_period * p.strain_increment * 0.99;
+  for (int i = 0; i < 6; i++) kp.applied[i] = p.applied_stress[i];
+  kp.kt0 = kp.n0 / 2 + 1; kp.kt1 = kp.n1 / 2 + 1; kp.kt2 = kp.n2 / 2 + 1;
+  kp.log_cap = 1 << 20;
+  kp.resolve_period = mixed ? p.resolve_period : 0;
+
+  const long long N = kp.N;
+  const int nc = kp.nc;
+  auto fail = [&](int code) {
+    stz_destroy(c);
+    return code;
+  };
+  if ((st = dalloc(&f.ctl, 1))) return fail(st);
+  if ((st = dalloc(&f.eps0, (size_t)nc * N))) return fail(st);
+  if ((st = dalloc(&f.prev_deps, (size_t)nc * N))) return fail(st);
+  if ((st = dalloc(&f.amark, (size_t)N))) return fail(st);
+  if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
+  if ((st = dalloc(&f.log, (size_t)kp.log_cap))) return fail(st);
+  if ((st = dalloc(&c->err_dev, 3))) return fail(st);
+  {
+    double2* sp = nullptr;
+    if ((st = dalloc(&sp, (size_t)nc * kp.Nk))) return fail(st);
+    f.spec = sp;
+  }
+  // scratch for error statistics nobody reads (3 doubles)
+  if ((st = dalloc(&f.scratch, 8))) return fail(st);
+  if (mixed) {
+    if ((st = dalloc(&f.sdev, (size_t)5 * N))) return fail(st);
+    if ((st = dalloc(&f.dF32, (size_t)N))) return fail(st);
+  } else {
+    if ((st = dalloc(&f.sig, (size_t)nc * N))) return fail(st);
+  }
+  if (ref2d) {
+    if ((st = dalloc(&f.Q0, (size_t)STZ_MODES * N))) return fail(st);
+    if ((st = dalloc(&f.deps, (size_t)STZ_MODES * 3 * N))) return fail(st);
+    if ((st = dalloc(&f.perm_soft, (size_t)N))) return fail(st);
+    if ((st = dalloc(&f.temp_soft, (size_t)N))) return fail(st);
+    if ((st = dalloc(&f.tlast, (size_t)N))) return fail(st);
+  } else {
+    if ((st = dalloc(&f.dF, (size_t)N))) return fail(st);
+  }
+  FFTPlan* plan = new FFTPlan();
+  c->fft = plan;
+  if ((st = fft_plan_create(plan, kp.n0, kp.n1, kp.n2, nc))) {
+    set_error("FFT plan for %dx%dx%d failed", kp.n0, kp.n1, kp.n2);
+    return fail(st);
+  }
+  MT rng;
+  mt_seed(&rng, (unsigned long)p.seed);
+  st = ref2d ? init_ref2d(c, &rng) : init_global3d(c, &rng);
+  if (st) return fail(st);
+  if (mixed) mixed_constants(c);
+
+  // control block
+  Ctl& h = c->host_ctl;
+  std::memset(&h, 0, sizeof(h));
+  h.rng = rng;
+  h.step_kind = kNone;
+  h.max_kstep = -1;
+  h.max_step = -1;
+  h.next_resolve = kp.resolve_period > 0 ? kp.resolve_period : 0;
+  if (p.loading == STZ_LOAD_STRESS) host_iso_inv(kp, p.applied_stress, h.eps_avg);
+  for (int i = 0; i < 6; i++) h.eps_avg_applied[i] = h.eps_avg[i];
+  {
+    // mean stress of the initial solve: C:(eps_avg - 0)
+    double e[6];
+    for (int i = 0; i < 6; i++) e[i] = h.eps_avg[i];
+    const int nd = nc == 3 ? 2 : 3;
+    double tr = 0;
+    for (int i = 0; i < nd; i++) tr += e[i];
+    for (int i = 0; i < nc; i++) h.stress[i] = (i < nd ? kp.lambda * tr : 0.0) + 2.0 * kp.mu * e[i];
+  }
+  if (cudaMemcpy(f.ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("control block upload failed");
+    return fail(STZ_ERR_CUDA);
+  }
+  // initial solve (bmg.c:117-124)
+  if (mixed) {
+    if ((st = build_response_table(c))) return fail(st);
+    solve_dev(c, f.ctl->eps_avg, nullptr, f.scratch);
+  } else {
+    solve_plain(c, nullptr, f.ctl->eps_avg);
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    set_error("initial solve failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(STZ_ERR_CUDA);
+  }
+  // L2 flush buffer (larger than the 126 MB L2)
+  c->l2flush_bytes = (size_t)256 << 20;
+  if (cudaMalloc(&c->l2buf, c->l2flush_bytes) != cudaSuccess) { c->l2buf = nullptr; c->l2flush_bytes = 0; }
+  c->launches = 0;
+  *out = c;
+  return STZ_OK;
+}
+
+extern "C" void stz_destroy(stz_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->p.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  Fields& f = c->f;
+  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
+                  f.tlast, f.amark, f.part, f.spec, f.ktab, f.log, f.ctl, f.scratch, c->err_dev, c->l2buf};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->fft) {
+    fft_plan_destroy(plan_of(c));
+    delete plan_of(c);
+  }
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->kev0) cudaEventDestroy(c->kev0);
+  if (c->kev1) cudaEventDestroy(c->kev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" int stz_run(stz_ctx* c, int64_t max_steps, int64_t max_events) {
+  if (!c) return STZ_ERR_INVALID;
+  int st;
+  cudaSetDevice(c->p.device);
+  if ((st = sync_ctl(c))) return st;
+  Ctl& h = c->host_ctl;
+  if (h.status) return h.status;
+  const long long tk = max_events > 0 ? h.kstep + max_events : -1;
+  const long long ts = max_steps > 0 ? h.step + max_steps : -1;
+  if ((st = set_targets(c, tk, ts))) return st;
+  const bool mixed = c->f.sdev != nullptr;
+  const int batch = mixed ? 64 : 16;
+  if (c->use_graph && (st = capture_plain_graph(c, batch))) return st;
+  for (;;) {
+    if (c->use_graph) {
+      if (cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) {
+        set_error("graph launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return STZ_ERR_CUDA;
+      }
+      c->launches += c->graph_launches;
+    } else {
+      for (int i = 0; i < batch; i++) {
+        if (mixed) { launch_mixed(c->kp, c->f, 0, c->stream); c->launches += 1; }
+        else enqueue_plain_step(c);
+      }
+    }
+    if ((st = sync_ctl(c))) return st;
+    if ((st = drain_log(c))) return st;
+    if (h.status) { set_error("device reported status %d", h.status); return h.status; }
+    if (mixed && h.halt) {
+      int done = 0;
+      if ((st = mixed_service(c, &done))) return st;
+      if ((st = drain_log(c))) return st;
+      if (done) break;
+      continue;
+    }
+    if (h.halt) break;
+  }
+  return h.status;
+}
+
+extern "C" int stz_solve(stz_ctx* c) {
+  if (!c) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  if (c->f.sdev) {
+    solve_dev(c, c->f.ctl->eps_avg, nullptr, c->f.scratch);
+    launch_mixed_after_resolve(c->kp, c->f, 0, c->stream);
+  } else {
+    solve_plain(c, nullptr, c->f.ctl->eps_avg);
+    double z[6] = {0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(c->f.ctl->u, z, sizeof(z), cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+extern "C" int stz_get_scalars(stz_ctx* c, stz_scalars* o) {
+  if (!c || !o) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  int st = sync_ctl(c);
+  if (st) return st;
+  const Ctl& h = c->host_ctl;
+  std::memset(o, 0, sizeof(*o));
+  o->time = h.totime;
+  for (int i = 0; i < 6; i++) {
+    o->eps_avg[i] = h.eps_avg[i];
+    o->stress[i] = h.stress[i];
+    o->eps0_avg[i] = h.eps0_sum[i] / (double)c->kp.N;
+  }
+  o->step = h.step; o->kstep = h.kstep; o->astep = h.astep; o->estep = h.estep;
+  o->n_print = h.n_print;
+  o->n_events_logged = (int64_t)c->host_log.size();
+  o->stopped = h.stopped;
+  o->status = h.status;
+  o->stress_err_max = c->err_max;
+  o->stress_err_rms = c->err_rms;
+  o->near_ties = h.near_ties;
+  o->reserved[0] = h.nlog_dropped;
+  return STZ_OK;
+}
+
+extern "C" int stz_get_events(stz_ctx* c, int64_t first, stz_event* out, int64_t cap, int64_t* n) {
+  if (!c || (!out && cap > 0)) return STZ_ERR_INVALID;
+  int64_t k = 0;
+  for (int64_t i = first; i < (int64_t)c->host_log.size() && k < cap; i++) out[k++] = c->host_log[(size_t)i];
+  if (n) *n = k;
+  return STZ_OK;
+}
+
+static int field_ptr(stz_ctx* c, int which, int comp, double** d64, float** d32) {
+  const long long N = c->kp.N;
+  const int nc = c->kp.nc;
+  Fields& f = c->f;
+  *d64 = nullptr;
+  *d32 = nullptr;
+  switch (which) {
+    case STZ_FIELD_SIGMA:
+      if (comp < 0 || comp >= nc || !f.sig) return STZ_ERR_INVALID;
+      *d64 = f.sig + (size_t)comp * N;
+      return STZ_OK;
+    case STZ_FIELD_EPS0:
+      if (comp < 0 || comp >= nc) return STZ_ERR_INVALID;
+      *d64 = f.eps0 + (size_t)comp * N;
+      return STZ_OK;
+    case STZ_FIELD_DF:
+      if (f.Q0) {
+        if (comp < 0 || comp >= STZ_MODES) return STZ_ERR_INVALID;
+        *d64 = f.Q0 + (size_t)comp * N;
+      } else {
+        if (comp != 0) return STZ_ERR_INVALID;
+        *d64 = f.dF;
+      }
+      return STZ_OK;
+    case STZ_FIELD_DEPS:
+      if (!f.deps || comp < 0 || comp >= 3 * STZ_MODES) return STZ_ERR_INVALID;
+      *d64 = f.deps + (size_t)comp * N;
+      return STZ_OK;
+    case STZ_FIELD_TLAST: *d64 = f.tlast; return f.tlast ? STZ_OK : STZ_ERR_INVALID;
+    case STZ_FIELD_PERM_SOFT: *d64 = f.perm_soft; return f.perm_soft ? STZ_OK : STZ_ERR_INVALID;
+    case STZ_FIELD_TEMP_SOFT: *d64 = f.temp_soft; return f.temp_soft ? STZ_OK : STZ_ERR_INVALID;
+    case STZ_FIELD_PREV_DEPS:
+      if (comp < 0 || comp >= nc) return STZ_ERR_INVALID;
+      *d64 = f.prev_deps + (size_t)comp * N;
+      return STZ_OK;
+  }
+  return STZ_ERR_INVALID;
+}
+
+extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* host, int64_t count) {
+  if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  const long long N = c->kp.N;
+  if (which == STZ_FIELD_Q) {
+    if (comp < 0 || comp >= STZ_MODES) return STZ_ERR_INVALID;
+    double* tmp = nullptr;
+    if (dalloc(&tmp, (size_t)N)) return STZ_ERR_NOMEM;
+    launch_q_mode(c->kp, c->f, comp, tmp, c->stream);
+    cudaMemcpyAsync(host, tmp, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    return STZ_OK;
+  }
+  if (which == STZ_FIELD_SIGMA && c->f.sdev) {
+    // mixed form: the full field comes from an FP64 solve of the current state
+    // (the stored FP32 field holds only the deviatoric coordinates)
+    double* tmp = nullptr;
+    if (dalloc(&tmp, (size_t)6 * N)) return STZ_ERR_NOMEM;
+    SolveArgs a{};
+    a.eps = c->f.eps0;
+    a.ebar = c->f.ctl->eps_avg_applied;
+    a.lambda = c->kp.lambda;
+    a.mu = c->kp.mu;
+    a.out = kOutSig64;
+    a.sig64 = tmp;
+    a.spec = c->f.spec;
+    fft_solve(*plan_of(c), a, c->stream, nullptr);
+    cudaMemcpyAsync(host, tmp + (size_t)comp * N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(tmp);
+    sync_ctl(c);
+    for (long long s = 0; s < N; s++) host[s] += c->host_ctl.u[comp];
+    return STZ_OK;
+  }
+  double* d64;
+  float* d32;
+  int st = field_ptr(c, which, comp, &d64, &d32);
+  if (st) return st;
+  CK(cudaMemcpyAsync(host, d64, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (which == STZ_FIELD_SIGMA) {
+    sync_ctl(c);
+    for (long long s = 0; s < N; s++) host[s] += c->host_ctl.u[comp];
+  }
+  return STZ_OK;
+}
+
+extern "C" int stz_set_field(stz_ctx* c, int32_t which, int32_t comp, const double* host, int64_t count) {
+  if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  double* d64;
+  float* d32;
+  int st = field_ptr(c, which, comp, &d64, &d32);
+  if (st) return st;
+  CK(cudaMemcpyAsync(d64, host, sizeof(double) * c->kp.N, cudaMemcpyHostToDevice, c->stream));
+  if (which == STZ_FIELD_DF && c->f.dF32) launch_fill_f32(c->f.dF, c->f.dF32, c->kp.N, c->stream);
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+extern "C" int stz_elastic_energy(stz_ctx* c, double* out) {
+  if (!c || !out) return STZ_ERR_INVALID;
+  const long long N = c->kp.N;
+  const int nc = c->kp.nc;
+  std::vector<double> sig((size_t)nc * N);
+  for (int comp = 0; comp < nc; comp++) {
+    int st = stz_get_field(c, STZ_FIELD_SIGMA, comp, sig.data() + (size_t)comp * N, N);
+    if (st) return st;
+  }
+  // ElasticEnergy (elastic.c:533-547)
+  double e = 0;
+  for (long long s = 0; s < N; s++) {
+    double sg[6] = {0, 0, 0, 0, 0, 0}, el[6];
+    for (int comp = 0; comp < nc; comp++) sg[comp] = sig[(size_t)comp * N + s];
+    host_iso_inv(c->kp, sg, el);
+    double acc = 0;
+    for (int comp = 0; comp < nc; comp++) acc += ((nc == 3 ? comp == 2 : comp >= 3) ? 2.0 : 1.0) * sg[comp] * el[comp];
+    e += 0.5 * acc;
+  }
+  *out = e;
+  return STZ_OK;
+}
+
+extern "C" int stz_sync(stz_ctx* c) {
+  if (!c) return STZ_ERR_INVALID;
+  CK(cudaStreamSynchronize(c->stream));
+  return STZ_OK;
+}
+
+extern "C" int stz_timer_start(stz_ctx* c) {
+  if (!c) return STZ_ERR_INVALID;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  return STZ_OK;
+}
+
+extern "C" int stz_timer_stop(stz_ctx* c, float* ms) {
+  if (!c || !ms) return STZ_ERR_INVALID;
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaEventSynchronize(c->ev1));
+  CK(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+  return STZ_OK;
+}
+
+extern "C" int stz_flush_l2(stz_ctx* c) {
+  if (!c) return STZ_ERR_INVALID;
+  if (!c->l2buf) return STZ_ERR_NOMEM;
+  launch_l2_flush(c->l2buf, c->l2flush_bytes, c->stream);
+  c->launches += 1;
+  return STZ_OK;
+}
+
+extern "C" int64_t stz_kernel_launches(stz_ctx* c) { return c ? c->launches : 0; }
+
+// Average device time of the per-step kernel: runs `steps` steps launching
+// that kernel directly between CUDA events (no graph), on the context's
+// stream. which = 0: the per-step rate/update kernel.
+extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_t* launches) {
+  if (!c || !ms_avg) return STZ_ERR_INVALID;
+  (void)which;
+  cudaSetDevice(c->p.device);
+  int st = sync_ctl(c);
+  if (st) return st;
+  const int steps = launches && *launches > 0 ? (int)*launches : 64;
+  const bool mixed = c->f.sdev != nullptr;
+  if (!mixed) {
+    *ms_avg = 0;
+    return STZ_ERR_UNSUPPORTED;
+  }
+  // run on a private copy of the targets: the kernel halts on its own rules
+  Ctl& h = c->host_ctl;
+  if ((st = set_targets(c, h.kstep + steps, -1))) return st;
+  double tot = 0;
+  int n = 0;
+  for (int i = 0; i < steps; i++) {
+    CK(cudaEventRecord(c->kev0, c->stream));
+    launch_mixed(c->kp, c->f, 0, c->stream);
+    CK(cudaEventRecord(c->kev1, c->stream));
+    CK(cudaEventSynchronize(c->kev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->kev0, c->kev1));
+    if ((st = sync_ctl(c))) return st;
+    if ((st = drain_log(c))) return st;
+    if (h.halt) {
+      int done = 0;
+      if ((st = mixed_service(c, &done))) return st;
+      drain_log(c);
+      if (done) break;
+      continue;  // a serviced step is not a plain launch; do not time it
+    }
+    tot += ms;
+    n++;
+  }
+  c->launches += steps;
+  *ms_avg = n ? tot / n : 0;
+  if (launches) *launches = n;
+  return STZ_OK;
+}

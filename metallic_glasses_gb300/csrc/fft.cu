@@ -1,0 +1,687 @@
+// fft.cu -- hand-written mixed-radix FFT and the fused Green's-operator pass.
+//
+// Layout: a real field is [N] with s = (i0*n1 + i1)*n2 + i2; its half
+// spectrum is [n0][n1][nh] complex with nh = n2/2 + 1 (R2C along axis 2).
+// A 3D solve is five passes:
+//   R2C along axis 2  ->  C2C along axis 1  ->  [C2C axis 0, Green, inverse C2C
+//   axis 0] in one kernel  ->  inverse C2C along axis 1  ->  C2R along axis 2
+// and a 2D solve (n0 == 1) three: R2C axis 2 -> [axis 1, Green, inverse] -> C2R.
+// Every pass stages a tile of lines in shared memory and runs a Stockham
+// autosort FFT over it with radix-8/4/3/2 butterflies in registers.
+//
+// Green's operator (elastic.c:802-809, generalised to 3D): with g the unit
+// wave vector of Grad() (init.c:112-140; wrap s - round(s), Nyquist -> -1/2),
+// tau = C:eps*, F = tau.g, G = g.F,
+//   eps_ij = (F_i g_j + F_j g_i)/(2 mu) - (alpha/mu) G g_i g_j,
+//   alpha = (lambda + mu)/(lambda + 2 mu),
+// and the pass writes the stress spectrum C:(eps - eps*) directly; the k = 0
+// term is C:(N <eps> - eps*_hat(0)). The reference transforms complex fields
+// and keeps the real part of the inverse; on a Nyquist plane its operator at k
+// and at -k differ (g picks -1/2 for both), so the real part it keeps is the
+// result of the average of the two operators. This pass applies that average
+// explicitly, which keeps the spectrum Hermitian and the C2R exact.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "fft.cuh"
+
+namespace stz {
+namespace {
+
+template <typename T> struct VT;
+template <> struct VT<double> { using V = double2; };
+template <> struct VT<float> { using V = float2; };
+
+template <typename V> __device__ __forceinline__ V vadd(V a, V b) { return V{a.x + b.x, a.y + b.y}; }
+template <typename V> __device__ __forceinline__ V vsub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
+template <typename V> __device__ __forceinline__ V vmul(V a, V b) {
+  return V{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// S * i * a
+template <int S, typename V> __device__ __forceinline__ V vmuli(V a) {
+  return S > 0 ? V{-a.y, a.x} : V{a.y, -a.x};
+}
+
+template <typename V, int S> __device__ __forceinline__ void dft2(V* v) {
+  V a = v[0], b = v[1];
+  v[0] = vadd(a, b);
+  v[1] = vsub(a, b);
+}
+template <typename V, int S> __device__ __forceinline__ void dft4(V* v) {
+  V a0 = vadd(v[0], v[2]), a1 = vsub(v[0], v[2]);
+  V a2 = vadd(v[1], v[3]), a3 = vsub(v[1], v[3]);
+  V b3 = vmuli<S>(a3);
+  v[0] = vadd(a0, a2);
+  v[2] = vsub(a0, a2);
+  v[1] = vadd(a1, b3);
+  v[3] = vsub(a1, b3);
+}
+template <typename V, int S> __device__ __forceinline__ void dft3(V* v) {
+  using T = decltype(v[0].x);
+  const T c = (T)-0.5;
+  const T s = (T)(S * 0.86602540378443864676);
+  V t = vadd(v[1], v[2]), u = vsub(v[1], v[2]);
+  V y0 = vadd(v[0], t);
+  V m = V{v[0].x + c * t.x, v[0].y + c * t.y};
+  V q = V{-s * u.y, s * u.x};
+  v[0] = y0;
+  v[1] = vadd(m, q);
+  v[2] = vsub(m, q);
+}
+template <typename V, int S> __device__ __forceinline__ void dft8(V* v) {
+  using T = decltype(v[0].x);
+  const T r = (T)0.70710678118654752440;
+  V e[4] = {v[0], v[2], v[4], v[6]};
+  V o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<V, S>(e);
+  dft4<V, S>(o);
+  o[1] = V{r * (o[1].x - S * o[1].y), r * (S * o[1].x + o[1].y)};
+  o[2] = vmuli<S>(o[2]);
+  o[3] = V{r * (-o[3].x - S * o[3].y), r * (S * o[3].x - o[3].y)};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    v[k] = vadd(e[k], o[k]);
+    v[k + 4] = vsub(e[k], o[k]);
+  }
+}
+
+template <typename V, int R, int S>
+__device__ __forceinline__ void stage(const V* __restrict__ src, V* __restrict__ dst, int n, int L, int ld,
+                                      int ns, const V* __restrict__ tw, int tid, int nth) {
+  const int m = n / R;
+  const int step = n / (ns * R);
+  const int total = L * m;
+  for (int idx = tid; idx < total; idx += nth) {
+    const int line = idx / m;
+    const int j = idx - line * m;
+    const int jm = j % ns;
+    const V* s = src + line * ld;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = s[j + r * m];
+    if (jm != 0) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        V w = tw[jm * r * step];
+        if (S > 0) w.y = -w.y;
+        v[r] = vmul(v[r], w);
+      }
+    }
+    if (R == 2) dft2<V, S>(v);
+    else if (R == 3) dft3<V, S>(v);
+    else if (R == 4) dft4<V, S>(v);
+    else dft8<V, S>(v);
+    V* d = dst + line * ld;
+    const int base = (j / ns) * ns * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[base + r * ns] = v[r];
+  }
+}
+
+// FFT of L lines of length sc.n stored with leading dimension ld in a; b is
+// scratch of the same size. Returns the buffer that holds the result. Must be
+// called by the whole block with the input visible (after __syncthreads).
+template <typename V, int S>
+__device__ V* fft_lines(V* a, V* b, int L, int ld, const Sched& sc, const V* tw) {
+  V* src = a;
+  V* dst = b;
+  int ns = 1;
+  for (int s = 0; s < sc.nst; s++) {
+    const int R = sc.r[s];
+    if (R == 8) stage<V, 8, S>(src, dst, sc.n, L, ld, ns, tw, threadIdx.x, blockDim.x);
+    else if (R == 4) stage<V, 4, S>(src, dst, sc.n, L, ld, ns, tw, threadIdx.x, blockDim.x);
+    else if (R == 3) stage<V, 3, S>(src, dst, sc.n, L, ld, ns, tw, threadIdx.x, blockDim.x);
+    else stage<V, 2, S>(src, dst, sc.n, L, ld, ns, tw, threadIdx.x, blockDim.x);
+    __syncthreads();
+    V* t = src;
+    src = dst;
+    dst = t;
+    ns *= R;
+  }
+  return src;
+}
+
+// ---------------------------------------------------------------- R2C, axis 2
+template <typename T>
+__global__ void __launch_bounds__(256) k_r2c_x(const double* __restrict__ in, typename VT<T>::V* __restrict__ out,
+                                               int n2, int h, int nh, long long rows, long long N, long long Nk,
+                                               int L, Sched sh, const typename VT<T>::V* __restrict__ tw_h,
+                                               const typename VT<T>::V* __restrict__ tw_p, const int* gate) {
+  using V = typename VT<T>::V;
+  if (gate && *gate == 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ld = h + 1;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + L * ld;
+  const int c = blockIdx.y;
+  const long long r0 = (long long)blockIdx.x * L;
+  const double2* src = reinterpret_cast<const double2*>(in + (long long)c * N);
+  for (int idx = threadIdx.x; idx < L * h; idx += blockDim.x) {
+    const int l = idx / h, j = idx - l * h;
+    const long long r = r0 + l;
+    V z = V{0, 0};
+    if (r < rows) {
+      double2 v = src[(r * n2) / 2 + j];
+      z = V{(T)v.x, (T)v.y};
+    }
+    a[l * ld + j] = z;
+  }
+  __syncthreads();
+  V* res = fft_lines<V, -1>(a, b, L, ld, sh, tw_h);
+  V* dst = out + (long long)c * Nk;
+  for (int idx = threadIdx.x; idx < L * nh; idx += blockDim.x) {
+    const int l = idx / nh, k = idx - l * nh;
+    const long long r = r0 + l;
+    if (r >= rows) continue;
+    V zk = res[l * ld + (k == h ? 0 : k)];
+    V zc = res[l * ld + (k == 0 ? 0 : h - k)];
+    zc.y = -zc.y;
+    V sum = vadd(zk, zc), dif = vsub(zk, zc);
+    V wd = vmul(tw_p[k], dif);
+    dst[r * nh + k] = V{(T)0.5 * (sum.x + wd.y), (T)0.5 * (sum.y - wd.x)};
+  }
+}
+
+// ------------------------------------------------------- C2C along axis 1 / 0
+template <typename T, int S>
+__global__ void __launch_bounds__(256) k_c2c_axis(typename VT<T>::V* __restrict__ data, int n, long long stride,
+                                                  long long inner, long long outer_stride, int ntile,
+                                                  long long Nk, int L, Sched sc,
+                                                  const typename VT<T>::V* __restrict__ tw, const int* gate) {
+  using V = typename VT<T>::V;
+  if (gate && *gate == 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ld = n + 1;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + L * ld;
+  const int c = blockIdx.y;
+  const long long o = blockIdx.x / ntile;
+  const long long q0 = (long long)(blockIdx.x % ntile) * L;
+  V* base = data + (long long)c * Nk + o * outer_stride;
+  for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
+    const int p = idx / L, l = idx - p * L;
+    const long long q = q0 + l;
+    a[l * ld + p] = q < inner ? base[p * stride + q] : V{0, 0};
+  }
+  __syncthreads();
+  V* res = fft_lines<V, S>(a, b, L, ld, sc, tw);
+  for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
+    const int p = idx / L, l = idx - p * L;
+    const long long q = q0 + l;
+    if (q < inner) base[p * stride + q] = res[l * ld + p];
+  }
+}
+
+// ------------------------------------------------------------- Green's pass
+struct GreenArgs {
+  int nc, is3d, n0, n1, n2, nh;
+  double lambda, mu;
+  double Ntot;
+};
+
+// stress = C:(e), Voigt with tensor shear; nc = 3 (xx yy xy) or 6 (xx yy zz yz xz xy)
+template <typename T, typename V>
+__device__ __forceinline__ void apply_C(int nc, T lam, T mu, const V* e, V* out) {
+  const int nd = nc == 3 ? 2 : 3;
+  V tr = V{0, 0};
+  for (int c = 0; c < nd; c++) tr = vadd(tr, e[c]);
+  for (int c = 0; c < nc; c++) {
+    V v = V{(T)2 * mu * e[c].x, (T)2 * mu * e[c].y};
+    if (c < nd) v = V{v.x + lam * tr.x, v.y + lam * tr.y};
+    out[c] = v;
+  }
+}
+
+// sigma_hat = C:(Gamma(g):C:e - e) for one unit wave vector g (x, y, z)
+template <typename T, typename V>
+__device__ __forceinline__ void green_op(int nc, T lam, T mu, T alpha, const T* g, const V* e, V* sig) {
+  V tau[6];
+  apply_C<T, V>(nc, lam, mu, e, tau);
+  // tensor form of tau
+  V t[3][3];
+  if (nc == 3) {
+    t[0][0] = tau[0]; t[1][1] = tau[1]; t[0][1] = t[1][0] = tau[2];
+    t[2][2] = t[0][2] = t[2][0] = t[1][2] = t[2][1] = V{0, 0};
+  } else {
+    t[0][0] = tau[0]; t[1][1] = tau[1]; t[2][2] = tau[2];
+    t[1][2] = t[2][1] = tau[3];
+    t[0][2] = t[2][0] = tau[4];
+    t[0][1] = t[1][0] = tau[5];
+  }
+  V F[3];
+  for (int a = 0; a < 3; a++) {
+    F[a] = V{t[a][0].x * g[0] + t[a][1].x * g[1] + t[a][2].x * g[2],
+             t[a][0].y * g[0] + t[a][1].y * g[1] + t[a][2].y * g[2]};
+  }
+  V G = V{g[0] * F[0].x + g[1] * F[1].x + g[2] * F[2].x, g[0] * F[0].y + g[1] * F[1].y + g[2] * F[2].y};
+  const T h = (T)0.5 / mu, am = -alpha / mu;
+  const int ia3[6] = {0, 1, 2, 1, 0, 0}, ib3[6] = {0, 1, 2, 2, 2, 1};
+  const int ia2[3] = {0, 1, 0}, ib2[3] = {0, 1, 1};
+  V d[6];
+  for (int c = 0; c < nc; c++) {
+    const int a = nc == 3 ? ia2[c] : ia3[c];
+    const int b = nc == 3 ? ib2[c] : ib3[c];
+    const T gg = g[a] * g[b];
+    V ep = V{h * (F[a].x * g[b] + F[b].x * g[a]) + am * (G.x * gg),
+             h * (F[a].y * g[b] + F[b].y * g[a]) + am * (G.y * gg)};
+    d[c] = vsub(ep, e[c]);
+  }
+  apply_C<T, V>(nc, lam, mu, d, sig);
+}
+
+__device__ __forceinline__ double wrapf(int k, int n) {
+  double s = (double)k * (1.0 / n);
+  return s - round(s);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ spec, int n, long long stride,
+                                               long long inner, long long Nk, int L, Sched sc,
+                                               const typename VT<T>::V* __restrict__ tw, GreenArgs ga,
+                                               const double* __restrict__ ebar, const int* gate) {
+  using V = typename VT<T>::V;
+  if (gate && *gate == 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nc = ga.nc;
+  const int ld = n + 1;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + nc * L * ld;
+  const long long q0 = (long long)blockIdx.x * L;
+  for (int idx = threadIdx.x; idx < nc * n * L; idx += blockDim.x) {
+    const int c = idx / (n * L);
+    const int rem = idx - c * n * L;
+    const int p = rem / L, l = rem - p * L;
+    const long long q = q0 + l;
+    a[(c * L + l) * ld + p] = q < inner ? spec[c * Nk + p * stride + q] : V{0, 0};
+  }
+  __syncthreads();
+  V* res = fft_lines<V, -1>(a, b, nc * L, ld, sc, tw);
+  const T lam = (T)ga.lambda, mu = (T)ga.mu;
+  const T alpha = (T)((ga.lambda + ga.mu) / (ga.lambda + 2.0 * ga.mu));
+  for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
+    const int p = idx / L, l = idx - p * L;
+    const long long q = q0 + l;
+    if (q >= inner) continue;
+    int k0, k1, k2;
+    if (ga.is3d) {
+      k0 = p;
+      k1 = (int)(q / ga.nh);
+      k2 = (int)(q - (long long)k1 * ga.nh);
+    } else {
+      k0 = 0;
+      k1 = p;
+      k2 = (int)q;
+    }
+    V e[6], sig[6];
+    for (int c = 0; c < nc; c++) e[c] = res[(c * L + l) * ld + p];
+    if (k0 == 0 && k1 == 0 && k2 == 0) {
+      V d[6];
+      for (int c = 0; c < nc; c++) {
+        const T eb = ebar ? (T)(ga.Ntot * ebar[c]) : (T)0;
+        d[c] = V{eb - e[c].x, -e[c].y};
+      }
+      apply_C<T, V>(nc, lam, mu, d, sig);
+    } else {
+      const double f2 = wrapf(k2, ga.n2), f1 = wrapf(k1, ga.n1), f0 = ga.is3d ? wrapf(k0, ga.n0) : 0.0;
+      const double gn = sqrt(f2 * f2 + f1 * f1 + f0 * f0);
+      T g[3] = {(T)(f2 / gn), (T)(f1 / gn), (T)(f0 / gn)};
+      const bool ny2 = (ga.n2 % 2 == 0) && (2 * k2 == ga.n2);
+      const bool ny1 = (ga.n1 % 2 == 0) && (2 * k1 == ga.n1);
+      const bool ny0 = ga.is3d && (ga.n0 % 2 == 0) && (2 * k0 == ga.n0);
+      green_op<T, V>(nc, lam, mu, alpha, g, e, sig);
+      if (ny2 || ny1 || ny0) {
+        T gm[3] = {ny2 ? -g[0] : g[0], ny1 ? -g[1] : g[1], ny0 ? -g[2] : g[2]};
+        V s2[6];
+        green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
+        for (int c = 0; c < nc; c++) sig[c] = V{(T)0.5 * (sig[c].x + s2[c].x), (T)0.5 * (sig[c].y + s2[c].y)};
+      }
+    }
+    for (int c = 0; c < nc; c++) res[(c * L + l) * ld + p] = sig[c];
+  }
+  __syncthreads();
+  V* other = (res == a) ? b : a;
+  V* res2 = fft_lines<V, +1>(res, other, nc * L, ld, sc, tw);
+  for (int idx = threadIdx.x; idx < nc * n * L; idx += blockDim.x) {
+    const int c = idx / (n * L);
+    const int rem = idx - c * n * L;
+    const int p = rem / L, l = rem - p * L;
+    const long long q = q0 + l;
+    if (q < inner) spec[c * Nk + p * stride + q] = res2[(c * L + l) * ld + p];
+  }
+}
+
+// ---------------------------------------------------------------- C2R, axis 2
+// Deviatoric coordinates of a Voigt stress (tensor shear) in the orthonormal
+// basis (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2*yz, sqrt2*xz, sqrt2*xy.
+__device__ __forceinline__ void dev_coords(const double* s, double* d) {
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, s2 = 1.41421356237309504880;
+  d[0] = (s[0] - s[1]) * r2;
+  d[1] = (2.0 * s[2] - s[0] - s[1]) * r6;
+  d[2] = s2 * s[3];
+  d[3] = s2 * s[4];
+  d[4] = s2 * s[5];
+}
+
+template <typename T, int OUT>
+__global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restrict__ in, int nc, int n2, int h,
+                                               int nh, long long rows, long long N, long long Nk, int L, Sched sh,
+                                               const typename VT<T>::V* __restrict__ tw_h,
+                                               const typename VT<T>::V* __restrict__ tw_p, double invN,
+                                               double* __restrict__ sig64, float* __restrict__ sig32,
+                                               float* __restrict__ sdev, const double* __restrict__ uadd,
+                                               double* __restrict__ err, const int* gate) {
+  using V = typename VT<T>::V;
+  if (gate && *gate == 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ld = h + 2;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + L * ld;
+  double* o = reinterpret_cast<double*>(b + L * ld);  // [nc][L][n2] for the deviatoric epilogue
+  const long long r0 = (long long)blockIdx.x * L;
+  for (int c = 0; c < nc; c++) {
+    const V* src = in + (long long)c * Nk;
+    for (int idx = threadIdx.x; idx < L * nh; idx += blockDim.x) {
+      const int l = idx / nh, k = idx - l * nh;
+      const long long r = r0 + l;
+      a[l * ld + k] = r < rows ? src[r * nh + k] : V{0, 0};
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < L * h; idx += blockDim.x) {
+      const int l = idx / h, k = idx - l * h;
+      V xk = a[l * ld + k];
+      V xc = a[l * ld + (h - k)];
+      xc.y = -xc.y;
+      V e = vadd(xk, xc), d = vsub(xk, xc);
+      V w = tw_p[k];
+      w.y = -w.y;
+      V od = vmul(w, d);
+      // Z = E + i O
+      b[l * ld + k] = V{e.x - od.y, e.y + od.x};
+    }
+    __syncthreads();
+    V* res = fft_lines<V, +1>(b, a, L, ld, sh, tw_h);
+    for (int idx = threadIdx.x; idx < L * h; idx += blockDim.x) {
+      const int l = idx / h, j = idx - l * h;
+      const long long r = r0 + l;
+      if (r >= rows) continue;
+      V z = res[l * ld + j];
+      const double x0 = (double)z.x * invN, x1 = (double)z.y * invN;
+      if (OUT == kOutSig64) {
+        reinterpret_cast<double2*>(sig64 + (long long)c * N)[(r * n2) / 2 + j] = make_double2(x0, x1);
+      } else if (OUT == kOutSig32) {
+        reinterpret_cast<float2*>(sig32 + (long long)c * N)[(r * n2) / 2 + j] = make_float2((float)x0, (float)x1);
+      } else {
+        o[(c * L + l) * n2 + 2 * j] = x0;
+        o[(c * L + l) * n2 + 2 * j + 1] = x1;
+      }
+    }
+    __syncthreads();
+  }
+  if (OUT == kOutDev32) {
+    double mx = 0, ss = 0, sr = 0;
+    for (int idx = threadIdx.x; idx < L * n2; idx += blockDim.x) {
+      const int l = idx / n2, i = idx - l * n2;
+      const long long r = r0 + l;
+      if (r >= rows) continue;
+      const long long s = r * n2 + i;
+      double sv[6], d[5];
+      for (int c = 0; c < 6; c++) sv[c] = o[(c * L + l) * n2 + i] + (uadd ? uadd[c] : 0.0);
+      dev_coords(sv, d);
+      double e2 = 0, n2s = 0;
+      for (int k = 0; k < 5; k++) {
+        const double old = (double)sdev[k * N + s];
+        const double dd = old - d[k];
+        e2 += dd * dd;
+        n2s += d[k] * d[k];
+        sdev[k * N + s] = (float)d[k];
+      }
+      mx = fmax(mx, e2);
+      ss += e2;
+      sr += n2s;
+    }
+    // block reduction
+    for (int off = 16; off > 0; off >>= 1) {
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      ss += __shfl_xor_sync(0xffffffffu, ss, off);
+      sr += __shfl_xor_sync(0xffffffffu, sr, off);
+    }
+    __shared__ double red[3][8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[0][w] = mx; red[1][w] = ss; red[2][w] = sr; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+        mx = fmax(mx, red[0][k]);
+        ss += red[1][k];
+        sr += red[2][k];
+      }
+      // non-negative doubles order like their bit patterns
+      atomicMax(reinterpret_cast<unsigned long long*>(&err[0]), (unsigned long long)__double_as_longlong(mx));
+      atomicAdd(&err[1], ss);
+      atomicAdd(&err[2], sr);
+    }
+  }
+}
+
+// ------------------------------------------------------------ filter (GRF)
+template <typename T>
+__global__ void k_gauss_filter(typename VT<T>::V* spec, int n0, int n1, int n2, int nh, double corr, long long Nk) {
+  using V = typename VT<T>::V;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Nk) return;
+  const int k2 = (int)(i % nh);
+  const int k1 = (int)((i / nh) % n1);
+  const int k0 = (int)(i / ((long long)nh * n1));
+  const double f0 = n0 > 1 ? wrapf(k0, n0) : 0.0, f1 = wrapf(k1, n1), f2 = wrapf(k2, n2);
+  const double k2s = 4 * 3.14159265358979323846 * 3.14159265358979323846 * (f0 * f0 + f1 * f1 + f2 * f2);
+  double w = exp(-0.25 * k2s * corr * corr);
+  if (i == 0) w = 0;
+  V v = spec[i];
+  spec[i] = V{(T)(v.x * w), (T)(v.y * w)};
+}
+
+// ------------------------------------------------------------------- host
+Sched make_sched(int n) {
+  Sched s;
+  s.n = n;
+  int m = n;
+  while (m % 8 == 0 && m > 8) { s.r[s.nst++] = 8; m /= 8; }
+  if (m == 8) { s.r[s.nst++] = 8; m = 1; }
+  while (m % 4 == 0) { s.r[s.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { s.r[s.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { s.r[s.nst++] = 3; m /= 3; }
+  if (m != 1) s.nst = -1;
+  return s;
+}
+
+int upload_twiddles(int n, int count, double2** d64, float2** d32) {
+  std::vector<double2> h(count > 0 ? count : 1);
+  std::vector<float2> hf(h.size());
+  for (int k = 0; k < count; k++) {
+    double ang = -2.0 * M_PI * (double)k / (double)n;
+    h[k] = make_double2(std::cos(ang), std::sin(ang));
+    hf[k] = make_float2((float)h[k].x, (float)h[k].y);
+  }
+  if (cudaMalloc(d64, sizeof(double2) * h.size()) != cudaSuccess) return STZ_ERR_NOMEM;
+  if (cudaMalloc(d32, sizeof(float2) * h.size()) != cudaSuccess) return STZ_ERR_NOMEM;
+  cudaMemcpy(*d64, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(*d32, hf.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
+  return STZ_OK;
+}
+
+template <typename T>
+void set_smem_attrs(size_t sx, size_t sy, size_t sg, size_t sc) {
+  cudaFuncSetAttribute(k_r2c_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
+  cudaFuncSetAttribute(k_c2c_axis<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy);
+  cudaFuncSetAttribute(k_c2c_axis<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy);
+  cudaFuncSetAttribute(k_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sg);
+  cudaFuncSetAttribute(k_c2r_x<T, kOutSig64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
+  cudaFuncSetAttribute(k_c2r_x<T, kOutSig32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
+  cudaFuncSetAttribute(k_c2r_x<T, kOutDev32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
+}
+
+template <typename T>
+struct Tw;
+template <>
+struct Tw<double> {
+  static const double2* h(const FFTPlan& p) { return p.tw_h; }
+  static const double2* a1(const FFTPlan& p) { return p.tw_1; }
+  static const double2* a0(const FFTPlan& p) { return p.tw_0; }
+  static const double2* post(const FFTPlan& p) { return p.tw_p; }
+};
+template <>
+struct Tw<float> {
+  static const float2* h(const FFTPlan& p) { return p.tw_hf; }
+  static const float2* a1(const FFTPlan& p) { return p.tw_1f; }
+  static const float2* a0(const FFTPlan& p) { return p.tw_0f; }
+  static const float2* post(const FFTPlan& p) { return p.tw_pf; }
+};
+
+template <typename T>
+int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* launches) {
+  using V = typename VT<T>::V;
+  V* spec = reinterpret_cast<V*>(a.spec);
+  const long long rows = (long long)p.n0 * p.n1;
+  const int TH = 256;
+  // R2C along axis 2
+  dim3 gx((unsigned)((rows + p.L_x - 1) / p.L_x), (unsigned)p.nc);
+  k_r2c_x<T><<<gx, TH, p.smem_x, st>>>(a.eps, spec, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh, Tw<T>::h(p),
+                                        Tw<T>::post(p), a.gate);
+  int nl = 1;
+  GreenArgs ga;
+  ga.nc = p.nc;
+  ga.is3d = p.n0 > 1;
+  ga.n0 = p.n0; ga.n1 = p.n1; ga.n2 = p.n2; ga.nh = p.nh;
+  ga.lambda = a.lambda; ga.mu = a.mu;
+  ga.Ntot = (double)p.N;
+  if (p.n0 > 1) {
+    // axis 1, forward
+    const long long inner = p.nh;
+    const int ntile = (int)((inner + p.L_y - 1) / p.L_y);
+    dim3 gy((unsigned)(ntile * p.n0), (unsigned)p.nc);
+    k_c2c_axis<T, -1><<<gy, TH, p.smem_y, st>>>(spec, p.n1, p.nh, inner, (long long)p.n1 * p.nh, ntile, p.Nk,
+                                                  p.L_y, p.s1, Tw<T>::a1(p), a.gate);
+    // axis 0 with Green
+    const long long inner0 = (long long)p.n1 * p.nh;
+    dim3 gg((unsigned)((inner0 + p.L_g - 1) / p.L_g));
+    k_green<T><<<gg, TH, p.smem_g, st>>>(spec, p.n0, inner0, inner0, p.Nk, p.L_g, p.s0, Tw<T>::a0(p), ga, a.ebar,
+                                          a.gate);
+    // axis 1, inverse
+    k_c2c_axis<T, +1><<<gy, TH, p.smem_y, st>>>(spec, p.n1, p.nh, inner, (long long)p.n1 * p.nh, ntile, p.Nk,
+                                                  p.L_y, p.s1, Tw<T>::a1(p), a.gate);
+    nl += 3;
+  } else {
+    const long long inner = p.nh;
+    dim3 gg((unsigned)((inner + p.L_g - 1) / p.L_g));
+    k_green<T><<<gg, TH, p.smem_g, st>>>(spec, p.n1, p.nh, inner, p.Nk, p.L_g, p.s1, Tw<T>::a1(p), ga, a.ebar,
+                                          a.gate);
+    nl += 1;
+  }
+  const double invN = 1.0 / (double)p.N;
+  size_t sc = p.smem_c2r;
+  if (a.out == kOutDev32) sc += sizeof(double) * (size_t)p.nc * p.L_x * p.n2;
+  if (a.out == kOutSig64)
+    k_c2r_x<T, kOutSig64><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
+                                               Tw<T>::h(p), Tw<T>::post(p), invN, a.sig64, nullptr, nullptr,
+                                               nullptr, nullptr, a.gate);
+  else if (a.out == kOutSig32)
+    k_c2r_x<T, kOutSig32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
+                                               Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, a.sig32, nullptr,
+                                               nullptr, nullptr, a.gate);
+  else
+    k_c2r_x<T, kOutDev32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
+                                               Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, nullptr, a.sdev, a.uadd,
+                                               a.err, a.gate);
+  nl += 1;
+  if (launches) *launches += nl;
+  return STZ_OK;
+}
+
+}  // namespace
+
+int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
+  std::memset((void*)p, 0, sizeof(*p));
+  if (n2 < 2 || n2 % 2 != 0 || n1 < 1 || n0 < 1) return STZ_ERR_INVALID;
+  p->n0 = n0; p->n1 = n1; p->n2 = n2; p->nc = nc;
+  p->h = n2 / 2;
+  p->nh = p->h + 1;
+  p->N = (long long)n0 * n1 * n2;
+  p->Nk = (long long)n0 * n1 * p->nh;
+  p->sh = make_sched(p->h);
+  p->s1 = make_sched(n1);
+  p->s0 = make_sched(n0);
+  if (p->sh.nst < 0 || p->s1.nst < 0 || p->s0.nst < 0) return STZ_ERR_INVALID;
+  if (p->h > 4096 || n1 > 1024 || n0 > 1024) return STZ_ERR_INVALID;
+  int st;
+  if ((st = upload_twiddles(p->h, p->h, &p->tw_h, &p->tw_hf))) return st;
+  if ((st = upload_twiddles(n1, n1, &p->tw_1, &p->tw_1f))) return st;
+  if ((st = upload_twiddles(n0, n0, &p->tw_0, &p->tw_0f))) return st;
+  if ((st = upload_twiddles(n2, p->nh, &p->tw_p, &p->tw_pf))) return st;
+  // tiles (FP64 sizes; the FP32 transform uses the same tiles)
+  const size_t cz = sizeof(double2);
+  p->L_x = std::max(1, 1024 / p->h);
+  while (p->L_x > 1 && 2 * (size_t)p->L_x * (p->h + 2) * cz + sizeof(double) * nc * p->L_x * n2 > 200 * 1024) p->L_x /= 2;
+  p->L_y = 8;
+  while (p->L_y > 1 && 2 * (size_t)p->L_y * (n1 + 1) * cz > 100 * 1024) p->L_y /= 2;
+  const int ng = n0 > 1 ? n0 : n1;
+  p->L_g = 8;
+  while (p->L_g > 1 && 2 * (size_t)nc * p->L_g * (ng + 1) * cz > 200 * 1024) p->L_g /= 2;
+  p->smem_x = 2 * (size_t)p->L_x * (p->h + 1) * cz;
+  p->smem_c2r = 2 * (size_t)p->L_x * (p->h + 2) * cz;
+  p->smem_y = 2 * (size_t)p->L_y * (n1 + 1) * cz;
+  p->smem_g = 2 * (size_t)nc * p->L_g * (ng + 1) * cz;
+  if (p->smem_g > 227 * 1024) return STZ_ERR_INVALID;
+  size_t sc_max = p->smem_c2r + sizeof(double) * nc * p->L_x * n2;
+  set_smem_attrs<double>(p->smem_x, p->smem_y, p->smem_g, sc_max);
+  set_smem_attrs<float>(p->smem_x, p->smem_y, p->smem_g, sc_max);
+  return STZ_OK;
+}
+
+void fft_plan_destroy(FFTPlan* p) {
+  cudaFree(p->tw_h); cudaFree(p->tw_1); cudaFree(p->tw_0); cudaFree(p->tw_p);
+  cudaFree(p->tw_hf); cudaFree(p->tw_1f); cudaFree(p->tw_0f); cudaFree(p->tw_pf);
+  std::memset((void*)p, 0, sizeof(*p));
+}
+
+int fft_solve(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* launches) {
+  return a.fp32 ? solve_t<float>(p, a, st, launches) : solve_t<double>(p, a, st, launches);
+}
+
+// Gaussian-covariance filter of one real field in place (unit-variance
+// renormalisation is done by the caller).
+int fft_filter_gaussian(const FFTPlan& p, double* field, double corr_len, void* spec, cudaStream_t st) {
+  using V = double2;
+  V* sp = reinterpret_cast<V*>(spec);
+  const long long rows = (long long)p.n0 * p.n1;
+  const int TH = 256;
+  dim3 gx((unsigned)((rows + p.L_x - 1) / p.L_x), 1);
+  k_r2c_x<double><<<gx, TH, p.smem_x, st>>>(field, sp, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh, p.tw_h,
+                                             p.tw_p, nullptr);
+  const long long inner1 = p.nh;
+  const int ntile1 = (int)((inner1 + p.L_y - 1) / p.L_y);
+  dim3 gy((unsigned)(ntile1 * p.n0), 1);
+  k_c2c_axis<double, -1><<<gy, TH, p.smem_y, st>>>(sp, p.n1, p.nh, inner1, (long long)p.n1 * p.nh, ntile1, p.Nk,
+                                                    p.L_y, p.s1, p.tw_1, nullptr);
+  const long long inner0 = (long long)p.n1 * p.nh;
+  const int ntile0 = (int)((inner0 + p.L_y - 1) / p.L_y);
+  size_t s0 = 2 * (size_t)p.L_y * (p.n0 + 1) * sizeof(V);
+  if (p.n0 > 1) {
+    cudaFuncSetAttribute(k_c2c_axis<double, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s0, p.smem_y));
+    cudaFuncSetAttribute(k_c2c_axis<double, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s0, p.smem_y));
+    k_c2c_axis<double, -1><<<ntile0, TH, s0, st>>>(sp, p.n0, inner0, inner0, 0, ntile0, p.Nk, p.L_y, p.s0, p.tw_0,
+                                                   nullptr);
+  }
+  k_gauss_filter<double><<<(unsigned)((p.Nk + 255) / 256), 256, 0, st>>>(sp, p.n0, p.n1, p.n2, p.nh, corr_len, p.Nk);
+  if (p.n0 > 1)
+    k_c2c_axis<double, +1><<<ntile0, TH, s0, st>>>(sp, p.n0, inner0, inner0, 0, ntile0, p.Nk, p.L_y, p.s0, p.tw_0,
+                                                   nullptr);
+  k_c2c_axis<double, +1><<<gy, TH, p.smem_y, st>>>(sp, p.n1, p.nh, inner1, (long long)p.n1 * p.nh, ntile1, p.Nk,
+                                                    p.L_y, p.s1, p.tw_1, nullptr);
+  k_c2r_x<double, kOutSig64><<<gx.x, TH, p.smem_c2r, st>>>(sp, 1, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
+                                                          p.tw_h, p.tw_p, 1.0, field, nullptr, nullptr, nullptr,
+                                                          nullptr, nullptr);
+  return STZ_OK;
+}
+
+}  // namespace stz

@@ -1,0 +1,1141 @@
+// kmc.cu -- the STZ kinetic Monte Carlo step on the device.
+//
+// One driver-loop iteration (bmg.c:139-178) of the FP64 forms is
+//   k_rate64     SofteningFactor + ActEnergy + KMC rates for every (mode, site)
+//                (init.c:561-739, evolution.c:120-128), per-(mode, block) FP64
+//                sums; the last block to finish reduces them, decides athermal
+//                / thermal / elastic, draws the dice, finds the event with a
+//                hierarchical search in the reference's mode-major order
+//                (evolution.c:136-193) and commits it (elastic.c:361-520)
+//   k_ath_mark, k_ath_commit   athermal avalanche (evolution.c:47-100)
+//   FFT solve    fft.cu
+//   k_post_a     loading, clock and print check (evolution.c:262-358, bmg.c:181-187)
+//   FFT solve    print re-solve (bmg.c:292-295), skipped unless printing
+//   k_post_b     stop conditions (bmg.c:382-410) and run targets
+// Kernels after the first read their work flags from the control block and
+// return at once when the step does not need them.
+//
+// The mixed form replaces the per-event FFT by the response of one voxel
+// (linearity of the Green's operator): k_mixed adds the pending
+// transformation's response to the FP32 deviatoric stress field, evaluates
+// the rates in FP32, sums them in FP64 and selects/commits in its last block.
+#include <cfloat>
+#include <cmath>
+
+#include "kmc.cuh"
+
+namespace stz {
+namespace {
+
+constexpr int TH = kRateThreads;
+constexpr unsigned FULL = 0xffffffffu;
+
+// ------------------------------------------------------------ scalar state
+__device__ __forceinline__ int ndiag(int nc) { return nc == 3 ? 2 : 3; }
+
+__device__ void apply_C(const KParams& kp, const double* e, double* s) {
+  const int nd = ndiag(kp.nc);
+  double tr = 0;
+  for (int c = 0; c < nd; c++) tr += e[c];
+  for (int c = 0; c < kp.nc; c++) s[c] = (c < nd ? kp.lambda * tr : 0.0) + 2.0 * kp.mu * e[c];
+}
+
+// isotropicinv (elastic.c:522-531) in DIM dimensions
+__device__ void iso_inv(const KParams& kp, const double* s, double* e) {
+  const double lam = kp.lambda, mu = kp.mu;
+  if (kp.nc == 3) {
+    double tra = -lam / 2 / mu / (2 * lam + 2 * mu) * (s[0] + s[1]);
+    e[0] = tra + s[0] / 2 / mu;
+    e[1] = tra + s[1] / 2 / mu;
+    e[2] = s[2] / 2 / mu;
+  } else {
+    double tra = -lam / 2 / mu / (3 * lam + 2 * mu) * (s[0] + s[1] + s[2]);
+    for (int c = 0; c < 3; c++) e[c] = tra + s[c] / 2 / mu;
+    for (int c = 3; c < 6; c++) e[c] = s[c] / 2 / mu;
+  }
+}
+
+__device__ void solved_mean_stress(const KParams& kp, const Ctl* ctl, const double* ebar, double* out) {
+  double e[6];
+  for (int c = 0; c < kp.nc; c++) e[c] = ebar[c] - ctl->eps0_sum[c] / (double)kp.N;
+  apply_C(kp, e, out);
+}
+
+__device__ __forceinline__ int shear_comp(const KParams& kp) { return kp.nc == 3 ? 2 : STZ_XY; }
+__device__ __forceinline__ int loaded_comp(const KParams& kp) {
+  return kp.loading == STZ_LOAD_SHEAR ? shear_comp(kp) : 0;
+}
+
+// eps_avg correction from the mean stress of the solved field
+// (evolution.c:92-97, 263-300)
+__device__ void subtract_error(const KParams& kp, const Ctl* ctl, int athermal, double* tmpStrain) {
+  double ts[6] = {0, 0, 0, 0, 0, 0};
+  if (!kp.no_subtract_error) {
+    for (int c = 0; c < kp.nc; c++) ts[c] = ctl->stress[c];
+    const int zc = (athermal && kp.nc == 3) ? 0 : loaded_comp(kp);
+    ts[zc] = 0.0;
+  }
+  iso_inv(kp, ts, tmpStrain);
+}
+
+__device__ void hold_stress(const KParams& kp, Ctl* ctl) {
+  double d[6] = {0, 0, 0, 0, 0, 0}, de[6];
+  for (int c = 0; c < kp.nc; c++) d[c] = kp.applied[c] - ctl->stress[c];
+  iso_inv(kp, d, de);
+  for (int c = 0; c < kp.nc; c++) {
+    ctl->eps_avg[c] += de[c];
+    ctl->u[c] += d[c];
+    ctl->stress[c] = kp.applied[c];
+  }
+}
+
+// loading after a thermal event (evolution.c:262-317); ctl->stress holds the
+// mean stress of the field solved right after the transformation
+__device__ void load_after_event(const KParams& kp, Ctl* ctl, double t_kmc) {
+  double ts[6];
+  const double rate = kp.strain_rate, nu = kp.poisson, E = kp.young, mu = kp.mu;
+  const bool d2 = kp.nc == 3;
+  switch (kp.loading) {
+    case STZ_LOAD_TENSION:
+      subtract_error(kp, ctl, 0, ts);
+      ctl->eps_avg[0] += (rate * t_kmc * 1 - ts[0]);
+      ctl->eps_avg[1] += (rate * t_kmc * (-nu) - ts[1]);
+      if (d2) {
+        ctl->eps_avg[2] += (-ts[2]);
+      } else {
+        ctl->eps_avg[2] += (rate * t_kmc * (-nu) - ts[2]);
+        for (int c = 3; c < 6; c++) ctl->eps_avg[c] += (-ts[c]);
+      }
+      ctl->stress[0] += E * rate * t_kmc;
+      ctl->u[0] += E * rate * t_kmc;
+      break;
+    case STZ_LOAD_COMPRESSION:
+      subtract_error(kp, ctl, 0, ts);
+      ctl->eps_avg[0] += (-rate * t_kmc * 1);
+      ctl->eps_avg[1] += (rate * t_kmc * (nu));
+      ctl->eps_avg[0] += (-rate * t_kmc * 1 - ts[0]);
+      ctl->eps_avg[1] += (rate * t_kmc * (nu) - ts[1]);
+      for (int c = 2; c < kp.nc; c++) ctl->eps_avg[c] += (-ts[c]);
+      ctl->stress[0] += -E * rate * t_kmc;
+      ctl->u[0] += -E * rate * t_kmc;
+      break;
+    case STZ_LOAD_SHEAR: {
+      const int sc = shear_comp(kp);
+      subtract_error(kp, ctl, 0, ts);
+      for (int c = 0; c < kp.nc; c++)
+        if (c != sc) ctl->eps_avg[c] += -ts[c];
+      ctl->eps_avg[sc] += rate * t_kmc;
+      ctl->stress[sc] += 2 * mu * rate * t_kmc;
+      ctl->u[sc] += 2 * mu * rate * t_kmc;
+      break;
+    }
+    case STZ_LOAD_STRESS:
+      hold_stress(kp, ctl);
+      break;
+  }
+}
+
+// pure elastic step (evolution.c:321-358)
+__device__ void elastic_step(const KParams& kp, Ctl* ctl) {
+  const double inc = kp.strain_increment, nu = kp.poisson, E = kp.young, mu = kp.mu;
+  const bool d2 = kp.nc == 3;
+  switch (kp.loading) {
+    case STZ_LOAD_TENSION:
+      ctl->eps_avg[0] += (inc * 1);
+      ctl->eps_avg[1] += (inc * (-nu));
+      ctl->eps_avg[2] += d2 ? (inc * 0.0) : (inc * (-nu));
+      ctl->stress[0] += E * inc;
+      ctl->u[0] += E * inc;
+      break;
+    case STZ_LOAD_COMPRESSION:
+      ctl->eps_avg[0] += (inc * (-1));
+      ctl->eps_avg[1] += (inc * (nu));
+      ctl->eps_avg[2] += d2 ? (inc * 0.0) : (inc * (nu));
+      ctl->stress[0] += -E * inc;
+      ctl->u[0] += -E * inc;
+      break;
+    case STZ_LOAD_SHEAR: {
+      const int sc = shear_comp(kp);
+      if (kp.shear_quirk) ctl->eps_avg[sc] += kp.strain_rate * 1;
+      else ctl->eps_avg[sc] += inc;
+      ctl->stress[sc] += 2 * mu * inc;
+      ctl->u[sc] += 2 * mu * inc;
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// print test (bmg.c:181-187); returns 1 when the step prints (and re-solves)
+__device__ int print_check(const KParams& kp, Ctl* ctl) {
+  if (kp.loading == STZ_LOAD_STRESS) return 0;
+  const int lc = loaded_comp(kp);
+  if (fabs(ctl->eps_avg[lc] - ctl->last_print_strain) >= kp.print_thr) {
+    ctl->n_print++;
+    ctl->last_print_strain = ctl->eps_avg[lc];
+    return 1;
+  }
+  return 0;
+}
+
+// stop conditions (bmg.c:382-410) and run targets; sets halt
+__device__ void stop_check(const KParams& kp, Ctl* ctl) {
+  if (kp.loading != STZ_LOAD_STRESS) {
+    const int lc = loaded_comp(kp);
+    if (fabs(ctl->eps_avg[lc]) > kp.end_strain) ctl->stopped = 1;
+    else if (kp.loading == STZ_LOAD_TENSION && ctl->stress[0] < -0.5) ctl->stopped = 2;
+    else if (kp.loading == STZ_LOAD_SHEAR && fabs(ctl->stress[lc]) < kEpsilon) ctl->stopped = 2;
+  }
+  if (ctl->stopped) { ctl->halt = 1; ctl->halt_reason = kHaltStop; return; }
+  if ((ctl->max_kstep >= 0 && ctl->kstep >= ctl->max_kstep) || (ctl->max_step >= 0 && ctl->step >= ctl->max_step)) {
+    ctl->halt = 1;
+    ctl->halt_reason = kHaltTarget;
+  }
+}
+
+__device__ void log_event(const KParams& kp, const Fields& f, Ctl* ctl, int kind, long long site, int mode,
+                          double time, double dt, double q, double R) {
+  const long long i = ctl->nlog;
+  if (i - ctl->log_base >= kp.log_cap) {
+    ctl->nlog_dropped++;
+    return;
+  }
+  stz_event e;
+  e.step = ctl->step;
+  e.site = site;
+  e.kind = kind;
+  e.mode = mode;
+  e.time = time;
+  e.dt = dt;
+  e.q = q;
+  e.total_rate = R;
+  f.log[i % kp.log_cap] = e;
+  ctl->nlog = i + 1;
+}
+
+// ------------------------------------------------------- per-site physics
+// Unpack a site index into grid coordinates.
+__device__ __forceinline__ void site_coords(const KParams& kp, long long s, int* i0, int* i1, int* i2) {
+  *i2 = (int)(s % kp.n2);
+  const long long r = s / kp.n2;
+  *i1 = (int)(r % kp.n1);
+  *i0 = (int)(r / kp.n1);
+}
+
+// Direction modifier of the softening schemes (init.c:590-642)
+__device__ __forceinline__ double dire_modifier(int scheme, double dot, double n1, double n2) {
+  double DM;
+  switch (scheme) {
+    case STZ_SF_LINEAR_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (DM + 1) / 2;
+    case STZ_SF_LINEAR_BWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (-DM + 1) / 2;
+    case STZ_SF_EVEN: return 0.5;
+    case STZ_SF_SQUARE_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (1 + DM) * (1 + DM) / 4;
+    case STZ_SF_CUBIC_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (DM + 1) * (DM + 1) * (DM + 1) / 8;
+    default: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return exp(-DM * DM * 9 / 2);
+  }
+}
+
+// REF2D: site data shared by the 20 modes
+struct R2Site {
+  double sg[3], pd[3], n2, soft;
+};
+
+__device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, const double* u, double totime,
+                                          long long s) {
+  R2Site d;
+  const long long N = kp.N;
+  for (int c = 0; c < 3; c++) {
+    d.sg[c] = f.sig[c * N + s] + u[c];
+    d.pd[c] = f.prev_deps[c * N + s];
+  }
+  d.n2 = sqrt(d.pd[0] * d.pd[0] + d.pd[1] * d.pd[1] + 2 * d.pd[2] * d.pd[2]);
+  d.soft = kp.softening ? f.perm_soft[s] + f.temp_soft[s] * exp((f.tlast[s] - totime) / kp.t_temp) : 0.0;
+  return d;
+}
+
+// ActEnergy for one (mode, site) of the reference model (init.c:585-686)
+__device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m) {
+  const long long N = kp.N;
+  const double* dd = f.deps + (long long)m * 3 * N;
+  const double d0 = dd[s], d1 = dd[N + s], d2 = dd[2 * N + s];
+  const double DWork = (d.sg[0] * d0 + d.sg[1] * d1 + 2 * d.sg[2] * d2) * kp.V0 * 1e-18 * kJInEv;
+  const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
+  const double n1 = sqrt(d0 * d0 + d1 * d1 + 2 * d2 * d2);
+  const double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
+  return f.Q0[(long long)m * N + s] * exp(-DM * d.soft) - DWork / 2;
+}
+
+// GLOBAL3D FP64: Q = dF - W/2 with W = sigma:deps_m
+__device__ __forceinline__ double g3_Q(const KParams& kp, const double* sg, double dF, int m) {
+  double w = 0;
+  for (int c = 0; c < 6; c++) w += (c >= 3 ? 2.0 : 1.0) * sg[c] * kp.modes[m][c];
+  return dF - w * kp.V0 * 1e-18 * kJInEv / 2;
+}
+
+__device__ __forceinline__ void g3_load(const KParams& kp, const Fields& f, const double* u, long long s, double* sg) {
+  for (int c = 0; c < 6; c++) sg[c] = f.sig[c * kp.N + s] + u[c];
+}
+
+// Mixed: scaled log2-rate x = log2(e)/kT (q_ref - Q); identical code in the
+// main pass and in the rescan so both see the same bits.
+__device__ __forceinline__ float mx_x(const KParams& kp, const float* sv, float a, int m) {
+  float x = a;
+#pragma unroll
+  for (int k = 0; k < 5; k++) x = __fmaf_rn(sv[k], kp.mdev[m][k], x);
+  return x;
+}
+
+// ---------------------------------------------------- block-level helpers
+// Inclusive scan of one double per thread over a 256-thread block; returns the
+// inclusive value and leaves every thread's inclusive value in sh_inc.
+__device__ double block_incl_scan(double v, double* sh_inc) {
+  __shared__ double wsum[TH / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double y = __shfl_up_sync(FULL, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < TH / 32 ? wsum[lane] : 0.0;
+#pragma unroll
+    for (int off = 1; off < TH / 32; off <<= 1) {
+      const double y = __shfl_up_sync(FULL, t, off);
+      if (lane >= off) t += y;
+    }
+    if (lane < TH / 32) wsum[lane] = t;
+  }
+  __syncthreads();
+  const double incl = (w > 0 ? wsum[w - 1] : 0.0) + x;
+  sh_inc[threadIdx.x] = incl;
+  __syncthreads();
+  return incl;
+}
+
+// Sum of STZ_MODES per-thread accumulators over the block, written to
+// part[m * nblk + b] by threads 0..STZ_MODES-1 in a fixed order.
+__device__ void block_mode_sums(const double* acc, double* part, int nblk, int b) {
+  __shared__ double red[TH / 32][STZ_MODES];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int m = 0; m < STZ_MODES; m++) {
+    double v = acc[m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+    if (lane == 0) red[w][m] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < STZ_MODES) {
+    double s = 0;
+    for (int k = 0; k < TH / 32; k++) s += red[k][threadIdx.x];
+    part[(long long)threadIdx.x * nblk + b] = s;
+  }
+}
+
+__device__ unsigned block_sum_u(unsigned v) {
+  __shared__ unsigned red[TH / 32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned t = 0;
+  for (int k = 0; k < TH / 32; k++) t += red[k];
+  return t;
+}
+
+// Last-block detection (threadfence reduction pattern). Returns true in the
+// block that finished last; that block then sees every block's writes.
+__device__ bool last_block(Ctl* ctl, int nblk) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(&ctl->ticket, 1u);
+    is_last = (t == (unsigned)nblk - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// ----------------------------------------------------------- selection
+// Rate of (site, mode) exactly as the main pass computed it (raw units).
+template <int MODEL>
+__device__ __forceinline__ double site_rate(const KParams& kp, const Fields& f, const double* u, double totime,
+                                            long long s, int m) {
+  if (MODEL == 0) {
+    const R2Site d = r2_load(kp, f, u, totime, s);
+    return kp.vt * exp(-r2_Q(kp, f, d, s, m) / kp.kT);
+  } else if (MODEL == 1) {
+    double sg[6];
+    g3_load(kp, f, u, s, sg);
+    return kp.vt * exp(-g3_Q(kp, sg, f.dF[s], m) / kp.kT);
+  } else {
+    float sv[5];
+    for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+    const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
+    return (double)exp2f(mx_x(kp, sv, a, m));
+  }
+}
+
+// Q of (site, mode) for the log (FP64 from the stored field).
+template <int MODEL>
+__device__ double site_Q(const KParams& kp, const Fields& f, const double* u, double totime, long long s, int m) {
+  if (MODEL == 0) {
+    const R2Site d = r2_load(kp, f, u, totime, s);
+    return r2_Q(kp, f, d, s, m);
+  } else if (MODEL == 1) {
+    double sg[6];
+    g3_load(kp, f, u, s, sg);
+    return g3_Q(kp, sg, f.dF[s], m);
+  } else {
+    float sv[5];
+    for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+    const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
+    return (double)kp.q_ref - (double)mx_x(kp, sv, a, m) / (double)kp.a_scale;
+  }
+}
+
+// Hierarchical search of the (mode, site) whose cumulative rate, in the
+// reference's mode-major order m*N + s, first reaches T. Level 1: the
+// per-(mode, block) sums, split into one contiguous chunk per thread and
+// scanned; level 2: the rates of the chosen mode in the chosen block,
+// recomputed and scanned. Called by the whole last block.
+template <int MODEL>
+__device__ void search_event(const KParams& kp, const Fields& f, const double* u, double totime, double T,
+                             long long* site_out, int* mode_out, double* margin_out) {
+  __shared__ double sh_inc[TH];
+  __shared__ long long sh_p;
+  __shared__ double sh_cb;
+  __shared__ long long sh_site;
+  __shared__ double sh_margin;
+  const int t = threadIdx.x;
+  const long long P = (long long)STZ_MODES * kp.nblk;
+  const long long ch = (P + TH - 1) / TH;
+  const long long p0 = t * ch, p1 = min(p0 + ch, P);
+  double S = 0;
+  for (long long p = p0; p < p1; p++) S += f.part[p];
+  if (t == 0) { sh_p = -1; sh_site = -1; sh_margin = 0; }
+  const double I = block_incl_scan(S, sh_inc);
+  const double E = t > 0 ? sh_inc[t - 1] : 0.0;
+  const double Ttot = sh_inc[TH - 1];
+  double Tq = T;
+  if (Tq > Ttot) Tq = Ttot;
+  if (E < Tq && Tq <= I) {
+    double run = E, before = E;
+    long long hit = -1, lastpos = -1;
+    double lastbefore = E;
+    for (long long p = p0; p < p1; p++) {
+      const double v = f.part[p];
+      before = run;
+      run += v;
+      if (v > 0) { lastpos = p; lastbefore = before; }
+      if (run >= Tq && v > 0) { hit = p; break; }
+    }
+    if (hit < 0) { hit = lastpos; before = lastbefore; }
+    sh_p = hit;
+    sh_cb = before;
+  }
+  __syncthreads();
+  const long long p = sh_p;
+  if (p < 0) {
+    if (t == 0) { *site_out = -1; *mode_out = -1; }
+    return;
+  }
+  const int m = (int)(p / kp.nblk);
+  const int b = (int)(p - (long long)m * kp.nblk);
+  double T2 = Tq - sh_cb;
+  const long long s0 = (long long)b * kp.bsites;
+  const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
+  const long long per = (s1 - s0 + TH - 1) / TH;
+  const long long a0 = s0 + t * per, a1 = min(a0 + per, s1);
+  double loc = 0;
+  for (long long s = a0; s < a1; s++) loc += site_rate<MODEL>(kp, f, u, totime, s, m);
+  __syncthreads();
+  const double I2 = block_incl_scan(loc, sh_inc);
+  const double E2 = t > 0 ? sh_inc[t - 1] : 0.0;
+  const double tot2 = sh_inc[TH - 1];
+  if (T2 > tot2) T2 = tot2;
+  if (!(T2 > 0)) T2 = DBL_MIN;
+  if (E2 < T2 && T2 <= I2) {
+    double run = E2;
+    long long hit = -1, lastpos = -1;
+    double hb = E2, ha = E2, lb = E2, la = E2;
+    for (long long s = a0; s < a1; s++) {
+      const double r = site_rate<MODEL>(kp, f, u, totime, s, m);
+      const double before = run;
+      run += r;
+      if (r > 0) { lastpos = s; lb = before; la = run; }
+      if (run >= T2 && r > 0) { hit = s; hb = before; ha = run; break; }
+    }
+    if (hit < 0) { hit = lastpos; hb = lb; ha = la; }
+    sh_site = hit;
+    sh_margin = fmin(T2 - hb, ha - T2);
+  }
+  __syncthreads();
+  if (t == 0) {
+    *site_out = sh_site;
+    *mode_out = m;
+    *margin_out = sh_margin;
+  }
+}
+
+// ------------------------------------------------------------ commits
+// VoxelShearTransform (elastic.c:361-520) for the FP64 models; thread 0 only.
+template <int MODEL>
+__device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, long long s) {
+  const long long N = kp.N;
+  double d[6];
+  if (MODEL == 0) {
+    const double* dd = f.deps + (long long)mm * 3 * N;
+    d[0] = dd[s]; d[1] = dd[N + s]; d[2] = dd[2 * N + s];
+  } else {
+    for (int c = 0; c < 6; c++) d[c] = kp.modes[mm][c];
+  }
+  for (int c = 0; c < kp.nc; c++) {
+    f.prev_deps[c * N + s] = d[c];
+    f.eps0[c * N + s] += d[c];
+    ctl->eps0_sum[c] += d[c];
+  }
+  if (MODEL == 0) {
+    const double ds = d[0] * d[0] + d[1] * d[1] + 2 * d[2] * d[2];
+    double ps = f.perm_soft[s] + ds * kp.perm_soft;
+    if (ps > kp.perm_soft_cap) ps = kp.perm_soft_cap;
+    f.perm_soft[s] = ps;
+    f.temp_soft[s] = ds * kp.temp_soft;
+    f.tlast[s] = ctl->totime;
+    // re-draw the site's modes, glass branch (elastic.c:508-512)
+    for (int i = 0; i < STZ_MODES; i++) {
+      double* dd = f.deps + (long long)i * 3 * N;
+      const double a = 0.5 * kp.gamma0 * mt_gaussian(&ctl->rng, 1.0);
+      dd[s] = a;
+      dd[N + s] = -a;
+      dd[2 * N + s] = 0.5 * kp.gamma0 * mt_gaussian(&ctl->rng, 1.0);
+    }
+  }
+}
+
+// Last block of the FP64 rate kernel: decide the step kind and commit.
+template <int MODEL>
+__device__ void finish_fp64(const KParams& kp, const Fields& f) {
+  Ctl* ctl = f.ctl;
+  __shared__ int sh_kind;
+  __shared__ double sh_T, sh_R;
+  __shared__ double sh_u[6];
+  __shared__ double sh_tot;
+  __shared__ long long sh_site;
+  __shared__ int sh_mode;
+  __shared__ double sh_margin;
+  __shared__ double sh_inc2[TH];
+  // total rate: per-thread contiguous chunks of the partials, fixed order
+  const long long P = (long long)STZ_MODES * kp.nblk;
+  const long long ch = (P + TH - 1) / TH;
+  const long long p0 = threadIdx.x * ch, p1 = min(p0 + ch, P);
+  double S = 0;
+  for (long long p = p0; p < p1; p++) S += f.part[p];
+  block_incl_scan(S, sh_inc2);
+  if (threadIdx.x == 0) {
+    ctl->ticket = 0;
+    ctl->step++;
+    const double R = sh_inc2[TH - 1];
+    sh_R = R;
+    for (int c = 0; c < 6; c++) sh_u[c] = ctl->u[c];
+    sh_tot = ctl->totime;
+    if (ctl->neg_count > 0) {
+      sh_kind = kAthermal;
+    } else if (!(R > 0) || !isfinite(R)) {
+      sh_kind = kNone;
+      ctl->status = STZ_ERR_NAN;
+      ctl->halt = 1;
+      ctl->halt_reason = kHaltError;
+    } else {
+      const double t_kmc = 1 / R;
+      if (t_kmc < kp.dt) {
+        sh_kind = kThermal;
+        ctl->kstep++;
+        const double dice = mt_uniform(&ctl->rng);
+        sh_T = dice * R;
+        ctl->t_kmc = t_kmc;
+        if (!(dice > 0)) {
+          sh_kind = kNone;
+          ctl->status = STZ_ERR_NO_EVENT;
+          ctl->halt = 1;
+          ctl->halt_reason = kHaltError;
+        }
+      } else {
+        sh_kind = kElastic;
+      }
+    }
+    ctl->neg_count = 0;
+    ctl->step_kind = sh_kind;
+    ctl->total_rate = R;
+  }
+  __syncthreads();
+  const int kind = sh_kind;
+  if (kind == kThermal) {
+    search_event<MODEL>(kp, f, sh_u, sh_tot, sh_T, &sh_site, &sh_mode, &sh_margin);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const long long s = sh_site;
+      const int m = sh_mode;
+      if (s < 0) {
+        ctl->status = STZ_ERR_NO_EVENT;
+        ctl->halt = 1;
+        ctl->halt_reason = kHaltError;
+        ctl->step_kind = kNone;
+      } else {
+        if (sh_margin < 1e-12 * sh_R) ctl->near_ties++;
+        const double q = site_Q<MODEL>(kp, f, sh_u, sh_tot, s, m);
+        transform<MODEL>(kp, f, ctl, m, s);
+        ctl->sel_site = s;
+        ctl->sel_mode = m;
+        ctl->sel_q = q;
+        ctl->solve_req = 1;
+        log_event(kp, f, ctl, STZ_EV_THERMAL, s, m, ctl->totime + ctl->t_kmc, ctl->t_kmc, q, sh_R);
+      }
+    }
+  } else if (kind == kElastic) {
+    if (threadIdx.x == 0) {
+      ctl->estep++;
+      ctl->totime += kp.dt;
+      elastic_step(kp, ctl);
+      ctl->solve_req = 0;
+      log_event(kp, f, ctl, STZ_EV_ELASTIC, -1, -1, ctl->totime, kp.dt, 0.0, sh_R);
+    }
+  } else if (kind == kAthermal) {
+    if (threadIdx.x == 0) ctl->solve_req = 0;  // set by the athermal commit
+  }
+}
+
+// ------------------------------------------------------------ FP64 rates
+template <int MODEL>
+__global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
+  Ctl* ctl = f.ctl;
+  if (ctl->halt) return;
+  const int b = blockIdx.x;
+  const long long s0 = (long long)b * kp.bsites;
+  const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
+  double u[6];
+  for (int c = 0; c < 6; c++) u[c] = ctl->u[c];
+  const double totime = ctl->totime;
+  double acc[STZ_MODES];
+#pragma unroll
+  for (int m = 0; m < STZ_MODES; m++) acc[m] = 0;
+  unsigned neg = 0;
+  for (long long s = s0 + threadIdx.x; s < s1; s += TH) {
+    if (MODEL == 0) {
+      const R2Site d = r2_load(kp, f, u, totime, s);
+#pragma unroll 4
+      for (int m = 0; m < STZ_MODES; m++) {
+        const double Q = r2_Q(kp, f, d, s, m);
+        neg += Q < 0;
+        acc[m] += kp.vt * exp(-Q / kp.kT);
+      }
+    } else {
+      double sg[6];
+      g3_load(kp, f, u, s, sg);
+      const double dF = f.dF[s];
+#pragma unroll 4
+      for (int m = 0; m < STZ_MODES; m++) {
+        const double Q = g3_Q(kp, sg, dF, m);
+        neg += Q < 0;
+        acc[m] += kp.vt * exp(-Q / kp.kT);
+      }
+    }
+  }
+  block_mode_sums(acc, f.part, kp.nblk, b);
+  const unsigned nb = block_sum_u(neg);
+  if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
+  if (!last_block(ctl, kp.nblk)) return;
+  finish_fp64<MODEL>(kp, f);
+}
+
+// ------------------------------------------------------------ athermal
+// Mark every site whose lowest-barrier mode has Q < 0 or |Q| < 0.33
+// (evolution.c:55-65). mixed: Q from the FP32 deviatoric field.
+__global__ void k_ath_mark(KParams kp, Fields f, int mixed) {
+  Ctl* ctl = f.ctl;
+  if (ctl->step_kind != kAthermal) return;
+  double u[6];
+  for (int c = 0; c < 6; c++) u[c] = ctl->u[c];
+  const double totime = ctl->totime;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < kp.N; s += (long long)gridDim.x * blockDim.x) {
+    int mm = 0;
+    double minQ = 0;
+    for (int m = 0; m < STZ_MODES; m++) {
+      double Q;
+      if (kp.model == STZ_MODEL_REF2D) Q = site_Q<0>(kp, f, u, totime, s, m);
+      else if (mixed) Q = site_Q<2>(kp, f, u, totime, s, m);
+      else Q = site_Q<1>(kp, f, u, totime, s, m);
+      if (m == 0 || minQ > Q) { mm = m; minQ = Q; }
+    }
+    f.amark[s] = (minQ < 0 || fabs(minQ) < 0.33) ? (signed char)(mm + 1) : (signed char)0;
+  }
+}
+
+// Transform the marked sites in index order (the RNG stream order of the
+// reference's space_loop); one block, thread 0 commits.
+__global__ void k_ath_commit(KParams kp, Fields f, int mixed) {
+  Ctl* ctl = f.ctl;
+  if (ctl->step_kind != kAthermal) return;
+  __shared__ unsigned ballot[TH / 32];
+  double u[6];
+  for (int c = 0; c < 6; c++) u[c] = ctl->u[c];
+  const double totime = ctl->totime;
+  if (threadIdx.x == 0) ctl->astep++;
+  for (long long base = 0; base < kp.N; base += TH) {
+    const long long s = base + threadIdx.x;
+    const bool mk = s < kp.N && f.amark[s] != 0;
+    const unsigned bal = __ballot_sync(FULL, mk);
+    if ((threadIdx.x & 31) == 0) ballot[threadIdx.x >> 5] = bal;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 0; w < TH / 32; w++) {
+        unsigned bb = ballot[w];
+        while (bb) {
+          const int lane = __ffs(bb) - 1;
+          bb &= bb - 1;
+          const long long site = base + w * 32 + lane;
+          const int mm = f.amark[site] - 1;
+          double q;
+          if (kp.model == STZ_MODEL_REF2D) q = site_Q<0>(kp, f, u, totime, site, mm);
+          else if (mixed) q = site_Q<2>(kp, f, u, totime, site, mm);
+          else q = site_Q<1>(kp, f, u, totime, site, mm);
+          if (kp.model == STZ_MODEL_REF2D) transform<0>(kp, f, ctl, mm, site);
+          else transform<1>(kp, f, ctl, mm, site);
+          log_event(kp, f, ctl, STZ_EV_ATHERMAL, site, mm, ctl->totime, 0.0, q, 0.0);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ctl->solve_req = 1;
+}
+
+// ------------------------------------------------------------ post steps
+__global__ void k_post_a(KParams kp, Fields f) {
+  Ctl* ctl = f.ctl;
+  if (ctl->halt && ctl->step_kind == kNone) return;
+  const int kind = ctl->step_kind;
+  if (kind == kThermal) {
+    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    for (int c = 0; c < 6; c++) ctl->u[c] = 0;
+    load_after_event(kp, ctl, ctl->t_kmc);
+    ctl->totime += ctl->t_kmc;
+  } else if (kind == kAthermal) {
+    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    for (int c = 0; c < 6; c++) ctl->u[c] = 0;
+    if (kp.loading == STZ_LOAD_STRESS) {
+      hold_stress(kp, ctl);
+    } else {
+      double ts[6];
+      subtract_error(kp, ctl, 1, ts);
+      for (int c = 0; c < kp.nc; c++) ctl->eps_avg[c] -= ts[c];
+    }
+  } else {
+    ctl->solve_req = 0;
+    return;
+  }
+  ctl->print_done = 0;
+  ctl->solve_req = 0;
+  (void)f;
+}
+
+// print check after every step kind; requests the print re-solve
+__global__ void k_post_print(KParams kp, Fields f) {
+  Ctl* ctl = f.ctl;
+  if (ctl->step_kind == kNone) return;
+  ctl->print_done = print_check(kp, ctl);
+  ctl->solve_req = ctl->print_done;
+}
+
+__global__ void k_post_b(KParams kp, Fields f) {
+  Ctl* ctl = f.ctl;
+  if (ctl->step_kind == kNone) return;
+  if (ctl->print_done) {
+    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    for (int c = 0; c < 6; c++) ctl->u[c] = 0;
+  }
+  ctl->print_done = 0;
+  ctl->solve_req = 0;
+  ctl->step_kind = kNone;
+  stop_check(kp, ctl);
+  (void)f;
+}
+
+// ------------------------------------------------------------ mixed form
+struct TabLoad {
+  float k[15];
+};
+
+__device__ __forceinline__ int fold(int d, int n, int* flip) {
+  if (d < 0) d += n;
+  if (2 * d > n) { *flip = 1; return n - d; }
+  *flip = 0;
+  return d;
+}
+
+template <int UPDATE_ONLY>
+__global__ void __launch_bounds__(TH) k_mixed(KParams kp, Fields f) {
+  Ctl* ctl = f.ctl;
+  if (ctl->halt && !UPDATE_ONLY) return;
+  const int b = blockIdx.x;
+  const long long N = kp.N;
+  const long long s0 = (long long)b * kp.bsites;
+  const long long s1 = min(s0 + (long long)kp.bsites, N);
+  // pending transformation and uniform change
+  const int hp = ctl->has_pend;
+  int pm = 0, p0 = 0, p1 = 0, p2 = 0;
+  float de[5] = {0, 0, 0, 0, 0};
+  if (hp) {
+    pm = ctl->pend_mode;
+    site_coords(kp, ctl->pend_site, &p0, &p1, &p2);
+    for (int k = 0; k < 5; k++) de[k] = kp.mdev_raw[pm][k];
+  }
+  float Ud[5];
+  {
+    double U6[6], ud[5];
+    for (int c = 0; c < 6; c++) U6[c] = ctl->U[c];
+    const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
+    ud[0] = (U6[0] - U6[1]) * r2;
+    ud[1] = (2.0 * U6[2] - U6[0] - U6[1]) * r6;
+    ud[2] = q2 * U6[3];
+    ud[3] = q2 * U6[4];
+    ud[4] = q2 * U6[5];
+    for (int k = 0; k < 5; k++) Ud[k] = (float)ud[k];
+  }
+  const long long ts = (long long)kp.kt1 * kp.kt2, tstride = (long long)kp.kt0 * ts;
+  float acc[STZ_MODES];
+#pragma unroll
+  for (int m = 0; m < STZ_MODES; m++) acc[m] = 0.f;
+  const float thr_neg = kp.q_ref * kp.a_scale;
+  unsigned neg = 0;
+  for (long long s = s0 + threadIdx.x; s < s1; s += TH) {
+    float sv[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) sv[k] = f.sdev[k * N + s];
+    if (hp) {
+      int i0, i1, i2, fx, fy, fz;
+      site_coords(kp, s, &i0, &i1, &i2);
+      const int d0 = fold(i0 - p0, kp.n0, &fz);
+      const int d1 = fold(i1 - p1, kp.n1, &fy);
+      const int d2 = fold(i2 - p2, kp.n2, &fx);
+      const float sx = fx ? -1.f : 1.f, sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
+      const float sg[5] = {1.f, 1.f, sy * sz, sx * sz, sx * sy};
+      const float* tp = f.ktab + (long long)d0 * ts + (long long)d1 * kp.kt2 + d2;
+      float K[15];
+#pragma unroll
+      for (int j = 0; j < 15; j++) K[j] = __ldg(tp + j * tstride);
+      float e[5];
+#pragma unroll
+      for (int k = 0; k < 5; k++) e[k] = sg[k] * de[k];
+      // symmetric 5x5 from the packed upper triangle (row-major, a <= b)
+      const float y0 = K[0] * e[0] + K[1] * e[1] + K[2] * e[2] + K[3] * e[3] + K[4] * e[4];
+      const float y1 = K[1] * e[0] + K[5] * e[1] + K[6] * e[2] + K[7] * e[3] + K[8] * e[4];
+      const float y2 = K[2] * e[0] + K[6] * e[1] + K[9] * e[2] + K[10] * e[3] + K[11] * e[4];
+      const float y3 = K[3] * e[0] + K[7] * e[1] + K[10] * e[2] + K[12] * e[3] + K[13] * e[4];
+      const float y4 = K[4] * e[0] + K[8] * e[1] + K[11] * e[2] + K[13] * e[3] + K[14] * e[4];
+      sv[0] += y0;
+      sv[1] += y1;
+      sv[2] += sg[2] * y2;
+      sv[3] += sg[3] * y3;
+      sv[4] += sg[4] * y4;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      sv[k] += Ud[k];
+      f.sdev[k * N + s] = sv[k];
+    }
+    if (!UPDATE_ONLY) {
+      const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
+#pragma unroll
+      for (int m = 0; m < STZ_MODES; m++) {
+        const float x = mx_x(kp, sv, a, m);
+        neg += x > thr_neg;
+        acc[m] += exp2f(x);
+      }
+    }
+  }
+  if (UPDATE_ONLY) {
+    if (!last_block(ctl, kp.nblk)) return;
+    if (threadIdx.x == 0) {
+      ctl->ticket = 0;
+      ctl->has_pend = 0;
+      for (int c = 0; c < 6; c++) ctl->U[c] = 0;
+    }
+    return;
+  }
+  double accd[STZ_MODES];
+#pragma unroll
+  for (int m = 0; m < STZ_MODES; m++) accd[m] = (double)acc[m];
+  block_mode_sums(accd, f.part, kp.nblk, b);
+  const unsigned nb = block_sum_u(neg);
+  if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
+  if (!last_block(ctl, kp.nblk)) return;
+
+  // ---- last block: select and commit
+  __shared__ int sh_kind;
+  __shared__ double sh_T, sh_R;
+  __shared__ double sh_inc2[TH];
+  __shared__ long long sh_site;
+  __shared__ int sh_mode;
+  __shared__ double sh_margin;
+  const long long P = (long long)STZ_MODES * kp.nblk;
+  const long long ch = (P + TH - 1) / TH;
+  const long long q0 = threadIdx.x * ch, q1 = min(q0 + ch, P);
+  double S = 0;
+  for (long long p = q0; p < q1; p++) S += f.part[p];
+  block_incl_scan(S, sh_inc2);
+  if (threadIdx.x == 0) {
+    ctl->ticket = 0;
+    ctl->has_pend = 0;
+    for (int c = 0; c < 6; c++) ctl->U[c] = 0;
+    ctl->step++;
+    const double Rraw = sh_inc2[TH - 1];
+    const double R = Rraw * kp.rate_scale;
+    sh_R = Rraw;
+    ctl->total_rate = R;
+    if (ctl->neg_count > 0) {
+      sh_kind = kAthermal;
+      ctl->halt = 1;
+      ctl->halt_reason = kHaltAthermal;
+    } else if (!(R > 0) || !isfinite(R)) {
+      sh_kind = kNone;
+      ctl->status = STZ_ERR_NAN;
+      ctl->halt = 1;
+      ctl->halt_reason = kHaltError;
+    } else {
+      const double t_kmc = 1 / R;
+      if (t_kmc < kp.dt) {
+        sh_kind = kThermal;
+        ctl->kstep++;
+        const double dice = mt_uniform(&ctl->rng);
+        sh_T = dice * Rraw;
+        ctl->t_kmc = t_kmc;
+        if (!(dice > 0)) {
+          sh_kind = kNone;
+          ctl->status = STZ_ERR_NO_EVENT;
+          ctl->halt = 1;
+          ctl->halt_reason = kHaltError;
+        }
+      } else {
+        sh_kind = kElastic;
+      }
+    }
+    ctl->neg_count = 0;
+    ctl->step_kind = sh_kind;
+  }
+  __syncthreads();
+  const int kind = sh_kind;
+  if (kind == kThermal) {
+    double zero[6] = {0, 0, 0, 0, 0, 0};
+    search_event<2>(kp, f, zero, 0.0, sh_T, &sh_site, &sh_mode, &sh_margin);
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  if (kind == kThermal) {
+    const long long s = sh_site;
+    const int m = sh_mode;
+    if (s < 0) {
+      ctl->status = STZ_ERR_NO_EVENT;
+      ctl->halt = 1;
+      ctl->halt_reason = kHaltError;
+      ctl->step_kind = kNone;
+      return;
+    }
+    if (sh_margin < 1e-12 * sh_R) ctl->near_ties++;
+    double zero[6] = {0, 0, 0, 0, 0, 0};
+    const double q = site_Q<2>(kp, f, zero, 0.0, s, m);
+    // eigenstrain (FP64) and the incremental "solve"
+    for (int c = 0; c < 6; c++) {
+      f.prev_deps[c * N + s] = kp.modes[m][c];
+      f.eps0[c * N + s] += kp.modes[m][c];
+      ctl->eps0_sum[c] += kp.modes[m][c];
+    }
+    double ebar_sol[6], dA[6], CdA[6];
+    for (int c = 0; c < 6; c++) {
+      ebar_sol[c] = ctl->eps_avg[c];
+      dA[c] = ebar_sol[c] - ctl->eps_avg_applied[c];
+    }
+    apply_C(kp, dA, CdA);
+    double unew[6];
+    for (int c = 0; c < 6; c++) {
+      ctl->U[c] = CdA[c] - ctl->u[c];
+      ctl->eps_avg_applied[c] = ebar_sol[c];
+      ctl->u[c] = 0;
+    }
+    solved_mean_stress(kp, ctl, ebar_sol, ctl->stress);
+    load_after_event(kp, ctl, ctl->t_kmc);
+    for (int c = 0; c < 6; c++) {
+      unew[c] = ctl->u[c];
+      ctl->U[c] += unew[c];
+    }
+    ctl->has_pend = 1;
+    ctl->pend_site = s;
+    ctl->pend_mode = m;
+    ctl->sel_site = s;
+    ctl->sel_mode = m;
+    ctl->sel_q = q;
+    ctl->totime += ctl->t_kmc;
+    log_event(kp, f, ctl, STZ_EV_THERMAL, s, m, ctl->totime, ctl->t_kmc, q, sh_R * kp.rate_scale);
+    if (kp.resolve_period > 0 && ctl->kstep >= ctl->next_resolve) {
+      ctl->halt = 1;
+      ctl->halt_reason = kHaltResolve;
+    }
+  } else if (kind == kElastic) {
+    ctl->estep++;
+    ctl->totime += kp.dt;
+    double u0[6];
+    for (int c = 0; c < 6; c++) u0[c] = ctl->u[c];
+    elastic_step(kp, ctl);
+    for (int c = 0; c < 6; c++) ctl->U[c] = ctl->u[c] - u0[c];
+    log_event(kp, f, ctl, STZ_EV_ELASTIC, -1, -1, ctl->totime, kp.dt, 0.0, sh_R * kp.rate_scale);
+  } else {
+    return;
+  }
+  if (print_check(kp, ctl)) {
+    ctl->print_done = 1;
+    ctl->halt = 1;
+    ctl->halt_reason = kHaltPrint;
+    return;
+  }
+  if (!ctl->halt) stop_check(kp, ctl);
+  ctl->step_kind = kNone;
+}
+
+// After a full FP64 re-solve into sdev (mixed form).
+__global__ void k_mixed_after_resolve(KParams kp, Fields f, int kind) {
+  Ctl* ctl = f.ctl;
+  ctl->has_pend = 0;
+  for (int c = 0; c < 6; c++) ctl->U[c] = 0;
+  if (kind == 0) {
+    for (int c = 0; c < 6; c++) {
+      ctl->eps_avg_applied[c] = ctl->eps_avg[c];
+      ctl->u[c] = 0;
+    }
+  }
+  (void)kp;
+}
+
+// ------------------------------------------------------------ misc
+__global__ void k_q_mode(KParams kp, Fields f, int mode, double* out, int model) {
+  Ctl* ctl = f.ctl;
+  double u[6];
+  for (int c = 0; c < 6; c++) u[c] = ctl->u[c];
+  const double totime = ctl->totime;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < kp.N; s += (long long)gridDim.x * blockDim.x) {
+    if (model == 0) out[s] = site_Q<0>(kp, f, u, totime, s, mode);
+    else if (model == 1) out[s] = site_Q<1>(kp, f, u, totime, s, mode);
+    else out[s] = site_Q<2>(kp, f, u, totime, s, mode);
+  }
+}
+
+__device__ __forceinline__ void dev5(const double* s, double* d) {
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
+  d[0] = (s[0] - s[1]) * r2;
+  d[1] = (2.0 * s[2] - s[0] - s[1]) * r6;
+  d[2] = q2 * s[3];
+  d[3] = q2 * s[4];
+  d[4] = q2 * s[5];
+}
+
+__global__ void k_dev_from_sig(KParams kp, const double* sig, float* sdev) {
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < kp.N; s += (long long)gridDim.x * blockDim.x) {
+    double v[6], d[5];
+    for (int c = 0; c < 6; c++) v[c] = sig[c * kp.N + s];
+    dev5(v, d);
+    for (int k = 0; k < 5; k++) sdev[k * kp.N + s] = (float)d[k];
+  }
+}
+
+// Column b of the response table: K[a][b](d) = e_a : sigma^(b)(d) for d in
+// the octant 0 <= d_i <= n_i/2, stored in the packed upper triangle.
+__global__ void k_ktab_column(KParams kp, const double* sig, float* ktab, int b) {
+  const long long ts = (long long)kp.kt1 * kp.kt2, tn = (long long)kp.kt0 * ts;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tn; t += (long long)gridDim.x * blockDim.x) {
+    const int d2 = (int)(t % kp.kt2);
+    const int d1 = (int)((t / kp.kt2) % kp.kt1);
+    const int d0 = (int)(t / ts);
+    const long long s = ((long long)d0 * kp.n1 + d1) * kp.n2 + d2;
+    double v[6], d[5];
+    for (int c = 0; c < 6; c++) v[c] = sig[c * kp.N + s];
+    dev5(v, d);
+    for (int a = 0; a <= b; a++) {
+      // packed index of (a, b), a <= b, row-major upper triangle
+      const int idx = a * 5 - a * (a - 1) / 2 + (b - a);
+      ktab[idx * tn + t] = (float)d[a];
+    }
+  }
+}
+
+__global__ void k_fill_f32(const double* in, float* out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+__global__ void k_l2_flush(uint4* buf, long long n, unsigned v) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    buf[i] = make_uint4(v, v + 1, v + 2, (unsigned)i);
+}
+
+}  // namespace
+
+void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st) {
+  if (kp.model == STZ_MODEL_REF2D) k_rate64<0><<<kp.nblk, TH, 0, st>>>(kp, f);
+  else k_rate64<1><<<kp.nblk, TH, 0, st>>>(kp, f);
+}
+
+void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
+  if (update_only) k_mixed<1><<<kp.nblk, TH, 0, st>>>(kp, f);
+  else k_mixed<0><<<kp.nblk, TH, 0, st>>>(kp, f);
+}
+
+void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t st) {
+  const long long nb = std::min<long long>((kp.N + TH - 1) / TH, 152LL * 8);
+  k_ath_mark<<<(unsigned)nb, TH, 0, st>>>(kp, f, mixed);
+  k_ath_commit<<<1, TH, 0, st>>>(kp, f, mixed);
+}
+
+void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st) {
+  k_post_a<<<1, 1, 0, st>>>(kp, f);
+  k_post_print<<<1, 1, 0, st>>>(kp, f);
+}
+
+void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st) { k_post_b<<<1, 1, 0, st>>>(kp, f); }
+
+void launch_mixed_after_resolve(const KParams& kp, const Fields& f, int kind, cudaStream_t st) {
+  k_mixed_after_resolve<<<1, 1, 0, st>>>(kp, f, kind);
+}
+
+void launch_q_mode(const KParams& kp, const Fields& f, int mode, double* out, cudaStream_t st) {
+  const int model = kp.model == STZ_MODEL_REF2D ? 0 : (f.sdev ? 2 : 1);
+  const long long nb = std::min<long long>((kp.N + 255) / 256, 4096);
+  k_q_mode<<<(unsigned)nb, 256, 0, st>>>(kp, f, mode, out, model);
+}
+
+void launch_dev_from_sig(const KParams& kp, const double* sig, float* sdev, cudaStream_t st) {
+  const long long nb = std::min<long long>((kp.N + 255) / 256, 4096);
+  k_dev_from_sig<<<(unsigned)nb, 256, 0, st>>>(kp, sig, sdev);
+}
+
+void launch_ktab_column(const KParams& kp, const double* sig, float* ktab, int b, cudaStream_t st) {
+  const long long tn = (long long)kp.kt0 * kp.kt1 * kp.kt2;
+  const long long nb = std::min<long long>((tn + 255) / 256, 4096);
+  k_ktab_column<<<(unsigned)nb, 256, 0, st>>>(kp, sig, ktab, b);
+}
+
+void launch_fill_f32(const double* in, float* out, long long n, cudaStream_t st) {
+  const long long nb = std::min<long long>((n + 255) / 256, 4096);
+  k_fill_f32<<<(unsigned)nb, 256, 0, st>>>(in, out, n);
+}
+
+void launch_l2_flush(void* buf, size_t bytes, cudaStream_t st) {
+  const long long n = (long long)(bytes / sizeof(uint4));
+  static unsigned v = 1;
+  k_l2_flush<<<152 * 4, 256, 0, st>>>(reinterpret_cast<uint4*>(buf), n, v++);
+}
+
+}  // namespace stz

@@ -1,0 +1,35 @@
+// kmc.cuh -- launch wrappers of the KMC step kernels (kmc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "stz_internal.h"
+
+namespace stz {
+
+constexpr int kRateThreads = 256;
+
+// Rate kernel of the FP64 forms (ActEnergy + KMC rates + selection/commit in
+// the last block). model: STZ_MODEL_REF2D or STZ_MODEL_GLOBAL3D.
+void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
+// Mixed form: incremental stress update + rates + selection/commit.
+// update_only: apply the pending transformation and uniform change, nothing else.
+void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
+// Athermal avalanche (evolution.c:47-100): mark sites, then commit in order.
+void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t st);
+// Bookkeeping after the solve of a step (loading, clock, print check) and
+// after the optional print re-solve (stop checks, targets).
+void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st);
+void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st);
+// Reset of the incremental state after a full re-solve (mixed form).
+// kind 0: field solved with the current mean strain (print / athermal);
+// kind 1: periodic re-solve with the applied mean strain (field unchanged).
+void launch_mixed_after_resolve(const KParams& kp, const Fields& f, int kind, cudaStream_t st);
+// Q of one mode at every site for the current field.
+void launch_q_mode(const KParams& kp, const Fields& f, int mode, double* out, cudaStream_t st);
+// Mixed-form helpers: deviatoric coordinates of an FP64 field, response table.
+void launch_dev_from_sig(const KParams& kp, const double* sig, float* sdev, cudaStream_t st);
+void launch_ktab_column(const KParams& kp, const double* sig, float* ktab, int b, cudaStream_t st);
+void launch_fill_f32(const double* in, float* out, long long n, cudaStream_t st);
+void launch_l2_flush(void* buf, size_t bytes, cudaStream_t st);
+
+}  // namespace stz

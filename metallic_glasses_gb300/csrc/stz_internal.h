@@ -1,0 +1,149 @@
+// stz_internal.h -- engine internals shared by the host and device sources.
+#pragma once
+
+#include <cstdarg>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/stz_api.h"
+#include "mt19937.cuh"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#else
+typedef struct CUstream_st* cudaStream_t;
+typedef struct CUevent_st* cudaEvent_t;
+typedef struct CUgraphExec_st* cudaGraphExec_t;
+#endif
+
+namespace stz {
+
+void set_error(const char* fmt, ...);
+
+// Physical constants of the reference (bmg.h:71-77).
+constexpr double kEvInJ = 1.60217733e-19;
+constexpr double kJInEv = 1 / kEvInJ;
+constexpr double kBoltz = 1.380658e-23;
+constexpr double kEpsilon = 1e-17;
+
+enum StepKind { kThermal = 0, kAthermal = 1, kElastic = 2, kNone = -1 };
+
+enum HaltReason {
+  kHaltNone = 0,
+  kHaltAthermal = 1,   // mixed path: an avalanche needs the FFT path
+  kHaltResolve = 2,    // mixed path: periodic FP64 re-solve due
+  kHaltPrint = 3,      // mixed path: print re-solve due
+  kHaltStop = 4,       // end strain / instability
+  kHaltError = 5,
+  kHaltTarget = 6      // requested number of events / steps reached
+};
+
+// Device-resident control block: every scalar of the simulation state plus
+// the per-step flags that steer the kernels of a step. One per context.
+struct Ctl {
+  double totime;
+  double eps_avg[6];         // EpsAvg
+  double eps_avg_applied[6]; // mean strain the stored field was solved with
+  double stress[6];          // Stress
+  double u[6];               // uniform stress added to the field since its solve
+  double eps0_sum[6];        // sum over sites of the eigenstrain
+  double last_print_strain;
+  double t_kmc;              // clock advance of the current thermal event
+  double U[6];               // incremental path: pending uniform stress change
+  double stress_err_max, stress_err_rms;
+  double total_rate;         // R of the last selection
+  double sel_q;              // Q of the last selected (site, mode)
+  long long step, kstep, astep, estep, n_print;
+  long long nlog, nlog_dropped, near_ties;
+  long long log_base;        // first log entry not yet copied to the host
+  long long max_kstep, max_step;  // halt targets (absolute), < 0 = none
+  long long next_resolve;    // mixed: kstep at which the periodic re-solve is due
+  unsigned long long neg_count;   // (mode, site) pairs with Q < 0 this step
+  int step_kind;
+  int solve_req;             // an FFT solve of the current phase is requested
+  int print_done;            // the print of this step re-solved the field
+  int stopped;
+  int status;                // sticky STZ_* error
+  int halt, halt_reason;
+  int has_pend;              // incremental path: a transformation is pending
+  int pend_mode;
+  long long pend_site;
+  unsigned int ticket;       // last-block-done counter of the rate kernels
+  int sel_mode;
+  long long sel_site;
+  int ath_count;
+  MT rng;
+};
+
+// Device fields. Layout: component-major structure of arrays, site index
+// s = (i0 * n1 + i1) * n2 + i2 (i2 fastest), 8-byte aligned rows.
+struct Fields {
+  double* eps0 = nullptr;    // [nc][N] accumulated eigenstrain (FP64 always)
+  double* sig = nullptr;     // [nc][N] stress (FP64 forms)
+  float* sdev = nullptr;     // [5][N] deviatoric stress coordinates (mixed form)
+  double* dF = nullptr;      // [N] barrier (GLOBAL3D)
+  float* dF32 = nullptr;     // [N] barrier (mixed form)
+  double* Q0 = nullptr;      // [MODES][N] (REF2D)
+  double* deps = nullptr;    // [MODES][3][N] (REF2D)
+  double* prev_deps = nullptr;  // [nc][N]
+  double* perm_soft = nullptr;
+  double* temp_soft = nullptr;
+  double* tlast = nullptr;
+  signed char* amark = nullptr; // [N] athermal marks (mode+1, 0 = none)
+  double* part = nullptr;    // [MODES][nblk] per (mode, block) rate sums
+  void* spec = nullptr;      // [nc][Nk] complex FP64 spectrum
+  float* ktab = nullptr;     // mixed: [15][kt0][kt1][kt2] response table
+  stz_event* log = nullptr;  // event ring
+  Ctl* ctl = nullptr;
+  double* scratch = nullptr;  // small scratch (error statistics nobody reads)
+};
+
+// Constant parameters of one context, passed to kernels by value.
+struct KParams {
+  int model, nc, n0, n1, n2, nh;
+  long long N, Nk;
+  int nblk, bsites;          // rate kernel: blocks and sites per block
+  int loading, softening, sf_scheme, no_subtract_error, shear_quirk;
+  double lambda, mu, young, poisson;
+  double kT, vt, V0, dt, gamma0;
+  double perm_soft, temp_soft, perm_soft_cap, t_temp;
+  double end_strain, strain_rate, strain_increment, print_thr;
+  double applied[6];
+  double modes[STZ_MODES][6];      // GLOBAL3D mode table (Voigt, tensor shear)
+  // mixed form
+  float mdev[STZ_MODES][5];        // mode deviatoric coords * (c/2) * log2(e)/kT
+  float a_scale;                   // log2(e)/kT
+  float q_ref;                     // reference barrier of the scaled rates
+  double rate_scale;               // vt * exp(-q_ref/kT): true rate per scaled unit
+  float mdev_raw[STZ_MODES][5];    // mode deviatoric coords (unscaled)
+  int kt0, kt1, kt2;               // response-table extents (n/2+1)
+  long long log_cap;
+  int resolve_period;
+};
+
+}  // namespace stz
+
+struct stz_ctx {
+  stz_params p{};
+  stz::KParams kp{};
+  stz::Fields f{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+  void* fft = nullptr;               // FFT plan (fft.cu)
+  int64_t launches = 0;
+  std::vector<stz_event> host_log;   // drained events
+  long long drained = 0;
+  stz::Ctl host_ctl{};
+  double ktime_ms = 0;
+  int64_t ktime_n = 0;
+  int use_graph = 1;
+  cudaGraphExec_t graph = nullptr;
+  int graph_batch = 0;
+  int64_t graph_launches = 0;        // kernels per graph launch
+  void* l2buf = nullptr;
+  size_t l2flush_bytes = 0;
+  double* err_dev = nullptr;         // [3] error sums of the periodic re-solve
+  double err_max = 0, err_rms = 0;
+};

@@ -1,0 +1,53 @@
+/*
+ * TEST INFRASTRUCTURE ONLY. Single-rank stand-in for the FFTW 2.x MPI
+ * interface used by the reference STZ code: an unnormalised complex 2D DFT
+ * (sign -1 forward, +1 backward) in normal order, computed by the oracle's
+ * FFT. The whole grid is the local slab (lnx = NX, lxs = 0).
+ */
+#ifndef STZ_SHIM_FFTW_MPI_H
+#define STZ_SHIM_FFTW_MPI_H
+#include <stddef.h>
+#include "mpi.h"
+
+typedef double fftw_real;
+typedef struct { fftw_real re, im; } fftw_complex;
+typedef enum { FFTW_FORWARD = -1, FFTW_BACKWARD = 1 } fftw_direction;
+typedef enum { FFTW_NORMAL_ORDER = 0, FFTW_TRANSPOSED_ORDER = 1 } fftwnd_mpi_output_order;
+#define FFTW_ESTIMATE 0
+typedef struct stz_shim_plan* fftwnd_mpi_plan;
+
+fftwnd_mpi_plan fftw2d_mpi_create_plan(MPI_Comm comm, int nx, int ny, fftw_direction dir, int flags);
+void fftwnd_mpi_local_sizes(fftwnd_mpi_plan p, int* local_nx, int* local_x_start,
+                            int* local_ny_after_transpose, int* local_y_start_after_transpose,
+                            int* total_local_size);
+void fftwnd_mpi(fftwnd_mpi_plan p, int n_fields, fftw_complex* local_data, fftw_complex* work,
+                fftwnd_mpi_output_order order);
+void fftwnd_mpi_destroy_plan(fftwnd_mpi_plan p);
+void* fftw_malloc(size_t n);
+void fftw_free(void* p);
+#endif
+
+/*
+ * Outside the include guard on purpose. The reference fixes the grid with
+ * '#define NX 512' / '#define NY 512' in bmg.h, and every translation unit
+ * includes this header a second time (through my_fft.h) after bmg.h. When the
+ * build passes -DSTZ_SHIM_NX=.. -DSTZ_SHIM_NY=.., the second inclusion
+ * replaces the grid size for the rest of the translation unit, so the
+ * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR swaps the
+ * loading switch of bmgFlags.h the same way.
+ */
+#if defined(NX) && defined(STZ_SHIM_NX)
+#undef NX
+#define NX STZ_SHIM_NX
+#endif
+#if defined(NY) && defined(STZ_SHIM_NY)
+#undef NY
+#define NY STZ_SHIM_NY
+#endif
+#if defined(H_BMGFLAGS) && defined(STZ_SHIM_LOAD_SHEAR)
+#undef TENSION
+#undef COMPRESSION
+#ifndef SHEAR
+#define SHEAR
+#endif
+#endif

@@ -1,0 +1,66 @@
+/*
+ * stz_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement (FP64, plain C) of the reference's STZ kinetic Monte Carlo
+ * step, used as the correctness oracle by tests/, by __graft_entry__.smoke()
+ * and as the CPU baseline leg of bench.py. Nothing in the product links it.
+ *
+ * Parity pinning: the 2D model is checked against the reference's own sources
+ * compiled unmodified against single-rank stand-ins for MPI, FFTW 2 and GSL
+ * (oracle/Makefile, target _ref/ref2d) and against fixtures produced by that
+ * build (tests/golden/). The 3D model generalises the same formulas; there is
+ * no reference code for 3D, so its parity rests on the 2D pinning plus the
+ * invariants tested in tests/ (equilibrium, compatibility, mean stress).
+ *
+ * Third-party algorithms restated here (absent from the reference tree):
+ *   GSL mt19937 generator (gsl_rng_default; rng/mt.c of GSL 1.x/2.x, version
+ *     not pinned by the reference Makefile), gsl_rng_uniform = u32 / 2^32,
+ *     gsl_rng_uniform_pos rejects 0, gsl_ran_gaussian = polar Box-Muller as
+ *     restated by the reference itself at init.c:207-223.
+ *   FFTW 2.x fftwnd_mpi: unnormalised complex DFT, sign -1 forward, +1 backward.
+ */
+#ifndef STZ_ORACLE_H
+#define STZ_ORACLE_H
+
+#include <stdint.h>
+#include "../include/stz_api.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- GSL-convention MT19937 ------------------------------------------------ */
+typedef struct or_rng { uint32_t mt[624]; int mti; } or_rng;
+void     or_rng_seed(or_rng* r, unsigned long s);
+uint32_t or_rng_get(or_rng* r);
+double   or_rng_uniform(or_rng* r);
+double   or_rng_uniform_pos(or_rng* r);
+double   or_ran_gaussian(or_rng* r, double sigma);
+
+/* ---- complex FFT on interleaved (re,im) doubles ---------------------------- */
+/* In-place unnormalised DFT of an n0 x n1 x n2 array (n2 fastest) along every
+ * axis of extent > 1. sign = -1 forward, +1 backward. Extents: 2^a 3^b. */
+int  or_fft3(int n0, int n1, int n2, double* data, int sign);
+
+/* ---- model ------------------------------------------------------------------ */
+typedef struct or_model or_model;
+
+or_model* or_create(const stz_params* p, int* status);
+void      or_destroy(or_model* m);
+/* The driver loop (bmg.c:138-411) until max_steps iterations or max_events
+ * thermal events, or a stop condition. Returns a stz status code. */
+int  or_run(or_model* m, int64_t max_steps, int64_t max_events);
+int  or_solve(or_model* m);        /* InhomogeneousStressSolver(...,0) */
+int  or_get_scalars(or_model* m, stz_scalars* out);
+int64_t or_num_events(or_model* m);
+int  or_get_events(or_model* m, int64_t first, stz_event* out, int64_t cap, int64_t* n);
+int  or_get_field(or_model* m, int which, int comp, double* out, int64_t count);
+int  or_set_field(or_model* m, int which, int comp, const double* in, int64_t count);
+int  or_elastic_energy(or_model* m, double* out);
+/* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
+int  or_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,116 @@
+"""Generate the parity fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own STZ sources (compiled unmodified against the
+single-rank stand-ins of oracle/shim by oracle/build_oracle.py) in a scratch
+directory and stores, per case:
+  <case>.npz   X     int64 [K, 4]  one row per VoxelShearTransform call:
+                                   (step, kind 0 thermal / 1 athermal, site, mode)
+               S     float64 [M, 9] one row per driver step:
+                                   (step, kind 0/1/2, time, EpsAvg[3], Stress[3])
+               hdr   int64 [5]     (N, steps done, kstep, astep, estep)
+               sc    float64 [7]   (time, EpsAvg[3], Stress[3]) at the end
+               sigma, eps0  float64 [3, N]  final stress and eigenstrain
+               tlast, perm_soft, temp_soft  float64 [N]
+               deps_sum   float64 [3] sum over modes and sites of DEps0[m][c]
+and the MT19937 known answers of the GSL conventions (mt19937_kat.npz).
+
+Only this script reads the reference tree; tests read the .npz files.
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from metallic_glasses_gb300 import configs  # noqa: E402
+from oracle.build_oracle import build_ref2d, build_oracle_lib  # noqa: E402
+
+CASES = {
+    # name: (nx, ny, loading, input overrides, thermal events)
+    "ref2d_64_tension_s123": (64, 64, "TENSION", {"end": "0.5"}, 10000),
+    "ref2d_32_shear_s7": (32, 32, "SHEAR", {"end": "0.5", "seed": "7"}, 150),
+    # runs into the reference's SHEAR instability stop after its first avalanche
+    "ref2d_32_shear_stop_s7": (32, 32, "SHEAR", {"end": "0.5", "seed": "7"}, 100000),
+    "ref2d_32_tension_nosoft_s5": (32, 32, "TENSION", {"end": "0.5", "seed": "5", "soft": "0"}, 3000),
+}
+
+
+def run_case(name, nx, ny, loading, overrides, events):
+    exe = build_ref2d(nx, ny, loading)
+    d = tempfile.mkdtemp(prefix="stz_ref_")
+    configs.write_input(os.path.join(d, "input"), **overrides)
+    env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS=str(events),
+               STZ_REF_DUMP=os.path.join(d, "dump.bin"))
+    subprocess.run([exe], cwd=d, env=env, stdout=subprocess.DEVNULL, check=True)
+    X, S = [], []
+    for line in open(os.path.join(d, "log.txt")):
+        t = line.split()
+        if t[0] == "X":
+            X.append([int(v) for v in t[1:5]])
+        else:
+            S.append([float(v) for v in t[1:]])
+    raw = open(os.path.join(d, "dump.bin"), "rb").read()
+    hdr = np.frombuffer(raw[:40], np.int64).copy()
+    sc = np.frombuffer(raw[40:96], np.float64).copy()
+    N = int(hdr[0])
+    arr = np.frombuffer(raw[96:], np.float64)
+    off = 0
+
+    def take(k):
+        nonlocal off
+        v = arr[off:off + k].copy()
+        off += k
+        return v
+
+    sigma = take(3 * N).reshape(3, N)
+    eps0 = take(3 * N).reshape(3, N)
+    deps = take(60 * N).reshape(20, 3, N)
+    take(20 * N)  # Q0
+    tlast = take(N)
+    perm = take(N)
+    temp = take(N)
+    out = os.path.join(HERE, name + ".npz")
+    S = np.array(S, np.float64)
+    # per-step time for every step; mean strain and stress for every 10th
+    np.savez_compressed(out, X=np.array(X, np.int64), S=S[:, :3], S10=S[::10], hdr=hdr, sc=sc, sigma=sigma,
+                        eps0=eps0, tlast=tlast, perm_soft=perm, temp_soft=temp, deps_sum=deps.sum(axis=(0, 2)),
+                        nx=nx, ny=ny, loading=loading, overrides=repr(overrides), events=events)
+    print(name, "transforms", len(X), "steps", len(S), "hdr", hdr, "->", out)
+
+
+def mt_kat():
+    """MT19937 known answers: C++ std::mt19937 (the same generator and seeding
+    recurrence) for seed 5489 gives 4123659995 as its 10000th output; the
+    first outputs for seeds 123 and 4357 come from g++'s std::mt19937."""
+    src = r'''
+#include <random>
+#include <cstdio>
+int main(){ std::mt19937 a(5489u); unsigned v=0; for(int i=0;i<10000;i++) v=a(); printf("%u\n", v);
+ for (unsigned s : {123u, 4357u}) { std::mt19937 g(s); for(int i=0;i<8;i++) printf("%u ", (unsigned)g()); printf("\n"); }
+ std::mt19937 g(123u); for(int i=0;i<700;i++) g(); for(int i=0;i<4;i++) printf("%u ", (unsigned)g()); printf("\n"); }
+'''
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "k.cpp"), "w") as f:
+        f.write(src)
+    subprocess.run(["g++", "-O1", "-o", os.path.join(d, "k"), os.path.join(d, "k.cpp")], check=True)
+    outp = subprocess.run([os.path.join(d, "k")], capture_output=True, text=True, check=True).stdout.split("\n")
+    v10000 = int(outp[0])
+    s123 = [int(x) for x in outp[1].split()]
+    s4357 = [int(x) for x in outp[2].split()]
+    s123_700 = [int(x) for x in outp[3].split()]
+    np.savez(os.path.join(HERE, "mt19937_kat.npz"), v10000=v10000, s123=np.array(s123, np.uint32),
+             s4357=np.array(s4357, np.uint32), s123_after700=np.array(s123_700, np.uint32))
+    print("mt19937 kat", v10000, s123[:2])
+
+
+if __name__ == "__main__":
+    build_oracle_lib()
+    mt_kat()
+    for name, (nx, ny, loading, ov, ev) in CASES.items():
+        run_case(name, nx, ny, loading, ov, ev)

@@ -1,0 +1,63 @@
+"""The C-ABI library loads without a GPU, exports every entry point declared
+in include/*.h, and its structs match the Python mirror (CPU only, no
+compute calls)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*([a-zA-Z_][A-Za-z0-9_]*)\s*\(", src, re.M):
+            name = m.group(1)
+            if name not in ("if", "while", "for", "switch", "return", "sizeof"):
+                names.add(name)
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    names = declared_functions()
+    assert "stz_create" in names and "stz_run" in names
+    missing = [n for n in names if not hasattr(engine_lib, n)]
+    assert not missing, "declared but not exported: %s" % missing
+
+
+def test_struct_sizes_match(engine_lib):
+    from metallic_glasses_gb300 import api
+    assert engine_lib.stz_sizeof(0) == C.sizeof(api.Params)
+    assert engine_lib.stz_sizeof(1) == C.sizeof(api.Event)
+    assert engine_lib.stz_sizeof(2) == C.sizeof(api.Scalars)
+
+
+def test_input_file_parse_matches_reference_init(engine_lib, tmp_path):
+    from metallic_glasses_gb300 import api, configs
+    path = configs.write_input(str(tmp_path / "input"))
+    p = api.params_from_input(path)
+    E, nu = 69.46, 0.365 * 2          # LOW_T doubles nu (init.c:26)
+    assert p.young == E and p.poisson == nu
+    assert p.mu == E / (2 + 2 * nu)
+    assert p.lambda_ == E * nu / (1 - nu * nu)
+    assert p.q0_mean == 2.0 and p.seed == 123 and p.softening == 1 and p.print_period == 5
+    assert p.strain_rate == 1e-4 and p.strain_increment == 1e-4 and p.end_strain == 0.06
+
+
+def test_bad_input_reports_io_error(engine_lib, tmp_path):
+    from metallic_glasses_gb300 import api
+    bad = tmp_path / "input"
+    bad.write_text("nothing useful\n")
+    with pytest.raises(api.StzError) as ei:
+        api.params_from_input(str(bad))
+    assert ei.value.code == api.ERR_IO
+    with pytest.raises(api.StzError):
+        api.params_from_input(str(tmp_path / "missing"))

@@ -1,0 +1,60 @@
+"""The oracle against the reference: fixtures produced by the reference's own
+sources (tests/golden/make_golden.py). CPU only."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from metallic_glasses_gb300 import api
+from ref2d_cases import CASES, params_for
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_reference_bitwise(oracle_lib, engine_lib, case):
+    g = golden(case)
+    p = params_for(g)
+    m = oracle_lib.Model(p)
+    hdr = g["hdr"]
+    m.run(max_steps=int(hdr[1]))
+    ev = m.events()
+    tr = ev[ev["kind"] != api.EV_ELASTIC]
+    X = g["X"]
+    # same (step, kind, site, mode) for every transformation
+    assert len(tr) == len(X)
+    assert np.array_equal(tr["step"], X[:, 0])
+    assert np.array_equal(tr["kind"], X[:, 1])
+    assert np.array_equal(tr["site"], X[:, 2])
+    assert np.array_equal(tr["mode"], X[:, 3])
+    sc = m.scalars()
+    assert [sc["step"], sc["kstep"], sc["astep"], sc["estep"]] == [int(v) for v in hdr[1:]]
+    # every step's clock
+    S = g["S"]
+    steps = np.unique(ev["step"])
+    assert len(steps) == len(S)
+    last_time = {}
+    for e in ev:
+        last_time[int(e["step"])] = e["time"]
+    t_or = np.array([last_time.get(int(s), np.nan) for s in S[:, 0]])
+    thermal_or_elastic = S[:, 1] != 1
+    assert np.array_equal(t_or[thermal_or_elastic], S[thermal_or_elastic, 2])
+    # final fields, bit for bit
+    for c in range(3):
+        assert np.array_equal(m.field(api.FIELD_SIGMA, c), g["sigma"][c])
+        assert np.array_equal(m.field(api.FIELD_EPS0, c), g["eps0"][c])
+    assert np.array_equal(m.field(api.FIELD_TLAST), g["tlast"])
+    assert np.array_equal(m.field(api.FIELD_PERM_SOFT), g["perm_soft"])
+    assert np.array_equal(m.field(api.FIELD_TEMP_SOFT), g["temp_soft"])
+    deps = np.stack([m.field(api.FIELD_DEPS, k) for k in range(60)]).reshape(20, 3, -1)
+    assert np.allclose(deps.sum(axis=(0, 2)), g["deps_sum"], rtol=0, atol=1e-12)
+    assert sc["eps_avg"][:3] == list(g["sc"][1:4])
+    assert sc["stress"][:3] == list(g["sc"][4:7])
+
+
+def test_shear_instability_stop(oracle_lib, engine_lib):
+    """In SHEAR mode the reference's athermal correction zeroes the mean shear
+    stress and its divergence test (bmg.c:402) ends the run; the oracle does too."""
+    g = golden("ref2d_32_shear_stop_s7")
+    m = oracle_lib.Model(params_for(g))
+    m.run(max_steps=100000)
+    sc = m.scalars()
+    assert sc["stopped"] == 2
+    assert sc["step"] == int(g["hdr"][1])
