@@ -43,7 +43,10 @@ int dalloc(T** p, size_t count) {
     set_error("cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
     return STZ_ERR_NOMEM;
   }
+  // zero on the legacy stream and wait: the engine's own stream does not
+  // order itself after the legacy stream
   cudaMemset(*p, 0, sizeof(T) * count);
+  cudaDeviceSynchronize();
   return STZ_OK;
 }
 
@@ -224,6 +227,7 @@ int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
   a.gate = gate;
   a.out = kOutSig64;
   a.sig64 = c->f.sig;
+  a.msum = c->f.msum;
   a.spec = c->f.spec;
   a.fp32 = 0;
   return fft_solve(*plan_of(c), a, c->stream, &c->launches);
@@ -536,6 +540,8 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
     set_error("FFT plan for %dx%dx%d failed", kp.n0, kp.n1, kp.n2);
     return fail(st);
   }
+  kp.c2r_blocks = fft_c2r_blocks(*plan);
+  if (!mixed && (st = dalloc(&f.msum, (size_t)nc * kp.c2r_blocks))) return fail(st);
   MT rng;
   mt_seed(&rng, (unsigned long)p.seed);
   st = ref2d ? init_ref2d(c, &rng) : init_global3d(c, &rng);
@@ -590,7 +596,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
-                  f.tlast, f.amark, f.part, f.spec, f.ktab, f.log, f.ctl, f.scratch, c->err_dev, c->l2buf};
+                  f.tlast, f.amark, f.part, f.spec, f.ktab, f.log, f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fft) {
@@ -655,7 +661,18 @@ extern "C" int stz_solve(stz_ctx* c) {
     launch_mixed_after_resolve(c->kp, c->f, 0, c->stream);
   } else {
     solve_plain(c, nullptr, c->f.ctl->eps_avg);
-    double z[6] = {0, 0, 0, 0, 0, 0};
+    // Stress = mean of the solved field (AvgStress), u = 0
+    const int nc = c->kp.nc, nb = c->kp.c2r_blocks;
+    std::vector<double> ms((size_t)nc * nb);
+    CK(cudaMemcpyAsync(ms.data(), c->f.msum, sizeof(double) * ms.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double st6[6] = {0, 0, 0, 0, 0, 0}, z[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nc; k++) {
+      double acc = 0;
+      for (int b = 0; b < nb; b++) acc += ms[(size_t)k * nb + b];
+      st6[k] = acc / (double)c->kp.N;
+    }
+    CK(cudaMemcpyAsync(c->f.ctl->stress, st6, sizeof(st6), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->f.ctl->u, z, sizeof(z), cudaMemcpyHostToDevice, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));

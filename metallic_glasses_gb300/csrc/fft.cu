@@ -19,7 +19,12 @@
 // and keeps the real part of the inverse; on a Nyquist plane its operator at k
 // and at -k differ (g picks -1/2 for both), so the real part it keeps is the
 // result of the average of the two operators. This pass applies that average
-// explicitly, which keeps the spectrum Hermitian and the C2R exact.
+// explicitly, which keeps the spectrum Hermitian and the C2R exact. In 3D,
+// where the reference has no code, wave vectors with Nyquist components use the
+// average over every sign choice of those components; this differs from the
+// two-operator average only where two or more components sit on a Nyquist
+// plane, and makes the discrete Green's function symmetric under the
+// reflection of each axis (the incremental solver relies on that).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -331,10 +336,29 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
       const bool ny0 = ga.is3d && (ga.n0 % 2 == 0) && (2 * k0 == ga.n0);
       green_op<T, V>(nc, lam, mu, alpha, g, e, sig);
       if (ny2 || ny1 || ny0) {
-        T gm[3] = {ny2 ? -g[0] : g[0], ny1 ? -g[1] : g[1], ny0 ? -g[2] : g[2]};
-        V s2[6];
-        green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
-        for (int c = 0; c < nc; c++) sig[c] = V{(T)0.5 * (sig[c].x + s2[c].x), (T)0.5 * (sig[c].y + s2[c].y)};
+        if (nc == 3) {
+          // 2D: the reference's real part of a complex transform, i.e. the
+          // average of the operators at k and -k
+          T gm[3] = {ny2 ? -g[0] : g[0], ny1 ? -g[1] : g[1], ny0 ? -g[2] : g[2]};
+          V s2[6];
+          green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
+          for (int c = 0; c < nc; c++) sig[c] = V{(T)0.5 * (sig[c].x + s2[c].x), (T)0.5 * (sig[c].y + s2[c].y)};
+        } else {
+          // 3D: average over every sign choice of the Nyquist components,
+          // which keeps the discrete Green's function symmetric under the
+          // reflection of each axis
+          int nv = 1;
+          for (int sg = 1; sg < 8; sg++) {
+            if (((sg & 1) && !ny2) || ((sg & 2) && !ny1) || ((sg & 4) && !ny0)) continue;
+            T gm[3] = {(sg & 1) ? -g[0] : g[0], (sg & 2) ? -g[1] : g[1], (sg & 4) ? -g[2] : g[2]};
+            V s2[6];
+            green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
+            for (int c = 0; c < nc; c++) sig[c] = vadd(sig[c], s2[c]);
+            nv++;
+          }
+          const T inv = (T)1 / (T)nv;
+          for (int c = 0; c < nc; c++) sig[c] = V{sig[c].x * inv, sig[c].y * inv};
+        }
       }
     }
     for (int c = 0; c < nc; c++) res[(c * L + l) * ld + p] = sig[c];
@@ -370,7 +394,8 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
                                                const typename VT<T>::V* __restrict__ tw_p, double invN,
                                                double* __restrict__ sig64, float* __restrict__ sig32,
                                                float* __restrict__ sdev, const double* __restrict__ uadd,
-                                               double* __restrict__ err, const int* gate) {
+                                               double* __restrict__ err, double* __restrict__ msum,
+                                               const int* gate) {
   using V = typename VT<T>::V;
   if (gate && *gate == 0) return;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -379,7 +404,9 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
   V* b = a + L * ld;
   double* o = reinterpret_cast<double*>(b + L * ld);  // [nc][L][n2] for the deviatoric epilogue
   const long long r0 = (long long)blockIdx.x * L;
+  __shared__ double msred[8];
   for (int c = 0; c < nc; c++) {
+    double part = 0;
     const V* src = in + (long long)c * Nk;
     for (int idx = threadIdx.x; idx < L * nh; idx += blockDim.x) {
       const int l = idx / nh, k = idx - l * nh;
@@ -409,11 +436,23 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
       const double x0 = (double)z.x * invN, x1 = (double)z.y * invN;
       if (OUT == kOutSig64) {
         reinterpret_cast<double2*>(sig64 + (long long)c * N)[(r * n2) / 2 + j] = make_double2(x0, x1);
+        part += x0 + x1;
       } else if (OUT == kOutSig32) {
         reinterpret_cast<float2*>(sig32 + (long long)c * N)[(r * n2) / 2 + j] = make_float2((float)x0, (float)x1);
       } else {
         o[(c * L + l) * n2 + 2 * j] = x0;
         o[(c * L + l) * n2 + 2 * j + 1] = x1;
+      }
+    }
+    if (OUT == kOutSig64 && msum) {
+      // deterministic block sum of this component (mean stress, AvgStress)
+      for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+      if ((threadIdx.x & 31) == 0) msred[threadIdx.x >> 5] = part;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += msred[k];
+        msum[(long long)c * gridDim.x + blockIdx.x] = t;
       }
     }
     __syncthreads();
@@ -584,15 +623,15 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   if (a.out == kOutSig64)
     k_c2r_x<T, kOutSig64><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, a.sig64, nullptr, nullptr,
-                                               nullptr, nullptr, a.gate);
+                                               nullptr, nullptr, a.msum, a.gate);
   else if (a.out == kOutSig32)
     k_c2r_x<T, kOutSig32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, a.sig32, nullptr,
-                                               nullptr, nullptr, a.gate);
+                                               nullptr, nullptr, nullptr, a.gate);
   else
     k_c2r_x<T, kOutDev32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, nullptr, a.sdev, a.uadd,
-                                               a.err, a.gate);
+                                               a.err, nullptr, a.gate);
   nl += 1;
   if (launches) *launches += nl;
   return STZ_OK;
@@ -638,6 +677,8 @@ int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
   return STZ_OK;
 }
 
+int fft_c2r_blocks(const FFTPlan& p) { return (int)(((long long)p.n0 * p.n1 + p.L_x - 1) / p.L_x); }
+
 void fft_plan_destroy(FFTPlan* p) {
   cudaFree(p->tw_h); cudaFree(p->tw_1); cudaFree(p->tw_0); cudaFree(p->tw_p);
   cudaFree(p->tw_hf); cudaFree(p->tw_1f); cudaFree(p->tw_0f); cudaFree(p->tw_pf);
@@ -680,7 +721,7 @@ int fft_filter_gaussian(const FFTPlan& p, double* field, double corr_len, void* 
                                                     p.L_y, p.s1, p.tw_1, nullptr);
   k_c2r_x<double, kOutSig64><<<gx.x, TH, p.smem_c2r, st>>>(sp, 1, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                           p.tw_h, p.tw_p, 1.0, field, nullptr, nullptr, nullptr,
-                                                          nullptr, nullptr);
+                                                          nullptr, nullptr, nullptr);
   return STZ_OK;
 }
 

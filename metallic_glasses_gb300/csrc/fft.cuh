@@ -37,6 +37,8 @@ struct FFTPlan {
 };
 
 int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc);
+// number of blocks of the C2R pass (the length of one component's msum row)
+int fft_c2r_blocks(const FFTPlan& p);
 void fft_plan_destroy(FFTPlan* p);
 
 struct SolveArgs {
@@ -50,6 +52,8 @@ struct SolveArgs {
   float* sig32;          // kOutSig32
   float* sdev;           // kOutDev32 (read for the error, then overwritten)
   double* err;           // kOutDev32: err[0] = max |d s|^2, err[1] = sum |d s|^2, err[2] = sum |s|^2
+  double* msum;          // kOutSig64, optional: per-(component, block) sums of the
+                         // solved field, [nc][fft_c2r_blocks] (for the mean stress)
   int fp32;              // run the transform in FP32 (eps converted on load)
   void* spec;            // [nc][Nk] complex scratch (double2, or float2 when fp32)
   int ortho_mean;        // 1: the k = 0 term is C:(N ebar - eps_hat(0)) (always 1 here)

@@ -55,6 +55,16 @@ __device__ void iso_inv(const KParams& kp, const double* s, double* e) {
   }
 }
 
+// AvgStress (elastic.c:733-752): mean of the solved field, from the per-block
+// sums the C2R pass left in msum (fixed summation order)
+__device__ void field_mean_stress(const KParams& kp, const Fields& f, double* out) {
+  for (int c = 0; c < kp.nc; c++) {
+    double s = 0;
+    for (int b = 0; b < kp.c2r_blocks; b++) s += f.msum[(long long)c * kp.c2r_blocks + b];
+    out[c] = s / (double)kp.N;
+  }
+}
+
 __device__ void solved_mean_stress(const KParams& kp, const Ctl* ctl, const double* ebar, double* out) {
   double e[6];
   for (int c = 0; c < kp.nc; c++) e[c] = ebar[c] - ctl->eps0_sum[c] / (double)kp.N;
@@ -720,13 +730,16 @@ __global__ void k_post_a(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->halt && ctl->step_kind == kNone) return;
   const int kind = ctl->step_kind;
+  const bool fieldmean = f.msum != nullptr;
   if (kind == kThermal) {
-    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (fieldmean) field_mean_stress(kp, f, ctl->stress);
+    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
     load_after_event(kp, ctl, ctl->t_kmc);
     ctl->totime += ctl->t_kmc;
   } else if (kind == kAthermal) {
-    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (fieldmean) field_mean_stress(kp, f, ctl->stress);
+    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
     if (kp.loading == STZ_LOAD_STRESS) {
       hold_stress(kp, ctl);
@@ -741,7 +754,6 @@ __global__ void k_post_a(KParams kp, Fields f) {
   }
   ctl->print_done = 0;
   ctl->solve_req = 0;
-  (void)f;
 }
 
 // print check after every step kind; requests the print re-solve
@@ -756,7 +768,8 @@ __global__ void k_post_b(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->step_kind == kNone) return;
   if (ctl->print_done) {
-    solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (f.msum) field_mean_stress(kp, f, ctl->stress);
+    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
   }
   ctl->print_done = 0;

@@ -96,6 +96,7 @@ struct Fields {
   stz_event* log = nullptr;  // event ring
   Ctl* ctl = nullptr;
   double* scratch = nullptr;  // small scratch (error statistics nobody reads)
+  double* msum = nullptr;     // [nc][c2r_blocks] block sums of the solved field
 };
 
 // Constant parameters of one context, passed to kernels by value.
@@ -119,6 +120,7 @@ struct KParams {
   int kt0, kt1, kt2;               // response-table extents (n/2+1)
   long long log_cap;
   int resolve_period;
+  int c2r_blocks;                  // blocks of the FFT's C2R pass (msum row length)
 };
 
 }  // namespace stz

@@ -452,6 +452,16 @@ static void homogeneous_solve(or_model* m, double* const* eps_in) {
     if (s == 0) g2 = 1.0;
     g[0] /= g2; g[1] /= g2; g[2] /= g2;
     if (D == 2) g[2] = 0;
+    /* 3D only: at wave vectors with Nyquist components the operator is
+     * averaged over the signs of those components (all 2^k choices), which
+     * keeps the discrete Green's function symmetric under reflections of each
+     * axis. The 2D path keeps the reference's operator unchanged. */
+    int nyq[3] = {0, 0, 0};
+    if (D == 3) {
+      nyq[0] = (m->n2 % 2 == 0) && (2 * i2 == m->n2);
+      nyq[1] = (m->n1 % 2 == 0) && (2 * i1 == m->n1);
+      nyq[2] = (m->n0 % 2 == 0) && (2 * i0 == m->n0);
+    }
     double er[6], ei[6], tr_r = 0, tr_i = 0;
     for (int c = 0; c < nc; c++) {
       er[c] = W[(size_t)c * 2 * N + 2 * s];
@@ -466,18 +476,27 @@ static void homogeneous_solve(or_model* m, double* const* eps_in) {
       tr[ci[c]][cj[c]] = vr; tr[cj[c]][ci[c]] = vr;
       ti[ci[c]][cj[c]] = vi; ti[cj[c]][ci[c]] = vi;
     }
-    double Fr[3], Fi[3], Gr = 0, Gi = 0;
-    for (int a = 0; a < 3; a++) {
-      Fr[a] = 0; Fi[a] = 0;
-      for (int b = 0; b < 3; b++) { Fr[a] += tr[a][b] * g[b]; Fi[a] += ti[a][b] * g[b]; }
+    double accr[6] = {0}, acci[6] = {0};
+    int nvar = 0;
+    for (int sgn = 0; sgn < 8; sgn++) {
+      if (((sgn & 1) && !nyq[0]) || ((sgn & 2) && !nyq[1]) || ((sgn & 4) && !nyq[2])) continue;
+      double gv[3] = {(sgn & 1) ? -g[0] : g[0], (sgn & 2) ? -g[1] : g[1], (sgn & 4) ? -g[2] : g[2]};
+      double Fr[3], Fi[3], Gr = 0, Gi = 0;
+      for (int a = 0; a < 3; a++) {
+        Fr[a] = 0; Fi[a] = 0;
+        for (int b = 0; b < 3; b++) { Fr[a] += tr[a][b] * gv[b]; Fi[a] += ti[a][b] * gv[b]; }
+      }
+      for (int a = 0; a < 3; a++) { Gr += gv[a] * Fr[a]; Gi += gv[a] * Fi[a]; }
+      for (int c = 0; c < nc; c++) {
+        int a = ci[c], b = cj[c];
+        accr[c] += (0.5 / mu) * (Fr[a] * gv[b] + Fr[b] * gv[a]) + (-1.0 * alpha / mu) * (Gr * (gv[a] * gv[b]));
+        acci[c] += (0.5 / mu) * (Fi[a] * gv[b] + Fi[b] * gv[a]) + (-1.0 * alpha / mu) * (Gi * (gv[a] * gv[b]));
+      }
+      nvar++;
     }
-    for (int a = 0; a < 3; a++) { Gr += g[a] * Fr[a]; Gi += g[a] * Fi[a]; }
     for (int c = 0; c < nc; c++) {
-      int a = ci[c], b = cj[c];
-      double sr = (0.5 / mu) * (Fr[a] * g[b] + Fr[b] * g[a]) + (-1.0 * alpha / mu) * (Gr * (g[a] * g[b]));
-      double si = (0.5 / mu) * (Fi[a] * g[b] + Fi[b] * g[a]) + (-1.0 * alpha / mu) * (Gi * (g[a] * g[b]));
-      W[(size_t)c * 2 * N + 2 * s] = sr;
-      W[(size_t)c * 2 * N + 2 * s + 1] = si;
+      W[(size_t)c * 2 * N + 2 * s] = nvar == 1 ? accr[c] : accr[c] / nvar;
+      W[(size_t)c * 2 * N + 2 * s + 1] = nvar == 1 ? acci[c] : acci[c] / nvar;
     }
   }
   double sum[6] = {0};

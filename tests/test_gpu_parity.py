@@ -1,0 +1,187 @@
+"""GPU parity: the CUDA engine (through its C ABI) against the reference's own
+fixtures and against the CPU oracle.
+
+Bars: (site, mode) event sequences identical; clocks and fields within 1e-10
+relative (the plain FP64 form); the mixed form's stress error against an FP64
+re-solve of its own eigenstrain <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from metallic_glasses_gb300 import api, configs
+from ref2d_cases import params_for
+
+pytestmark = pytest.mark.gpu
+
+FIELD_RTOL = 1e-10
+
+
+def rel_err(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+# ----------------------------------------------------------------- solver
+@pytest.mark.parametrize("model,shape", [
+    (api.MODEL_GLOBAL3D, (8, 8, 8)), (api.MODEL_GLOBAL3D, (12, 6, 16)), (api.MODEL_GLOBAL3D, (16, 24, 32)),
+    (api.MODEL_GLOBAL3D, (48, 48, 48)), (api.MODEL_REF2D, (1, 64, 64)), (api.MODEL_REF2D, (1, 48, 96)),
+    (api.MODEL_REF2D, (1, 512, 512)),
+])
+def test_fft_green_solve_matches_oracle(engine_lib, oracle_lib, model, shape):
+    """The hand-written R2C/C2R solve with the fused Green's pass against the
+    oracle's complex-FFT solve that keeps the real part, as the reference does."""
+    if model == api.MODEL_REF2D:
+        p = configs.ref2d(shape[1], shape[2])
+    else:
+        p = configs.shear64(seed=2)
+        p.n[0], p.n[1], p.n[2] = shape
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(p)
+    rng = np.random.default_rng(11)
+    nc = eng.nc
+    N = eng.N
+    for c in range(nc):
+        v = rng.standard_normal(N) * 0.02
+        eng.set_field(api.FIELD_EPS0, c, v)
+        ora.set_field(api.FIELD_EPS0, c, v)
+    eng.solve()
+    ora.solve()
+    for c in range(nc):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), ora.field(api.FIELD_SIGMA, c)) < 1e-11
+    eng.close()
+
+
+# ----------------------------------------------------- reference fixtures
+def _shear_prefix_ok(eng, g):
+    """SHEAR mode: after an avalanche the reference's mean-strain correction
+    (evolution.c:92-97, first component masked in every mode) zeroes the mean
+    shear stress, and its divergence test |Stress[2]| < 1e-17 (bmg.c:402)
+    then compares rounding noise of the field average. Where the engine's
+    noise falls below the bound first, it stops there with status 2; the
+    events up to that step must still be the reference's."""
+    sc = eng.scalars()
+    if sc["stopped"] != 2:
+        return False
+    ev = eng.events()
+    X = g["X"]
+    tr = ev[ev["kind"] != api.EV_ELASTIC]
+    k = len(tr)
+    assert k <= len(X)
+    assert np.array_equal(np.stack([tr["step"], tr["kind"], tr["site"], tr["mode"]], 1), X[:k])
+    last = int(sc["step"])
+    assert (X[:, 0] == last).any() and (X[X[:, 0] == last, 1] == 1).all(), "stop must follow an avalanche"
+    return True
+
+
+@pytest.mark.parametrize("case", ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5"])
+def test_ref2d_event_sequence_matches_reference(engine_lib, case):
+    g = golden(case)
+    p = params_for(g)
+    eng = api.Engine(p)
+    hdr = g["hdr"]
+    eng.run(max_steps=int(hdr[1]))
+    if "shear" in case and _shear_prefix_ok(eng, g):
+        return
+    ev = eng.events()
+    tr = ev[ev["kind"] != api.EV_ELASTIC]
+    X = g["X"]
+    assert len(tr) == len(X)
+    for col, k in ((0, "step"), (1, "kind"), (2, "site"), (3, "mode")):
+        assert np.array_equal(tr[k], X[:, col]), "first mismatch in %s at %s" % (
+            k, np.nonzero(tr[k] != X[:, col])[0][:3])
+    sc = eng.scalars()
+    assert [sc["step"], sc["kstep"], sc["astep"], sc["estep"]] == [int(v) for v in hdr[1:]]
+    S = g["S"]
+    last_time = {}
+    for e in ev:
+        last_time[int(e["step"])] = e["time"]
+    t = np.array([last_time[int(s)] for s in S[:, 0] if int(s) in last_time])
+    assert len(t) == len(S)
+    assert np.abs(t - S[:, 2]).max() <= FIELD_RTOL * np.abs(S[:, 2]).max()
+    for c in range(3):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), g["sigma"][c]) < FIELD_RTOL
+        assert rel_err(eng.field(api.FIELD_EPS0, c), g["eps0"][c]) < FIELD_RTOL
+    assert rel_err(eng.field(api.FIELD_TLAST), g["tlast"]) < FIELD_RTOL
+    assert rel_err(eng.field(api.FIELD_PERM_SOFT), g["perm_soft"]) < FIELD_RTOL
+    assert rel_err(eng.field(api.FIELD_TEMP_SOFT), g["temp_soft"]) < FIELD_RTOL
+    assert np.allclose(sc["eps_avg"][:3], g["sc"][1:4], rtol=FIELD_RTOL, atol=1e-14)
+    assert np.allclose(sc["stress"][:3], g["sc"][4:7], rtol=1e-9, atol=1e-12)
+    eng.close()
+
+
+def test_ref2d_deterministic(engine_lib):
+    p = configs.ref2d(32, 32)
+    a, b = api.Engine(p), api.Engine(p)
+    a.run(max_events=200)
+    b.run(max_events=200)
+    assert np.array_equal(a.events(), b.events())
+
+
+# ------------------------------------------------------------- 3D vs oracle
+@pytest.mark.parametrize("cfg,events", [("stress32", 400), ("shear16", 400)])
+def test_global3d_plain_matches_oracle(engine_lib, oracle_lib, cfg, events):
+    p = configs.stress32() if cfg == "stress32" else configs.shear64(seed=5, n=16)
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(p)
+    eng.run(max_events=events)
+    ora.run(max_events=events)
+    a, b = eng.events(), ora.events()
+    assert len(a) == len(b)
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(a[k], b[k])
+    assert np.abs(a["time"] - b["time"]).max() <= FIELD_RTOL * np.abs(b["time"]).max()
+    for c in range(6):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), ora.field(api.FIELD_SIGMA, c)) < FIELD_RTOL
+        assert rel_err(eng.field(api.FIELD_EPS0, c), ora.field(api.FIELD_EPS0, c)) < FIELD_RTOL
+    assert rel_err(eng.field(api.FIELD_DF), ora.field(api.FIELD_DF)) < 1e-15
+
+
+def test_correlated_barrier_field_matches_oracle(engine_lib, oracle_lib):
+    p = configs.grf256(n=16)
+    p.precision = api.PREC_FP64
+    p.solver = api.SOLVER_FFT
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(p)
+    a, b = eng.field(api.FIELD_DF), ora.field(api.FIELD_DF)
+    assert np.abs(a - b).max() < 1e-10
+    assert abs(a.mean() - 1.2) < 0.05
+
+
+# ------------------------------------------------------------- mixed form
+def test_mixed_rates_select_like_plain_for_a_while(engine_lib):
+    """FP32 rates against the FP64 plain form on the same seed: the same
+    events until a near-tie of the FP32 rates flips one."""
+    pm = configs.mixed128(n=16)
+    pp = configs.plain128(n=16)
+    m, q = api.Engine(pm), api.Engine(pp)
+    m.run(max_events=20)
+    q.run(max_events=20)
+    a, b = m.events(), q.events()
+    same = 0
+    for x, y in zip(a, b):
+        if x["site"] != y["site"] or x["mode"] != y["mode"]:
+            break
+        same += 1
+    assert same >= 5
+    assert np.allclose(a["time"][:same], b["time"][:same], rtol=1e-5)
+
+
+def test_mixed_stress_error_within_bound(engine_lib):
+    p = configs.mixed128(n=32, resolve_period=500)
+    m = api.Engine(p)
+    m.run(max_events=1000)
+    sc = m.scalars()
+    assert sc["kstep"] == 1000
+    assert 0 < sc["stress_err_max"] < 1e-5
+    assert sc["stress_err_rms"] < 1e-6
+
+
+def test_mixed_first_resolve_error_small(engine_lib):
+    """One event after the start: the incremental update of one voxel's
+    response against the FP64 re-solve of the same state."""
+    p = configs.mixed128(n=24, resolve_period=1)
+    m = api.Engine(p)
+    m.run(max_events=3)
+    sc = m.scalars()
+    assert sc["kstep"] == 3
+    assert 0 < sc["stress_err_max"] < 1e-6
