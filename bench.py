@@ -1,0 +1,286 @@
+"""Benchmark: KMC events/s of the STZ step at 128^3, mixed precision vs FP64 plain.
+
+One step = one batch of `--events-per-step` thermal KMC events of the mixed
+form on the 128^3 shear-loaded configuration (synthetic barriers and modes
+drawn from seed 0, all state resident in HBM). L2 is flushed between steps
+(a 256 MB write). The line also carries the FP64 plain form measured on the
+same grid, the stress error of the mixed form against its FP64 re-solves, the
+roofline of the per-event kernel, the end-to-end figure through the C ABI
+with host-side event and scalar reads, and the CPU oracle timed on the host.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank runs its own replica (seed = rank): scaling is weak
+and no data-path collective exists.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = 128
+METRIC = "KMC events/s, 128^3 grid: mixed vs FP64 plain, 1 GB300, stress err ≤1e-5"
+UNIT = "events/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_record(kernel, grid):
+    """ncu DRAM bytes per launch recorded under profiles/ (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        return d.get("%s@%d" % (kernel, grid))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            t = [x.strip() for x in line.split(",")]
+            if len(t) < 9:
+                continue
+            try:
+                sm.append(float(t[1]))
+                smax = float(t[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, t[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.remove(self.path)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(seconds=15.0, grid=GRID):
+    """The CPU oracle (FP64, the reference's full re-solve per event) on all
+    host threads, on a bounded sample of the same workload."""
+    from metallic_glasses_gb300 import configs
+    from oracle import pyoracle
+    p = configs.plain128(n=grid)
+    m = pyoracle.Model(p)
+    m.run(max_events=1)  # first event outside the sample (warm caches)
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < seconds and n < 2000:
+        m.run(max_events=1)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": pyoracle.threads(), "kind": "port",
+            "sample": "%d thermal events of the %d^3 FP64 shear configuration (seed 0) after setup, %.1f s" %
+                      (n, grid, dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    cb = cpu_baseline(seconds=max(5.0, 30.0 / max(args.steps + args.warmup, 1)))
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "dtype": "f64",
+            "data": "synthetic", "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": "FP64 STZ KMC at %d^3, shear strain rate, seed 0" % GRID,
+                       "implementation": "CPU restatement of the reference method (oracle/stz_oracle.c, "
+                                         "OpenMP); the reference's own FFTW2+MPI+GSL build is not buildable "
+                                         "on this box"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine")
+    ap.add_argument("--events-per-step", type=int, default=1000)
+    ap.add_argument("--grid", type=int, default=GRID)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if dist:
+            dist.destroy_process_group()
+        return rc
+
+    from metallic_glasses_gb300 import api, configs
+    n = args.grid
+    B = args.events_per_step
+    p = configs.mixed128(seed=rank, n=n, resolve_period=1000)
+    p.device = local
+    eng = api.Engine(p)
+    # warm-up
+    for _ in range(args.warmup):
+        eng.flush_l2()
+        eng.run(max_events=B)
+    eng.sync()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    barrier()
+    eng.sync()
+    l0 = eng.launches()
+    k0 = eng.scalars()["kstep"]
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        eng.timer_start()
+        for _ in range(args.steps):
+            eng.flush_l2()
+            eng.run(max_events=B)
+        ms = eng.timer_stop()
+        t_wall = time.perf_counter() - t_wall
+    eng.sync()
+    barrier()
+    sc = eng.scalars()
+    events = sc["kstep"] - k0
+    launches = eng.launches() - l0
+    ms_max = ms
+    ev_total = events
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        e = torch.tensor([events], dtype=torch.float64)
+        dist.all_reduce(e)
+        ev_total = int(e.item())
+    value = ev_total / (ms_max / 1e3)
+
+    # e2e through the C ABI: run + copy this step's events and scalars to host
+    h0, d0 = eng.transfer_bytes()
+    first = sc["n_events_logged"]
+    t_e2e = time.perf_counter()
+    e2e_events = 0
+    for _ in range(args.steps):
+        eng.run(max_events=B)
+        s2 = eng.scalars()
+        evs = eng.events(first=first)
+        first += len(evs)
+        e2e_events += int((evs["kind"] == api.EV_THERMAL).sum())
+    t_e2e = time.perf_counter() - t_e2e
+    h1, d1 = eng.transfer_bytes()
+    e2e = {"value": e2e_events / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int((h1 - h0) / args.steps), "d2h_bytes_per_step": int((d1 - d0) / args.steps),
+           "note": "stz_run of %d events + event log and scalars read back to host memory, wall clock" % B}
+
+    # per-event kernel, timed launch by launch with CUDA events
+    k_ms, k_n = eng.kernel_time(steps=200)
+    N = n ** 3
+    alg_bytes = 44 * N  # read+write 5 FP32 deviatoric stress components, read the FP32 barrier
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (k_ms / 1e3) / 1e9 if k_ms > 0 else None
+    tr = traffic_record("k_mixed", n)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": tr,
+            "kernel": "k_mixed (incremental update + rates + FP64 partial sums + last-block select/commit)",
+            "alg_bytes_per_launch": alg_bytes, "launch_ms": k_ms, "launches_timed": k_n,
+            "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
+    scf = eng.scalars()
+    stress_err = {"rel_l2_worst": scf["stress_err_rms_worst"], "rel_max_worst": scf["stress_err_max_worst"],
+                  "resolves": scf["n_resolves"],
+                  "definition": "deviatoric stress of the FP32 incremental field vs an FP64 re-solve of the "
+                                "same eigenstrain every 1000 events; relative L2 norm and max norm"}
+    eng.close()
+
+    # FP64 plain form on the same grid (full FFT re-solve per event)
+    pp = configs.plain128(seed=rank, n=n)
+    pp.device = local
+    pe = api.Engine(pp)
+    pe.run(max_events=3)
+    pe.sync()
+    plain_events = 30
+    pe.flush_l2()
+    pe.timer_start()
+    pe.run(max_events=plain_events)
+    pms = pe.timer_stop()
+    plain = plain_events / (pms / 1e3)
+    pe.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 field/rates, f64 sums/clock/eigenstrain",
+            "data": "synthetic (seeded barriers, modes)",
+            "config": {"workload": "STZ KMC, mixed form, %d^3 grid, 20 modes, shear strain rate 5e-5/s, "
+                                   "T=455 K, %d thermal events per step, FP64 re-solve every 1000 events" % (n, B),
+                       "grid": n, "sites": N, "events_per_step": B, "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "flushed between steps (256 MB write)"},
+            "plain_fp64_events_per_s": plain, "mixed_over_plain": value / world / plain,
+            "stress_err": stress_err,
+            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+            "wall_s": t_wall}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

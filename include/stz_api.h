@@ -170,10 +170,15 @@ typedef struct stz_scalars {
   int64_t n_events_logged;
   int32_t stopped;           /* 1: end strain reached, 2: unstable (bmg.c:382-409) */
   int32_t status;            /* sticky device error status */
-  double  stress_err_max;    /* mixed: max relative stress error at the last FP64 re-solve */
-  double  stress_err_rms;
-  int64_t near_ties;         /* selections whose cumulative margin was below 1e-12 */
-  int64_t reserved[6];
+  double  stress_err_max;    /* mixed, last FP64 re-solve: max |ds| / max |s| of the
+                                deviatoric stress s against the FP64 re-solve */
+  double  stress_err_rms;    /* mixed, last FP64 re-solve: |ds|_2 / |s|_2 */
+  int64_t near_ties;         /* selections whose cumulative margin was below 1e-12 R */
+  int64_t log_dropped;       /* events not logged (ring full) */
+  int64_t n_resolves;        /* periodic FP64 re-solves done */
+  double  stress_err_rms_worst;  /* worst of stress_err_rms over all re-solves */
+  double  stress_err_max_worst;
+  int64_t reserved[2];
 } stz_scalars;
 
 /* field selectors for stz_get_field / stz_set_field */
@@ -186,7 +191,11 @@ enum {
   STZ_FIELD_PERM_SOFT = 5,
   STZ_FIELD_TEMP_SOFT = 6,
   STZ_FIELD_PREV_DEPS = 7,   /* eigenstrain increment of the site's last transformation */
-  STZ_FIELD_Q = 8            /* activation energy Q[mode] for the current stress */
+  STZ_FIELD_Q = 8,           /* activation energy Q[mode] for the current stress */
+  STZ_FIELD_SDEV = 9         /* mixed form: the stored FP32 deviatoric stress,
+                                coordinate comp 0..4 of the orthonormal basis
+                                (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2 yz,
+                                sqrt2 xz, sqrt2 xy (pending update applied first) */
 };
 
 typedef struct stz_ctx stz_ctx;
@@ -229,10 +238,14 @@ int stz_timer_start(stz_ctx* ctx);
 int stz_timer_stop(stz_ctx* ctx, float* ms);       /* CUDA events on the ctx stream */
 int stz_flush_l2(stz_ctx* ctx);                      /* writes a buffer larger than L2 */
 int64_t stz_kernel_launches(stz_ctx* ctx);           /* kernels launched by this ctx so far */
+/* Bytes copied host->device and device->host by this ctx so far. */
+int stz_transfer_bytes(stz_ctx* ctx, int64_t* h2d, int64_t* d2h);
 /* sizeof the ABI structs, for bindings: 0 stz_params, 1 stz_event, 2 stz_scalars */
 int64_t stz_sizeof(int32_t which);
-/* Average device time (ms) of the dominant per-event kernel over the last
- * stz_run call, measured with CUDA events around its launches. */
+/* Average device time (ms) of the mixed form's per-event kernel, launched one
+ * by one between CUDA events for *launches steps (which = 0), or of its
+ * update-only variant (which = 1, the stress-field streaming floor).
+ * *launches receives the number of launches timed. */
 int stz_kernel_time(stz_ctx* ctx, int32_t which, double* ms_avg, int64_t* launches);
 
 #ifdef __cplusplus

@@ -24,7 +24,7 @@ DF_TRUNC_NORMAL, DF_CORRELATED = 0, 1
 XX, YY, ZZ, YZ, XZ, XY = range(6)
 EV_THERMAL, EV_ATHERMAL, EV_ELASTIC = 0, 1, 2
 FIELD_SIGMA, FIELD_EPS0, FIELD_DF, FIELD_DEPS, FIELD_TLAST, FIELD_PERM_SOFT, FIELD_TEMP_SOFT, \
-    FIELD_PREV_DEPS, FIELD_Q = range(9)
+    FIELD_PREV_DEPS, FIELD_Q, FIELD_SDEV = range(10)
 
 
 class Params(C.Structure):
@@ -57,7 +57,9 @@ class Scalars(C.Structure):
                 ("eps0_avg", C.c_double * 6), ("step", C.c_int64), ("kstep", C.c_int64), ("astep", C.c_int64),
                 ("estep", C.c_int64), ("n_print", C.c_int64), ("n_events_logged", C.c_int64),
                 ("stopped", C.c_int32), ("status", C.c_int32), ("stress_err_max", C.c_double),
-                ("stress_err_rms", C.c_double), ("near_ties", C.c_int64), ("reserved", C.c_int64 * 6)]
+                ("stress_err_rms", C.c_double), ("near_ties", C.c_int64), ("log_dropped", C.c_int64),
+                ("n_resolves", C.c_int64), ("stress_err_rms_worst", C.c_double),
+                ("stress_err_max_worst", C.c_double), ("reserved", C.c_int64 * 2)]
 
 
 EVENT_DTYPE = np.dtype([("step", np.int64), ("site", np.int64), ("kind", np.int32), ("mode", np.int32),
@@ -96,6 +98,7 @@ def load_library(path=None):
     lib.stz_kernel_launches.argtypes = [vp]
     lib.stz_kernel_launches.restype = C.c_int64
     lib.stz_kernel_time.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.stz_transfer_bytes.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.stz_sizeof.argtypes = [C.c_int32]
     lib.stz_sizeof.restype = C.c_int64
     for name, s in ((0, Params), (1, Event), (2, Scalars)):
@@ -134,7 +137,8 @@ def scalars_dict(s):
             "step": s.step, "kstep": s.kstep, "astep": s.astep, "estep": s.estep, "n_print": s.n_print,
             "n_events_logged": s.n_events_logged, "stopped": s.stopped, "status": s.status,
             "stress_err_max": s.stress_err_max, "stress_err_rms": s.stress_err_rms, "near_ties": s.near_ties,
-            "log_dropped": s.reserved[0]}
+            "log_dropped": s.log_dropped, "n_resolves": s.n_resolves,
+            "stress_err_rms_worst": s.stress_err_rms_worst, "stress_err_max_worst": s.stress_err_max_worst}
 
 
 class Engine:
@@ -211,8 +215,13 @@ class Engine:
     def launches(self):
         return self.lib.stz_kernel_launches(self.h)
 
-    def kernel_time(self, steps=64):
+    def transfer_bytes(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(self.lib.stz_transfer_bytes(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def kernel_time(self, steps=64, which=0):
         ms = C.c_double()
         n = C.c_int64(steps)
-        _check(self.lib.stz_kernel_time(self.h, 0, C.byref(ms), C.byref(n)))
+        _check(self.lib.stz_kernel_time(self.h, which, C.byref(ms), C.byref(n)))
         return ms.value, n.value

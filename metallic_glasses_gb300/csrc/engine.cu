@@ -308,6 +308,7 @@ void enqueue_plain_step(stz_ctx* c) {
 int sync_ctl(stz_ctx* c) {
   CK(cudaMemcpyAsync(&c->host_ctl, c->f.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  c->d2h_bytes += sizeof(Ctl);
   return STZ_OK;
 }
 
@@ -324,10 +325,12 @@ int drain_log(stz_ctx* c) {
       const long long n = std::min(to - i, cap - slot);
       CK(cudaMemcpyAsync(c->host_log.data() + old + (i - from), c->f.log + slot, sizeof(stz_event) * n,
                          cudaMemcpyDeviceToHost, c->stream));
+      c->d2h_bytes += (int64_t)sizeof(stz_event) * n;
       i += n;
     }
     h.log_base = to;
     CK(cudaMemcpyAsync(&c->f.ctl->log_base, &h.log_base, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    c->h2d_bytes += sizeof(long long);
     CK(cudaStreamSynchronize(c->stream));
   }
   return STZ_OK;
@@ -341,6 +344,7 @@ int set_targets(stz_ctx* c, long long max_kstep, long long max_step) {
   h.halt_reason = h.stopped ? kHaltStop : kHaltNone;
   CK(cudaMemcpyAsync(&c->f.ctl->max_kstep, &h.max_kstep, sizeof(long long) * 2, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(&c->f.ctl->halt, &h.halt, sizeof(int) * 2, cudaMemcpyHostToDevice, c->stream));
+  c->h2d_bytes += sizeof(long long) * 2 + sizeof(int) * 2;
   return STZ_OK;
 }
 
@@ -351,8 +355,12 @@ int capture_plain_graph(stz_ctx* c, int steps) {
   const int64_t l0 = c->launches;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   for (int i = 0; i < steps; i++) {
-    if (c->kp.nc == 6 && c->f.sdev) launch_mixed(c->kp, c->f, 0, c->stream);
-    else enqueue_plain_step(c);
+    if (c->kp.nc == 6 && c->f.sdev) {
+      launch_mixed(c->kp, c->f, 0, c->stream);
+      c->launches += 1;
+    } else {
+      enqueue_plain_step(c);
+    }
   }
   CK(cudaStreamEndCapture(c->stream, &g));
   c->graph_launches = c->launches - l0;
@@ -391,16 +399,19 @@ int mixed_service(stz_ctx* c, int* done) {
       // periodic FP64 re-solve: bring the FP32 field up to date, re-solve it
       // in FP64 with the same mean strain and offsets, record the difference
       launch_mixed(kp, f, 1, c->stream);
-      double zero[3] = {0, 0, 0};
+      double zero[4] = {0, 0, 0, 0};
       CK(cudaMemcpyAsync(c->err_dev, zero, sizeof(zero), cudaMemcpyHostToDevice, c->stream));
       solve_dev(c, f.ctl->eps_avg_applied, f.ctl->u, c->err_dev);
       launch_mixed_after_resolve(kp, f, 1, c->stream);
-      double e[3];
+      double e[4];
       CK(cudaMemcpyAsync(e, c->err_dev, sizeof(e), cudaMemcpyDeviceToHost, c->stream));
       CK(cudaStreamSynchronize(c->stream));
-      const double ref2 = std::max(e[2], 1e-300) / (double)kp.N;
-      c->err_max = std::sqrt(e[0] / ref2);
-      c->err_rms = std::sqrt((e[1] / (double)kp.N) / ref2);
+      // relative L2 norm and max norm of the deviatoric stress difference
+      c->err_rms = std::sqrt(e[1] / std::max(e[2], 1e-300));
+      c->err_max = std::sqrt(e[0] / std::max(e[3], 1e-300));
+      c->err_rms_worst = std::max(c->err_rms_worst, c->err_rms);
+      c->err_max_worst = std::max(c->err_max_worst, c->err_max);
+      c->n_resolves++;
       h.next_resolve += kp.resolve_period;
       CK(cudaMemcpyAsync(&f.ctl->next_resolve, &h.next_resolve, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
       c->launches += 2;
@@ -475,9 +486,10 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   kp.nh = kp.n2 / 2 + 1;
   kp.N = (long long)kp.n0 * kp.n1 * kp.n2;
   kp.Nk = (long long)kp.n0 * kp.n1 * kp.nh;
-  const int spt = mixed ? 8 : 4;
+  const int spt = mixed ? kSptMixed : kSptFp64;
   kp.bsites = kRateThreads * spt;
   kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
+  kp.ngroups = (kp.nblk + kGroup - 1) / kGroup;
   kp.loading = p.loading;
   kp.softening = p.softening;
   kp.sf_scheme = p.sf_scheme;
@@ -497,6 +509,10 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   for (int i = 0; i < 6; i++) kp.applied[i] = p.applied_stress[i];
   kp.kt0 = kp.n0 / 2 + 1; kp.kt1 = kp.n1 / 2 + 1; kp.kt2 = kp.n2 / 2 + 1;
   kp.log_cap = 1 << 20;
+  kp.fast_inv = mixed ? 1 : 0;
+  kp.inv_2mu = 1.0 / (2.0 * p.mu);
+  kp.inv_lam_coef = p.lambda / (2.0 * p.mu * ((ref2d ? 2.0 : 3.0) * p.lambda + 2.0 * p.mu));
+  kp.invN = 1.0 / (double)((long long)p.n[0] * p.n[1] * p.n[2]);
   kp.resolve_period = mixed ? p.resolve_period : 0;
 
   const long long N = kp.N;
@@ -510,8 +526,10 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   if ((st = dalloc(&f.prev_deps, (size_t)nc * N))) return fail(st);
   if ((st = dalloc(&f.amark, (size_t)N))) return fail(st);
   if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
+  if ((st = dalloc(&f.gsum, (size_t)STZ_MODES * kp.ngroups))) return fail(st);
+  if ((st = dalloc(&f.gticket, (size_t)kp.ngroups))) return fail(st);
   if ((st = dalloc(&f.log, (size_t)kp.log_cap))) return fail(st);
-  if ((st = dalloc(&c->err_dev, 3))) return fail(st);
+  if ((st = dalloc(&c->err_dev, 4))) return fail(st);
   {
     double2* sp = nullptr;
     if ((st = dalloc(&sp, (size_t)nc * kp.Nk))) return fail(st);
@@ -596,7 +614,8 @@ extern "C" void stz_destroy(stz_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
-                  f.tlast, f.amark, f.part, f.spec, f.ktab, f.log, f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf};
+                  f.tlast, f.amark, f.part, f.gsum, f.gticket, f.spec, f.ktab, f.log, f.ctl, f.scratch, f.msum,
+                  c->err_dev, c->l2buf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fft) {
@@ -700,7 +719,10 @@ extern "C" int stz_get_scalars(stz_ctx* c, stz_scalars* o) {
   o->stress_err_max = c->err_max;
   o->stress_err_rms = c->err_rms;
   o->near_ties = h.near_ties;
-  o->reserved[0] = h.nlog_dropped;
+  o->log_dropped = h.nlog_dropped;
+  o->n_resolves = c->n_resolves;
+  o->stress_err_rms_worst = c->err_rms_worst;
+  o->stress_err_max_worst = c->err_max_worst;
   return STZ_OK;
 }
 
@@ -763,6 +785,18 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
     cudaMemcpyAsync(host, tmp, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
     cudaStreamSynchronize(c->stream);
     cudaFree(tmp);
+    return STZ_OK;
+  }
+  if (which == STZ_FIELD_SDEV) {
+    if (!c->f.sdev || comp < 0 || comp >= 5) return STZ_ERR_INVALID;
+    launch_mixed(c->kp, c->f, 1, c->stream);  // apply the pending update
+    float* tmp = nullptr;
+    if (dalloc(&tmp, (size_t)N)) return STZ_ERR_NOMEM;
+    std::vector<float> hf((size_t)N);
+    CK(cudaMemcpyAsync(hf.data(), c->f.sdev + (size_t)comp * N, sizeof(float) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(tmp);
+    for (long long s = 0; s < N; s++) host[s] = hf[(size_t)s];
     return STZ_OK;
   }
   if (which == STZ_FIELD_SIGMA && c->f.sdev) {
@@ -865,12 +899,18 @@ extern "C" int stz_flush_l2(stz_ctx* c) {
 
 extern "C" int64_t stz_kernel_launches(stz_ctx* c) { return c ? c->launches : 0; }
 
+extern "C" int stz_transfer_bytes(stz_ctx* c, int64_t* h2d, int64_t* d2h) {
+  if (!c) return STZ_ERR_INVALID;
+  if (h2d) *h2d = c->h2d_bytes;
+  if (d2h) *d2h = c->d2h_bytes;
+  return STZ_OK;
+}
+
 // Average device time of the per-step kernel: runs `steps` steps launching
 // that kernel directly between CUDA events (no graph), on the context's
 // stream. which = 0: the per-step rate/update kernel.
 extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_t* launches) {
   if (!c || !ms_avg) return STZ_ERR_INVALID;
-  (void)which;
   cudaSetDevice(c->p.device);
   int st = sync_ctl(c);
   if (st) return st;
@@ -879,6 +919,24 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
   if (!mixed) {
     *ms_avg = 0;
     return STZ_ERR_UNSUPPORTED;
+  }
+  if (which == 1) {
+    // update-only variant: streams the stress field (read + write) and the
+    // response table; state is unchanged after its first launch
+    double tot = 0;
+    for (int i = 0; i < steps; i++) {
+      CK(cudaEventRecord(c->kev0, c->stream));
+      launch_mixed(c->kp, c->f, 1, c->stream);
+      CK(cudaEventRecord(c->kev1, c->stream));
+      CK(cudaEventSynchronize(c->kev1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->kev0, c->kev1));
+      tot += ms;
+    }
+    c->launches += steps;
+    *ms_avg = tot / steps;
+    if (launches) *launches = steps;
+    return STZ_OK;
   }
   // run on a private copy of the targets: the kernel halts on its own rules
   Ctl& h = c->host_ctl;

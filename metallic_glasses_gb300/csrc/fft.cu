@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
     __syncthreads();
   }
   if (OUT == kOutDev32) {
-    double mx = 0, ss = 0, sr = 0;
+    double mx = 0, ss = 0, sr = 0, mr = 0;
     for (int idx = threadIdx.x; idx < L * n2; idx += blockDim.x) {
       const int l = idx / n2, i = idx - l * n2;
       const long long r = r0 + l;
@@ -476,29 +476,33 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
         sdev[k * N + s] = (float)d[k];
       }
       mx = fmax(mx, e2);
+      mr = fmax(mr, n2s);
       ss += e2;
       sr += n2s;
     }
     // block reduction
     for (int off = 16; off > 0; off >>= 1) {
       mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, off));
       ss += __shfl_xor_sync(0xffffffffu, ss, off);
       sr += __shfl_xor_sync(0xffffffffu, sr, off);
     }
-    __shared__ double red[3][8];
+    __shared__ double red[4][8];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { red[0][w] = mx; red[1][w] = ss; red[2][w] = sr; }
+    if (lane == 0) { red[0][w] = mx; red[1][w] = ss; red[2][w] = sr; red[3][w] = mr; }
     __syncthreads();
     if (threadIdx.x == 0) {
       for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
         mx = fmax(mx, red[0][k]);
         ss += red[1][k];
         sr += red[2][k];
+        mr = fmax(mr, red[3][k]);
       }
       // non-negative doubles order like their bit patterns
       atomicMax(reinterpret_cast<unsigned long long*>(&err[0]), (unsigned long long)__double_as_longlong(mx));
       atomicAdd(&err[1], ss);
       atomicAdd(&err[2], sr);
+      atomicMax(reinterpret_cast<unsigned long long*>(&err[3]), (unsigned long long)__double_as_longlong(mr));
     }
   }
 }

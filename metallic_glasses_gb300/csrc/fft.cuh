@@ -51,7 +51,8 @@ struct SolveArgs {
   double* sig64;         // kOutSig64
   float* sig32;          // kOutSig32
   float* sdev;           // kOutDev32 (read for the error, then overwritten)
-  double* err;           // kOutDev32: err[0] = max |d s|^2, err[1] = sum |d s|^2, err[2] = sum |s|^2
+  double* err;           // kOutDev32: err[0] = max |d s|^2, err[1] = sum |d s|^2,
+                         // err[2] = sum |s|^2, err[3] = max |s|^2 (s: the FP64 result)
   double* msum;          // kOutSig64, optional: per-(component, block) sums of the
                          // solved field, [nc][fft_c2r_blocks] (for the mean stress)
   int fp32;              // run the transform in FP32 (eps converted on load)

@@ -40,9 +40,19 @@ __device__ void apply_C(const KParams& kp, const double* e, double* s) {
   for (int c = 0; c < kp.nc; c++) s[c] = (c < nd ? kp.lambda * tr : 0.0) + 2.0 * kp.mu * e[c];
 }
 
-// isotropicinv (elastic.c:522-531) in DIM dimensions
+// isotropicinv (elastic.c:522-531) in DIM dimensions. The mixed form uses
+// precomputed coefficients (no divisions on the one-thread commit path); the
+// FP64 forms keep the reference's operation order.
 __device__ void iso_inv(const KParams& kp, const double* s, double* e) {
   const double lam = kp.lambda, mu = kp.mu;
+  if (kp.fast_inv) {
+    const int nd = ndiag(kp.nc);
+    double tr = 0;
+    for (int c = 0; c < nd; c++) tr += s[c];
+    const double t = -kp.inv_lam_coef * tr;
+    for (int c = 0; c < kp.nc; c++) e[c] = (c < nd ? t : 0.0) + s[c] * kp.inv_2mu;
+    return;
+  }
   if (kp.nc == 3) {
     double tra = -lam / 2 / mu / (2 * lam + 2 * mu) * (s[0] + s[1]);
     e[0] = tra + s[0] / 2 / mu;
@@ -67,7 +77,7 @@ __device__ void field_mean_stress(const KParams& kp, const Fields& f, double* ou
 
 __device__ void solved_mean_stress(const KParams& kp, const Ctl* ctl, const double* ebar, double* out) {
   double e[6];
-  for (int c = 0; c < kp.nc; c++) e[c] = ebar[c] - ctl->eps0_sum[c] / (double)kp.N;
+  for (int c = 0; c < kp.nc; c++) e[c] = ebar[c] - ctl->eps0_sum[c] * kp.invN;
   apply_C(kp, e, out);
 }
 
@@ -225,12 +235,14 @@ __device__ void log_event(const KParams& kp, const Fields& f, Ctl* ctl, int kind
 }
 
 // ------------------------------------------------------- per-site physics
-// Unpack a site index into grid coordinates.
+// Unpack a site index into grid coordinates (32-bit: grids hold < 2^31 sites).
 __device__ __forceinline__ void site_coords(const KParams& kp, long long s, int* i0, int* i1, int* i2) {
-  *i2 = (int)(s % kp.n2);
-  const long long r = s / kp.n2;
-  *i1 = (int)(r % kp.n1);
-  *i0 = (int)(r / kp.n1);
+  const unsigned u = (unsigned)s;
+  const unsigned r = u / (unsigned)kp.n2;
+  *i2 = (int)(u - r * (unsigned)kp.n2);
+  const unsigned q = r / (unsigned)kp.n1;
+  *i1 = (int)(r - q * (unsigned)kp.n1);
+  *i0 = (int)q;
 }
 
 // Direction modifier of the softening schemes (init.c:590-642)
@@ -346,6 +358,26 @@ __device__ void block_mode_sums(const double* acc, double* part, int nblk, int b
   }
 }
 
+// Mixed form: the per-thread FP32 sums are reduced within each warp in FP32
+// (32 values), then across the warps of the block in FP64.
+__device__ void block_mode_sums_f32(const float* acc, double* part, int nblk, int b) {
+  __shared__ double red[TH / 32][STZ_MODES];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int m = 0; m < STZ_MODES; m++) {
+    float v = acc[m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+    if (lane == 0) red[w][m] = (double)v;
+  }
+  __syncthreads();
+  if (threadIdx.x < STZ_MODES) {
+    double s = 0;
+    for (int k = 0; k < TH / 32; k++) s += red[k][threadIdx.x];
+    part[(long long)threadIdx.x * nblk + b] = s;
+  }
+}
+
 __device__ unsigned block_sum_u(unsigned v) {
   __shared__ unsigned red[TH / 32];
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
@@ -369,6 +401,65 @@ __device__ bool last_block(Ctl* ctl, int nblk) {
   __syncthreads();
   if (is_last) __threadfence();
   return is_last;
+}
+
+// ------------------------------------------------------------------ RNG
+// Whole block: when the generator is exhausted, refill its 624 words with the
+// MT19937 recurrence in four phases, each of which only reads words that no
+// thread of the same phase writes (old words k, k+1 and either old k+397 or
+// new k-227). Bit-identical to the sequential twist.
+__device__ void block_twist_if_needed(MT* g) {
+  __shared__ int need;
+  __syncthreads();
+  if (threadIdx.x == 0) need = g->mti >= 624;
+  __syncthreads();
+  if (!need) return;
+  const uint32_t UP = 0x80000000u, LO = 0x7fffffffu, A = 0x9908b0dfu;
+  uint32_t* mt = g->mt;
+  const int k0[4] = {0, 227, 454, 623}, k1[4] = {227, 454, 623, 624};
+  for (int ph = 0; ph < 4; ph++) {
+    const int k = k0[ph] + (int)threadIdx.x;
+    uint32_t v = 0;
+    const bool mine = k < k1[ph];
+    if (mine) {
+      const uint32_t y = (mt[k] & UP) | (mt[k == 623 ? 0 : k + 1] & LO);
+      const uint32_t src = k < 227 ? mt[k + 397] : mt[k - 227];
+      v = src ^ (y >> 1) ^ ((y & 1u) ? A : 0u);
+    }
+    __syncthreads();
+    if (mine) mt[k] = v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) g->mti = 0;
+  __syncthreads();
+}
+
+// Second level of the rate sums: the last block of each group of kGroup
+// blocks reduces the group's per-(mode, block) sums to per-(mode, group) sums
+// with a fixed warp butterfly (every lane ends with the same bits). Returns
+// true in that block.
+__device__ bool group_reduce(const KParams& kp, const Fields& f, int b) {
+  __shared__ bool is_last;
+  const int g = b / kGroup;
+  const int g0 = g * kGroup, g1 = min(g0 + kGroup, kp.nblk);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(&f.gticket[g], 1u);
+    is_last = (t == (unsigned)(g1 - g0 - 1));
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int m = w; m < STZ_MODES; m += TH / 32) {
+    double v = (g0 + lane < g1) ? f.part[(long long)m * kp.nblk + g0 + lane] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+    if (lane == 0) f.gsum[(long long)m * kp.ngroups + g] = v;
+  }
+  if (threadIdx.x == 0) f.gticket[g] = 0;
+  return true;
 }
 
 // ----------------------------------------------------------- selection
@@ -411,78 +502,117 @@ __device__ double site_Q(const KParams& kp, const Fields& f, const double* u, do
 
 // Hierarchical search of the (mode, site) whose cumulative rate, in the
 // reference's mode-major order m*N + s, first reaches T. Level 1: the
-// per-(mode, block) sums, split into one contiguous chunk per thread and
-// scanned; level 2: the rates of the chosen mode in the chosen block,
-// recomputed and scanned. Called by the whole last block.
+// per-(mode, block) sums, one contiguous chunk per thread, whose inclusive
+// scan the caller left in sh_inc; level 2: the rates of the chosen mode in the
+// chosen block, recomputed into registers and scanned. Whole block.
 template <int MODEL>
 __device__ void search_event(const KParams& kp, const Fields& f, const double* u, double totime, double T,
-                             long long* site_out, int* mode_out, double* margin_out) {
-  __shared__ double sh_inc[TH];
+                             const double* sh_inc, long long* site_out, int* mode_out, double* margin_out) {
+  __shared__ double sh_inc2[TH];
   __shared__ long long sh_p;
   __shared__ double sh_cb;
   __shared__ long long sh_site;
   __shared__ double sh_margin;
   const int t = threadIdx.x;
-  const long long P = (long long)STZ_MODES * kp.nblk;
+  const long long P = (long long)STZ_MODES * kp.ngroups;
   const long long ch = (P + TH - 1) / TH;
   const long long p0 = t * ch, p1 = min(p0 + ch, P);
-  double S = 0;
-  for (long long p = p0; p < p1; p++) S += f.part[p];
   if (t == 0) { sh_p = -1; sh_site = -1; sh_margin = 0; }
-  const double I = block_incl_scan(S, sh_inc);
+  __syncthreads();
+  const double I = sh_inc[t];
   const double E = t > 0 ? sh_inc[t - 1] : 0.0;
   const double Ttot = sh_inc[TH - 1];
   double Tq = T;
   if (Tq > Ttot) Tq = Ttot;
   if (E < Tq && Tq <= I) {
-    double run = E, before = E;
+    double run = E;
     long long hit = -1, lastpos = -1;
-    double lastbefore = E;
-    for (long long p = p0; p < p1; p++) {
-      const double v = f.part[p];
-      before = run;
+    double hb = E, lastbefore = E;
+    for (long long q = p0; q < p1; q++) {
+      const double v = f.gsum[q];
+      const double before = run;
       run += v;
-      if (v > 0) { lastpos = p; lastbefore = before; }
-      if (run >= Tq && v > 0) { hit = p; break; }
+      const bool pos = v > 0;
+      if (pos) { lastpos = q; lastbefore = before; }
+      if (hit < 0 && pos && run >= Tq) { hit = q; hb = before; }
     }
-    if (hit < 0) { hit = lastpos; before = lastbefore; }
+    if (hit < 0) { hit = lastpos; hb = lastbefore; }
     sh_p = hit;
-    sh_cb = before;
+    sh_cb = hb;
   }
   __syncthreads();
-  const long long p = sh_p;
-  if (p < 0) {
+  const long long pg = sh_p;
+  if (pg < 0) {
     if (t == 0) { *site_out = -1; *mode_out = -1; }
     return;
   }
-  const int m = (int)(p / kp.nblk);
-  const int b = (int)(p - (long long)m * kp.nblk);
+  const int m = (int)(pg / kp.ngroups);
+  const int g = (int)(pg - (long long)m * kp.ngroups);
+  // level 1.5: the blocks of group g for mode m, one warp
+  if (t < 32) {
+    const int g0 = g * kGroup, g1 = min(g0 + kGroup, kp.nblk);
+    const double v = (g0 + t < g1) ? f.part[(long long)m * kp.nblk + g0 + t] : 0.0;
+    double x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double y = __shfl_up_sync(FULL, x, off);
+      if (t >= off) x += y;
+    }
+    const double before = __shfl_up_sync(FULL, x, 1);
+    const double ex = t > 0 ? before : 0.0;
+    const double Tg = Tq - sh_cb;
+    const unsigned ok = __ballot_sync(FULL, v > 0 && x >= Tg);
+    const unsigned posb = __ballot_sync(FULL, v > 0);
+    int lane = ok ? __ffs(ok) - 1 : (posb ? 31 - __clz(posb) : -1);
+    if (lane >= 0) {
+      const double exl = __shfl_sync(FULL, ex, lane);
+      if (t == 0) {
+        sh_p = g0 + lane;
+        sh_cb = sh_cb + exl;
+      }
+    } else if (t == 0) {
+      sh_p = -1;
+    }
+  }
+  __syncthreads();
+  if (sh_p < 0) {
+    if (t == 0) { *site_out = -1; *mode_out = -1; }
+    return;
+  }
+  const int b = (int)sh_p;
   double T2 = Tq - sh_cb;
   const long long s0 = (long long)b * kp.bsites;
   const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
   const long long per = (s1 - s0 + TH - 1) / TH;
-  const long long a0 = s0 + t * per, a1 = min(a0 + per, s1);
+  const long long a0 = s0 + t * per;
+  constexpr int kMaxPer = MODEL == 2 ? kSptMixed : kSptFp64;  // sites per thread
+  double rr[kMaxPer];
   double loc = 0;
-  for (long long s = a0; s < a1; s++) loc += site_rate<MODEL>(kp, f, u, totime, s, m);
-  __syncthreads();
-  const double I2 = block_incl_scan(loc, sh_inc);
-  const double E2 = t > 0 ? sh_inc[t - 1] : 0.0;
-  const double tot2 = sh_inc[TH - 1];
+#pragma unroll
+  for (int k = 0; k < kMaxPer; k++) {
+    const long long s = a0 + k;
+    rr[k] = (k < per && s < s1) ? site_rate<MODEL>(kp, f, u, totime, s, m) : 0.0;
+    loc += rr[k];
+  }
+  const double I2 = block_incl_scan(loc, sh_inc2);
+  const double E2 = t > 0 ? sh_inc2[t - 1] : 0.0;
+  const double tot2 = sh_inc2[TH - 1];
   if (T2 > tot2) T2 = tot2;
   if (!(T2 > 0)) T2 = DBL_MIN;
   if (E2 < T2 && T2 <= I2) {
     double run = E2;
-    long long hit = -1, lastpos = -1;
+    int hit = -1, lastk = -1;
     double hb = E2, ha = E2, lb = E2, la = E2;
-    for (long long s = a0; s < a1; s++) {
-      const double r = site_rate<MODEL>(kp, f, u, totime, s, m);
+#pragma unroll
+    for (int k = 0; k < kMaxPer; k++) {
       const double before = run;
-      run += r;
-      if (r > 0) { lastpos = s; lb = before; la = run; }
-      if (run >= T2 && r > 0) { hit = s; hb = before; ha = run; break; }
+      run += rr[k];
+      const bool pos = rr[k] > 0;
+      if (pos) { lastk = k; lb = before; la = run; }
+      if (hit < 0 && pos && run >= T2) { hit = k; hb = before; ha = run; }
     }
-    if (hit < 0) { hit = lastpos; hb = lb; ha = la; }
-    sh_site = hit;
+    if (hit < 0) { hit = lastk; hb = lb; ha = la; }
+    sh_site = hit < 0 ? -1 : a0 + hit;
     sh_margin = fmin(T2 - hb, ha - T2);
   }
   __syncthreads();
@@ -496,7 +626,7 @@ __device__ void search_event(const KParams& kp, const Fields& f, const double* u
 // ------------------------------------------------------------ commits
 // VoxelShearTransform (elastic.c:361-520) for the FP64 models; thread 0 only.
 template <int MODEL>
-__device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, long long s) {
+__device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, long long s, MT* rng) {
   const long long N = kp.N;
   double d[6];
   if (MODEL == 0) {
@@ -520,18 +650,54 @@ __device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, 
     // re-draw the site's modes, glass branch (elastic.c:508-512)
     for (int i = 0; i < STZ_MODES; i++) {
       double* dd = f.deps + (long long)i * 3 * N;
-      const double a = 0.5 * kp.gamma0 * mt_gaussian(&ctl->rng, 1.0);
+      const double a = 0.5 * kp.gamma0 * mt_gaussian(rng, 1.0);
       dd[s] = a;
       dd[N + s] = -a;
-      dd[2 * N + s] = 0.5 * kp.gamma0 * mt_gaussian(&ctl->rng, 1.0);
+      dd[2 * N + s] = 0.5 * kp.gamma0 * mt_gaussian(rng, 1.0);
     }
   }
 }
 
-// Last block of the FP64 rate kernel: decide the step kind and commit.
+// Block copy of the control block between global and shared memory: the
+// last block does its sequential bookkeeping on the shared copy (the global
+// one would cost an L2 round trip per field access).
+__device__ __forceinline__ void ctl_copy(Ctl* dst, const Ctl* src) {
+  const uint32_t* a = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  for (int i = threadIdx.x; i < (int)(sizeof(Ctl) / 4); i += blockDim.x) d[i] = a[i];
+}
+
+// Incremental "solve" of a thermal event in the mixed form, then the
+// loading of evolution.c:262-317 (thread 0, on the shared control block).
+__device__ void mixed_commit(const KParams& kp, const Fields& f, Ctl* c, long long s, int m) {
+  const long long N = kp.N;
+  for (int k = 0; k < 6; k++) {
+    f.prev_deps[k * N + s] = kp.modes[m][k];
+    f.eps0[k * N + s] += kp.modes[m][k];
+    c->eps0_sum[k] += kp.modes[m][k];
+  }
+  double dA[6], CdA[6];
+  for (int k = 0; k < 6; k++) dA[k] = c->eps_avg[k] - c->eps_avg_applied[k];
+  apply_C(kp, dA, CdA);
+  for (int k = 0; k < 6; k++) {
+    c->U[k] = CdA[k] - c->u[k];
+    c->eps_avg_applied[k] = c->eps_avg[k];
+    c->u[k] = 0;
+  }
+  solved_mean_stress(kp, c, c->eps_avg_applied, c->stress);
+  load_after_event(kp, c, c->t_kmc);
+  for (int k = 0; k < 6; k++) c->U[k] += c->u[k];
+  c->has_pend = 1;
+  c->pend_site = s;
+  c->pend_mode = m;
+}
+
+// Last block of a rate kernel: total rate, step kind, dice, event search and
+// commit. MODEL 0 REF2D FP64, 1 GLOBAL3D FP64, 2 mixed form.
 template <int MODEL>
-__device__ void finish_fp64(const KParams& kp, const Fields& f) {
-  Ctl* ctl = f.ctl;
+__device__ void finish_step(const KParams& kp, const Fields& f) {
+  __shared__ Ctl sc;
+  __shared__ double sh_inc[TH];
   __shared__ int sh_kind;
   __shared__ double sh_T, sh_R;
   __shared__ double sh_u[6];
@@ -539,85 +705,124 @@ __device__ void finish_fp64(const KParams& kp, const Fields& f) {
   __shared__ long long sh_site;
   __shared__ int sh_mode;
   __shared__ double sh_margin;
-  __shared__ double sh_inc2[TH];
-  // total rate: per-thread contiguous chunks of the partials, fixed order
-  const long long P = (long long)STZ_MODES * kp.nblk;
+  Ctl* const g = f.ctl;
+  ctl_copy(&sc, g);
+  // per-thread contiguous chunks of the per-(mode, group) sums, fixed order
+  const long long P = (long long)STZ_MODES * kp.ngroups;
   const long long ch = (P + TH - 1) / TH;
   const long long p0 = threadIdx.x * ch, p1 = min(p0 + ch, P);
   double S = 0;
-  for (long long p = p0; p < p1; p++) S += f.part[p];
-  block_incl_scan(S, sh_inc2);
+  for (long long p = p0; p < p1; p++) S += f.gsum[p];
+  block_incl_scan(S, sh_inc);  // also orders the copy above
+  if (MODEL != 0) block_twist_if_needed(&sc.rng);
+  Ctl* c = &sc;
   if (threadIdx.x == 0) {
-    ctl->ticket = 0;
-    ctl->step++;
-    const double R = sh_inc2[TH - 1];
-    sh_R = R;
-    for (int c = 0; c < 6; c++) sh_u[c] = ctl->u[c];
-    sh_tot = ctl->totime;
-    if (ctl->neg_count > 0) {
-      sh_kind = kAthermal;
+    c->ticket = 0;
+    c->step++;
+    if (MODEL == 2) {
+      c->has_pend = 0;
+      for (int k = 0; k < 6; k++) c->U[k] = 0;
+    }
+    const double Rraw = sh_inc[TH - 1];
+    const double R = MODEL == 2 ? Rraw * kp.rate_scale : Rraw;
+    sh_R = Rraw;
+    for (int k = 0; k < 6; k++) sh_u[k] = c->u[k];
+    sh_tot = c->totime;
+    c->total_rate = R;
+    int kind;
+    if (c->neg_count > 0) {
+      kind = kAthermal;
+      if (MODEL == 2) { c->halt = 1; c->halt_reason = kHaltAthermal; }
     } else if (!(R > 0) || !isfinite(R)) {
-      sh_kind = kNone;
-      ctl->status = STZ_ERR_NAN;
-      ctl->halt = 1;
-      ctl->halt_reason = kHaltError;
+      kind = kNone;
+      c->status = STZ_ERR_NAN;
+      c->halt = 1;
+      c->halt_reason = kHaltError;
     } else {
       const double t_kmc = 1 / R;
       if (t_kmc < kp.dt) {
-        sh_kind = kThermal;
-        ctl->kstep++;
-        const double dice = mt_uniform(&ctl->rng);
-        sh_T = dice * R;
-        ctl->t_kmc = t_kmc;
+        kind = kThermal;
+        c->kstep++;
+        const double dice = mt_uniform(&c->rng);
+        sh_T = dice * Rraw;
+        c->t_kmc = t_kmc;
         if (!(dice > 0)) {
-          sh_kind = kNone;
-          ctl->status = STZ_ERR_NO_EVENT;
-          ctl->halt = 1;
-          ctl->halt_reason = kHaltError;
+          kind = kNone;
+          c->status = STZ_ERR_NO_EVENT;
+          c->halt = 1;
+          c->halt_reason = kHaltError;
         }
       } else {
-        sh_kind = kElastic;
+        kind = kElastic;
       }
     }
-    ctl->neg_count = 0;
-    ctl->step_kind = sh_kind;
-    ctl->total_rate = R;
+    c->neg_count = 0;
+    c->step_kind = kind;
+    sh_kind = kind;
   }
   __syncthreads();
   const int kind = sh_kind;
   if (kind == kThermal) {
-    search_event<MODEL>(kp, f, sh_u, sh_tot, sh_T, &sh_site, &sh_mode, &sh_margin);
+    search_event<MODEL>(kp, f, sh_u, sh_tot, sh_T, sh_inc, &sh_site, &sh_mode, &sh_margin);
     __syncthreads();
-    if (threadIdx.x == 0) {
+  }
+  if (threadIdx.x == 0) {
+    const double Rtrue = MODEL == 2 ? sh_R * kp.rate_scale : sh_R;
+    if (kind == kThermal) {
       const long long s = sh_site;
       const int m = sh_mode;
       if (s < 0) {
-        ctl->status = STZ_ERR_NO_EVENT;
-        ctl->halt = 1;
-        ctl->halt_reason = kHaltError;
-        ctl->step_kind = kNone;
+        c->status = STZ_ERR_NO_EVENT;
+        c->halt = 1;
+        c->halt_reason = kHaltError;
+        c->step_kind = kNone;
       } else {
-        if (sh_margin < 1e-12 * sh_R) ctl->near_ties++;
+        if (sh_margin < 1e-12 * sh_R) c->near_ties++;
         const double q = site_Q<MODEL>(kp, f, sh_u, sh_tot, s, m);
-        transform<MODEL>(kp, f, ctl, m, s);
-        ctl->sel_site = s;
-        ctl->sel_mode = m;
-        ctl->sel_q = q;
-        ctl->solve_req = 1;
-        log_event(kp, f, ctl, STZ_EV_THERMAL, s, m, ctl->totime + ctl->t_kmc, ctl->t_kmc, q, sh_R);
+        c->sel_site = s;
+        c->sel_mode = m;
+        c->sel_q = q;
+        if (MODEL == 2) {
+          mixed_commit(kp, f, c, s, m);
+          c->totime += c->t_kmc;
+          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime, c->t_kmc, q, Rtrue);
+          if (kp.resolve_period > 0 && c->kstep >= c->next_resolve) {
+            c->halt = 1;
+            c->halt_reason = kHaltResolve;
+          }
+        } else {
+          transform<MODEL>(kp, f, c, m, s, &c->rng);
+          c->solve_req = 1;
+          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue);
+        }
+      }
+    } else if (kind == kElastic) {
+      c->estep++;
+      c->totime += kp.dt;
+      double u0[6];
+      for (int k = 0; k < 6; k++) u0[k] = c->u[k];
+      elastic_step(kp, c);
+      if (MODEL == 2)
+        for (int k = 0; k < 6; k++) c->U[k] = c->u[k] - u0[k];
+      else
+        c->solve_req = 0;
+      log_event(kp, f, c, STZ_EV_ELASTIC, -1, -1, c->totime, kp.dt, 0.0, Rtrue);
+    } else if (kind == kAthermal && MODEL != 2) {
+      c->solve_req = 0;  // the athermal commit requests the solve
+    }
+    if (MODEL == 2 && (kind == kThermal || kind == kElastic) && c->step_kind != kNone) {
+      if (print_check(kp, c)) {
+        c->print_done = 1;
+        c->halt = 1;
+        c->halt_reason = kHaltPrint;
+      } else {
+        if (!c->halt) stop_check(kp, c);
+        c->step_kind = kNone;
       }
     }
-  } else if (kind == kElastic) {
-    if (threadIdx.x == 0) {
-      ctl->estep++;
-      ctl->totime += kp.dt;
-      elastic_step(kp, ctl);
-      ctl->solve_req = 0;
-      log_event(kp, f, ctl, STZ_EV_ELASTIC, -1, -1, ctl->totime, kp.dt, 0.0, sh_R);
-    }
-  } else if (kind == kAthermal) {
-    if (threadIdx.x == 0) ctl->solve_req = 0;  // set by the athermal commit
   }
+  __syncthreads();
+  ctl_copy(g, &sc);
 }
 
 // ------------------------------------------------------------ FP64 rates
@@ -659,8 +864,9 @@ __global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
   block_mode_sums(acc, f.part, kp.nblk, b);
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
-  if (!last_block(ctl, kp.nblk)) return;
-  finish_fp64<MODEL>(kp, f);
+  if (!group_reduce(kp, f, b)) return;
+  if (!last_block(ctl, kp.ngroups)) return;
+  finish_step<MODEL>(kp, f);
 }
 
 // ------------------------------------------------------------ athermal
@@ -692,6 +898,13 @@ __global__ void k_ath_commit(KParams kp, Fields f, int mixed) {
   Ctl* ctl = f.ctl;
   if (ctl->step_kind != kAthermal) return;
   __shared__ unsigned ballot[TH / 32];
+  __shared__ MT srng;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&ctl->rng);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&srng);
+    for (int i = threadIdx.x; i < (int)(sizeof(MT) / 4); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
   double u[6];
   for (int c = 0; c < 6; c++) u[c] = ctl->u[c];
   const double totime = ctl->totime;
@@ -714,13 +927,18 @@ __global__ void k_ath_commit(KParams kp, Fields f, int mixed) {
           if (kp.model == STZ_MODEL_REF2D) q = site_Q<0>(kp, f, u, totime, site, mm);
           else if (mixed) q = site_Q<2>(kp, f, u, totime, site, mm);
           else q = site_Q<1>(kp, f, u, totime, site, mm);
-          if (kp.model == STZ_MODEL_REF2D) transform<0>(kp, f, ctl, mm, site);
-          else transform<1>(kp, f, ctl, mm, site);
+          if (kp.model == STZ_MODEL_REF2D) transform<0>(kp, f, ctl, mm, site, &srng);
+          else transform<1>(kp, f, ctl, mm, site, &srng);
           log_event(kp, f, ctl, STZ_EV_ATHERMAL, site, mm, ctl->totime, 0.0, q, 0.0);
         }
       }
     }
     __syncthreads();
+  }
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&srng);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ctl->rng);
+    for (int i = threadIdx.x; i < (int)(sizeof(MT) / 4); i += blockDim.x) dst[i] = src[i];
   }
   if (threadIdx.x == 0) ctl->solve_req = 1;
 }
@@ -792,7 +1010,7 @@ __device__ __forceinline__ int fold(int d, int n, int* flip) {
 }
 
 template <int UPDATE_ONLY>
-__global__ void __launch_bounds__(TH) k_mixed(KParams kp, Fields f) {
+__global__ void __launch_bounds__(TH, 2) k_mixed(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->halt && !UPDATE_ONLY) return;
   const int b = blockIdx.x;
@@ -881,142 +1099,12 @@ __global__ void __launch_bounds__(TH) k_mixed(KParams kp, Fields f) {
     }
     return;
   }
-  double accd[STZ_MODES];
-#pragma unroll
-  for (int m = 0; m < STZ_MODES; m++) accd[m] = (double)acc[m];
-  block_mode_sums(accd, f.part, kp.nblk, b);
+  block_mode_sums_f32(acc, f.part, kp.nblk, b);
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
-  if (!last_block(ctl, kp.nblk)) return;
-
-  // ---- last block: select and commit
-  __shared__ int sh_kind;
-  __shared__ double sh_T, sh_R;
-  __shared__ double sh_inc2[TH];
-  __shared__ long long sh_site;
-  __shared__ int sh_mode;
-  __shared__ double sh_margin;
-  const long long P = (long long)STZ_MODES * kp.nblk;
-  const long long ch = (P + TH - 1) / TH;
-  const long long q0 = threadIdx.x * ch, q1 = min(q0 + ch, P);
-  double S = 0;
-  for (long long p = q0; p < q1; p++) S += f.part[p];
-  block_incl_scan(S, sh_inc2);
-  if (threadIdx.x == 0) {
-    ctl->ticket = 0;
-    ctl->has_pend = 0;
-    for (int c = 0; c < 6; c++) ctl->U[c] = 0;
-    ctl->step++;
-    const double Rraw = sh_inc2[TH - 1];
-    const double R = Rraw * kp.rate_scale;
-    sh_R = Rraw;
-    ctl->total_rate = R;
-    if (ctl->neg_count > 0) {
-      sh_kind = kAthermal;
-      ctl->halt = 1;
-      ctl->halt_reason = kHaltAthermal;
-    } else if (!(R > 0) || !isfinite(R)) {
-      sh_kind = kNone;
-      ctl->status = STZ_ERR_NAN;
-      ctl->halt = 1;
-      ctl->halt_reason = kHaltError;
-    } else {
-      const double t_kmc = 1 / R;
-      if (t_kmc < kp.dt) {
-        sh_kind = kThermal;
-        ctl->kstep++;
-        const double dice = mt_uniform(&ctl->rng);
-        sh_T = dice * Rraw;
-        ctl->t_kmc = t_kmc;
-        if (!(dice > 0)) {
-          sh_kind = kNone;
-          ctl->status = STZ_ERR_NO_EVENT;
-          ctl->halt = 1;
-          ctl->halt_reason = kHaltError;
-        }
-      } else {
-        sh_kind = kElastic;
-      }
-    }
-    ctl->neg_count = 0;
-    ctl->step_kind = sh_kind;
-  }
-  __syncthreads();
-  const int kind = sh_kind;
-  if (kind == kThermal) {
-    double zero[6] = {0, 0, 0, 0, 0, 0};
-    search_event<2>(kp, f, zero, 0.0, sh_T, &sh_site, &sh_mode, &sh_margin);
-    __syncthreads();
-  }
-  if (threadIdx.x != 0) return;
-  if (kind == kThermal) {
-    const long long s = sh_site;
-    const int m = sh_mode;
-    if (s < 0) {
-      ctl->status = STZ_ERR_NO_EVENT;
-      ctl->halt = 1;
-      ctl->halt_reason = kHaltError;
-      ctl->step_kind = kNone;
-      return;
-    }
-    if (sh_margin < 1e-12 * sh_R) ctl->near_ties++;
-    double zero[6] = {0, 0, 0, 0, 0, 0};
-    const double q = site_Q<2>(kp, f, zero, 0.0, s, m);
-    // eigenstrain (FP64) and the incremental "solve"
-    for (int c = 0; c < 6; c++) {
-      f.prev_deps[c * N + s] = kp.modes[m][c];
-      f.eps0[c * N + s] += kp.modes[m][c];
-      ctl->eps0_sum[c] += kp.modes[m][c];
-    }
-    double ebar_sol[6], dA[6], CdA[6];
-    for (int c = 0; c < 6; c++) {
-      ebar_sol[c] = ctl->eps_avg[c];
-      dA[c] = ebar_sol[c] - ctl->eps_avg_applied[c];
-    }
-    apply_C(kp, dA, CdA);
-    double unew[6];
-    for (int c = 0; c < 6; c++) {
-      ctl->U[c] = CdA[c] - ctl->u[c];
-      ctl->eps_avg_applied[c] = ebar_sol[c];
-      ctl->u[c] = 0;
-    }
-    solved_mean_stress(kp, ctl, ebar_sol, ctl->stress);
-    load_after_event(kp, ctl, ctl->t_kmc);
-    for (int c = 0; c < 6; c++) {
-      unew[c] = ctl->u[c];
-      ctl->U[c] += unew[c];
-    }
-    ctl->has_pend = 1;
-    ctl->pend_site = s;
-    ctl->pend_mode = m;
-    ctl->sel_site = s;
-    ctl->sel_mode = m;
-    ctl->sel_q = q;
-    ctl->totime += ctl->t_kmc;
-    log_event(kp, f, ctl, STZ_EV_THERMAL, s, m, ctl->totime, ctl->t_kmc, q, sh_R * kp.rate_scale);
-    if (kp.resolve_period > 0 && ctl->kstep >= ctl->next_resolve) {
-      ctl->halt = 1;
-      ctl->halt_reason = kHaltResolve;
-    }
-  } else if (kind == kElastic) {
-    ctl->estep++;
-    ctl->totime += kp.dt;
-    double u0[6];
-    for (int c = 0; c < 6; c++) u0[c] = ctl->u[c];
-    elastic_step(kp, ctl);
-    for (int c = 0; c < 6; c++) ctl->U[c] = ctl->u[c] - u0[c];
-    log_event(kp, f, ctl, STZ_EV_ELASTIC, -1, -1, ctl->totime, kp.dt, 0.0, sh_R * kp.rate_scale);
-  } else {
-    return;
-  }
-  if (print_check(kp, ctl)) {
-    ctl->print_done = 1;
-    ctl->halt = 1;
-    ctl->halt_reason = kHaltPrint;
-    return;
-  }
-  if (!ctl->halt) stop_check(kp, ctl);
-  ctl->step_kind = kNone;
+  if (!group_reduce(kp, f, b)) return;
+  if (!last_block(ctl, kp.ngroups)) return;
+  finish_step<2>(kp, f);
 }
 
 // After a full FP64 re-solve into sdev (mixed form).

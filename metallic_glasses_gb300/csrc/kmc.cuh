@@ -7,6 +7,9 @@
 namespace stz {
 
 constexpr int kRateThreads = 256;
+constexpr int kSptMixed = 8;   // sites per thread of the mixed-form kernel
+constexpr int kSptFp64 = 4;    // sites per thread of the FP64 rate kernels
+constexpr int kGroup = 32;     // blocks per group in the two-level rate sums
 
 // Rate kernel of the FP64 forms (ActEnergy + KMC rates + selection/commit in
 // the last block). model: STZ_MODEL_REF2D or STZ_MODEL_GLOBAL3D.

@@ -91,6 +91,8 @@ struct Fields {
   double* tlast = nullptr;
   signed char* amark = nullptr; // [N] athermal marks (mode+1, 0 = none)
   double* part = nullptr;    // [MODES][nblk] per (mode, block) rate sums
+  double* gsum = nullptr;    // [MODES][ngroups] per (mode, group of blocks) sums
+  unsigned* gticket = nullptr;  // [ngroups] last-block counters of the groups
   void* spec = nullptr;      // [nc][Nk] complex FP64 spectrum
   float* ktab = nullptr;     // mixed: [15][kt0][kt1][kt2] response table
   stz_event* log = nullptr;  // event ring
@@ -104,6 +106,9 @@ struct KParams {
   int model, nc, n0, n1, n2, nh;
   long long N, Nk;
   int nblk, bsites;          // rate kernel: blocks and sites per block
+  int ngroups;               // groups of kGroup blocks
+  int fast_inv;              // mixed form: precomputed compliance coefficients
+  double inv_2mu, inv_lam_coef, invN;
   int loading, softening, sf_scheme, no_subtract_error, shear_quirk;
   double lambda, mu, young, poisson;
   double kT, vt, V0, dt, gamma0;
@@ -146,6 +151,9 @@ struct stz_ctx {
   int64_t graph_launches = 0;        // kernels per graph launch
   void* l2buf = nullptr;
   size_t l2flush_bytes = 0;
-  double* err_dev = nullptr;         // [3] error sums of the periodic re-solve
-  double err_max = 0, err_rms = 0;
+  double* err_dev = nullptr;         // [4] error sums of the periodic re-solve
+  double err_max = 0, err_rms = 0;   // last periodic re-solve
+  double err_max_worst = 0, err_rms_worst = 0;
+  int64_t n_resolves = 0;
+  int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies made by stepping and getters
 };
