@@ -99,6 +99,7 @@ def load_library(path=None):
     lib.stz_kernel_launches.restype = C.c_int64
     lib.stz_kernel_time.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.stz_transfer_bytes.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.stz_phase_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.stz_sizeof.argtypes = [C.c_int32]
     lib.stz_sizeof.restype = C.c_int64
     for name, s in ((0, Params), (1, Event), (2, Scalars)):
@@ -214,6 +215,11 @@ class Engine:
 
     def launches(self):
         return self.lib.stz_kernel_launches(self.h)
+
+    def phase_times(self):
+        a, b, n = C.c_double(), C.c_double(), C.c_int64()
+        _check(self.lib.stz_phase_times(self.h, C.byref(a), C.byref(b), C.byref(n)))
+        return a.value, b.value, n.value
 
     def transfer_bytes(self):
         a, b = C.c_int64(), C.c_int64()

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -206,6 +207,7 @@ void mixed_constants(stz_ctx* c) {
   const double l2e = 1.4426950408889634074;
   kp.q_ref = (float)c->p.q0_mean;
   kp.a_scale = (float)(l2e / kp.kT);
+  kp.inv_a_scale = 1.0 / (double)kp.a_scale;
   kp.rate_scale = kp.vt * std::exp(-(double)kp.q_ref / kp.kT);
   for (int m = 0; m < STZ_MODES; m++) {
     double d[5];
@@ -357,7 +359,7 @@ int capture_plain_graph(stz_ctx* c, int steps) {
   for (int i = 0; i < steps; i++) {
     if (c->kp.nc == 6 && c->f.sdev) {
       launch_mixed(c->kp, c->f, 0, c->stream);
-      c->launches += 1;
+      c->launches += 2;
     } else {
       enqueue_plain_step(c);
     }
@@ -490,6 +492,8 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   kp.bsites = kRateThreads * spt;
   kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
   kp.ngroups = (kp.nblk + kGroup - 1) / kGroup;
+  kp.adv_q2 = kRateThreads / kp.n2;
+  kp.adv_r2 = kRateThreads % kp.n2;
   kp.loading = p.loading;
   kp.softening = p.softening;
   kp.sf_scheme = p.sf_scheme;
@@ -653,7 +657,7 @@ extern "C" int stz_run(stz_ctx* c, int64_t max_steps, int64_t max_events) {
       c->launches += c->graph_launches;
     } else {
       for (int i = 0; i < batch; i++) {
-        if (mixed) { launch_mixed(c->kp, c->f, 0, c->stream); c->launches += 1; }
+        if (mixed) { launch_mixed(c->kp, c->f, 0, c->stream); c->launches += 2; }
         else enqueue_plain_step(c);
       }
     }
@@ -899,6 +903,21 @@ extern "C" int stz_flush_l2(stz_ctx* c) {
 
 extern "C" int64_t stz_kernel_launches(stz_ctx* c) { return c ? c->launches : 0; }
 
+extern "C" int stz_phase_times(stz_ctx* c, double* main_us, double* tail_us, int64_t* n) {
+  if (!c) return STZ_ERR_INVALID;
+  int st = sync_ctl(c);
+  if (st) return st;
+  const Ctl& h = c->host_ctl;
+  const double k = h.prof_n ? 1e-3 / (double)h.prof_n : 0.0;
+  if (main_us) *main_us = (double)h.prof_main_ns * k;
+  if (tail_us) *tail_us = (double)h.prof_tail_ns * k;
+  if (n) *n = (int64_t)h.prof_n;
+  if (std::getenv("STZ_PHASE_DETAIL"))
+    std::fprintf(stderr, "stz tail parts (us): sums %.2f decide %.2f search %.2f commit %.2f\n",
+                 h.prof_part_ns[0] * k, h.prof_part_ns[1] * k, h.prof_part_ns[2] * k, h.prof_part_ns[3] * k);
+  return STZ_OK;
+}
+
 extern "C" int stz_transfer_bytes(stz_ctx* c, int64_t* h2d, int64_t* d2h) {
   if (!c) return STZ_ERR_INVALID;
   if (h2d) *h2d = c->h2d_bytes;
@@ -926,14 +945,16 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
     double tot = 0;
     for (int i = 0; i < steps; i++) {
       CK(cudaEventRecord(c->kev0, c->stream));
-      launch_mixed(c->kp, c->f, 1, c->stream);
+      launch_mixed_main(c->kp, c->f, 1, c->stream);
       CK(cudaEventRecord(c->kev1, c->stream));
+      launch_mixed_tail(c->kp, c->f, 1, c->stream);
       CK(cudaEventSynchronize(c->kev1));
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, c->kev0, c->kev1));
       tot += ms;
     }
-    c->launches += steps;
+    CK(cudaStreamSynchronize(c->stream));
+    c->launches += 2 * steps;
     *ms_avg = tot / steps;
     if (launches) *launches = steps;
     return STZ_OK;
@@ -944,10 +965,14 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
   double tot = 0;
   int n = 0;
   for (int i = 0; i < steps; i++) {
+    // which 0: the grid-wide update/rate kernel alone; 2: the whole event
+    // (that kernel plus the selection/commit kernel)
     CK(cudaEventRecord(c->kev0, c->stream));
-    launch_mixed(c->kp, c->f, 0, c->stream);
-    CK(cudaEventRecord(c->kev1, c->stream));
-    CK(cudaEventSynchronize(c->kev1));
+    launch_mixed_main(c->kp, c->f, 0, c->stream);
+    if (which == 0) CK(cudaEventRecord(c->kev1, c->stream));
+    launch_mixed_tail(c->kp, c->f, 0, c->stream);
+    if (which != 0) CK(cudaEventRecord(c->kev1, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, c->kev0, c->kev1));
     if ((st = sync_ctl(c))) return st;
@@ -962,7 +987,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
     tot += ms;
     n++;
   }
-  c->launches += steps;
+  c->launches += 2 * steps;
   *ms_avg = n ? tot / n : 0;
   if (launches) *launches = n;
   return STZ_OK;

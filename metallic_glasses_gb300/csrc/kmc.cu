@@ -21,6 +21,7 @@
 // the rates in FP32, sums them in FP64 and selects/commits in its last block.
 #include <cfloat>
 #include <cmath>
+#include <cstddef>
 
 #include "kmc.cuh"
 
@@ -299,6 +300,20 @@ __device__ __forceinline__ void g3_load(const KParams& kp, const Fields& f, cons
   for (int c = 0; c < 6; c++) sg[c] = f.sig[c * kp.N + s] + u[c];
 }
 
+// 2^x with the hardware approximation (PTX ex2.approx.ftz.f32: one MUFU
+// operation, relative error below 2^-22; results under 2^-126 flush to 0).
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Mixed: scaled log2-rate x = log2(e)/kT (q_ref - Q); identical code in the
 // main pass and in the rescan so both see the same bits.
 __device__ __forceinline__ float mx_x(const KParams& kp, const float* sv, float a, int m) {
@@ -478,7 +493,7 @@ __device__ __forceinline__ double site_rate(const KParams& kp, const Fields& f, 
     float sv[5];
     for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
     const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
-    return (double)exp2f(mx_x(kp, sv, a, m));
+    return (double)ex2_approx(mx_x(kp, sv, a, m));
   }
 }
 
@@ -705,6 +720,7 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
   __shared__ long long sh_site;
   __shared__ int sh_mode;
   __shared__ double sh_margin;
+  const unsigned long long t_tail = gtimer();
   Ctl* const g = f.ctl;
   ctl_copy(&sc, g);
   // per-thread contiguous chunks of the per-(mode, group) sums, fixed order
@@ -714,6 +730,7 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
   double S = 0;
   for (long long p = p0; p < p1; p++) S += f.gsum[p];
   block_incl_scan(S, sh_inc);  // also orders the copy above
+  const unsigned long long t_sums = gtimer();
   if (MODEL != 0) block_twist_if_needed(&sc.rng);
   Ctl* c = &sc;
   if (threadIdx.x == 0) {
@@ -761,11 +778,13 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
     sh_kind = kind;
   }
   __syncthreads();
+  const unsigned long long t_dec = gtimer();
   const int kind = sh_kind;
   if (kind == kThermal) {
     search_event<MODEL>(kp, f, sh_u, sh_tot, sh_T, sh_inc, &sh_site, &sh_mode, &sh_margin);
     __syncthreads();
   }
+  const unsigned long long t_search = gtimer();
   if (threadIdx.x == 0) {
     const double Rtrue = MODEL == 2 ? sh_R * kp.rate_scale : sh_R;
     if (kind == kThermal) {
@@ -809,6 +828,16 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
       log_event(kp, f, c, STZ_EV_ELASTIC, -1, -1, c->totime, kp.dt, 0.0, Rtrue);
     } else if (kind == kAthermal && MODEL != 2) {
       c->solve_req = 0;  // the athermal commit requests the solve
+    }
+    if (MODEL == 2) {
+      const unsigned long long t_end = gtimer();
+      c->prof_main_ns += t_tail - c->prof_t0;
+      c->prof_tail_ns += t_end - t_tail;
+      c->prof_part_ns[0] += t_sums - t_tail;
+      c->prof_part_ns[1] += t_dec - t_sums;
+      c->prof_part_ns[2] += t_search - t_dec;
+      c->prof_part_ns[3] += t_end - t_search;
+      c->prof_n++;
     }
     if (MODEL == 2 && (kind == kThermal || kind == kElastic) && c->step_kind != kNone) {
       if (print_check(kp, c)) {
@@ -1010,9 +1039,10 @@ __device__ __forceinline__ int fold(int d, int n, int* flip) {
 }
 
 template <int UPDATE_ONLY>
-__global__ void __launch_bounds__(TH, 2) k_mixed(KParams kp, Fields f) {
+__global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->halt && !UPDATE_ONLY) return;
+  if (!UPDATE_ONLY && blockIdx.x == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
   const int b = blockIdx.x;
   const long long N = kp.N;
   const long long s0 = (long long)b * kp.bsites;
@@ -1038,25 +1068,29 @@ __global__ void __launch_bounds__(TH, 2) k_mixed(KParams kp, Fields f) {
     ud[4] = q2 * U6[5];
     for (int k = 0; k < 5; k++) Ud[k] = (float)ud[k];
   }
-  const long long ts = (long long)kp.kt1 * kp.kt2, tstride = (long long)kp.kt0 * ts;
+  const int ts = kp.kt1 * kp.kt2, tstride = kp.kt0 * ts;
   float acc[STZ_MODES];
 #pragma unroll
   for (int m = 0; m < STZ_MODES; m++) acc[m] = 0.f;
   const float thr_neg = kp.q_ref * kp.a_scale;
-  unsigned neg = 0;
-  for (long long s = s0 + threadIdx.x; s < s1; s += TH) {
+  float xmax = -INFINITY;
+  // site coordinates, advanced incrementally by TH sites per iteration
+  const int N32 = (int)N;
+  int s = (int)s0 + (int)threadIdx.x;
+  int i0, i1, i2;
+  site_coords(kp, s, &i0, &i1, &i2);
+  for (; s < (int)s1; s += TH) {
     float sv[5];
 #pragma unroll
-    for (int k = 0; k < 5; k++) sv[k] = f.sdev[k * N + s];
+    for (int k = 0; k < 5; k++) sv[k] = f.sdev[k * N32 + s];
     if (hp) {
-      int i0, i1, i2, fx, fy, fz;
-      site_coords(kp, s, &i0, &i1, &i2);
+      int fx, fy, fz;
       const int d0 = fold(i0 - p0, kp.n0, &fz);
       const int d1 = fold(i1 - p1, kp.n1, &fy);
       const int d2 = fold(i2 - p2, kp.n2, &fx);
       const float sx = fx ? -1.f : 1.f, sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
       const float sg[5] = {1.f, 1.f, sy * sz, sx * sz, sx * sy};
-      const float* tp = f.ktab + (long long)d0 * ts + (long long)d1 * kp.kt2 + d2;
+      const float* tp = f.ktab + d0 * ts + d1 * kp.kt2 + d2;
       float K[15];
 #pragma unroll
       for (int j = 0; j < 15; j++) K[j] = __ldg(tp + j * tstride);
@@ -1078,33 +1112,386 @@ __global__ void __launch_bounds__(TH, 2) k_mixed(KParams kp, Fields f) {
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       sv[k] += Ud[k];
-      f.sdev[k * N + s] = sv[k];
+      f.sdev[k * N32 + s] = sv[k];
     }
     if (!UPDATE_ONLY) {
       const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
 #pragma unroll
       for (int m = 0; m < STZ_MODES; m++) {
         const float x = mx_x(kp, sv, a, m);
-        neg += x > thr_neg;
-        acc[m] += exp2f(x);
+        xmax = fmaxf(xmax, x);
+        acc[m] += ex2_approx(x);
       }
     }
+    // advance (i0, i1, i2) by TH sites
+    i2 += kp.adv_r2;
+    int carry = 0;
+    if (i2 >= kp.n2) { i2 -= kp.n2; carry = 1; }
+    i1 += kp.adv_q2 + carry;
+    while (i1 >= kp.n1) { i1 -= kp.n1; i0++; }
   }
-  if (UPDATE_ONLY) {
-    if (!last_block(ctl, kp.nblk)) return;
-    if (threadIdx.x == 0) {
-      ctl->ticket = 0;
-      ctl->has_pend = 0;
-      for (int c = 0; c < 6; c++) ctl->U[c] = 0;
-    }
-    return;
-  }
+  // Q < 0 for some mode of some site of this thread
+  const unsigned neg = xmax > thr_neg ? 1u : 0u;
+  if (UPDATE_ONLY) return;
   block_mode_sums_f32(acc, f.part, kp.nblk, b);
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
-  if (!group_reduce(kp, f, b)) return;
-  if (!last_block(ctl, kp.ngroups)) return;
-  finish_step<2>(kp, f);
+  group_reduce(kp, f, b);
+}
+
+// ------------------------------------------------------- mixed-form tail
+// Lane-parallel scalar algebra on the shared control block: lane k of warp 0
+// owns Voigt component k (k < 6); the traces come from warp shuffles. Lanes
+// >= 6 take part in the shuffles only.
+__device__ __forceinline__ double lane_trace(double v, int k) {
+  double t = k < 3 ? v : 0.0;
+  t += __shfl_xor_sync(FULL, t, 1);
+  t += __shfl_xor_sync(FULL, t, 2);
+  t += __shfl_xor_sync(FULL, t, 4);  // lanes 0..7 now hold the sum of lanes 0..2
+  return __shfl_sync(FULL, t, 0);
+}
+// C:e for component k
+__device__ __forceinline__ double lane_C(const KParams& kp, double e, int k) {
+  const double tr = lane_trace(e, k);
+  return (k < 3 ? kp.lambda * tr : 0.0) + 2.0 * kp.mu * e;
+}
+// C^-1:s for component k (3D isotropic compliance)
+__device__ __forceinline__ double lane_Cinv(const KParams& kp, double s, int k) {
+  const double tr = lane_trace(s, k);
+  return (k < 3 ? -kp.inv_lam_coef * tr : 0.0) + s * kp.inv_2mu;
+}
+
+// Thermal event of the mixed form: eigenstrain update, the incremental
+// "solve" (pending response + uniform change U) and the loading of
+// evolution.c:262-317, lane-parallel over the six components.
+__device__ void mixed_commit_lanes(const KParams& kp, const Fields& f, Ctl* c, long long s, int m) {
+  const int k = threadIdx.x & 31;
+  const bool own = k < 6;
+  const long long N = kp.N;
+  const double mk = own ? kp.modes[m][k] : 0.0;
+  if (own) {
+    f.prev_deps[k * N + s] = mk;
+    f.eps0[k * N + s] += mk;
+    c->eps0_sum[k] += mk;
+  }
+  __syncwarp();
+  const double ebar = own ? c->eps_avg[k] : 0.0;
+  const double dA = own ? ebar - c->eps_avg_applied[k] : 0.0;
+  const double CdA = lane_C(kp, dA, k);
+  const double u_old = own ? c->u[k] : 0.0;
+  // mean stress of the field solved with ebar: C:(ebar - <eps*>)
+  const double em = own ? ebar - c->eps0_sum[k] * kp.invN : 0.0;
+  double stress = lane_C(kp, em, k);
+  // subtract_error (evolution.c:263-300): loaded component masked
+  const int lc = kp.loading == STZ_LOAD_SHEAR ? STZ_XY : 0;
+  const double ts = (kp.no_subtract_error || k == lc || !own) ? 0.0 : stress;
+  const double te = lane_Cinv(kp, ts, k);
+  const double t = c->t_kmc, rate = kp.strain_rate, nu = kp.poisson, E = kp.young, mu = kp.mu;
+  double de = 0.0, u_new = 0.0;
+  switch (kp.loading) {
+    case STZ_LOAD_TENSION:
+      de = (k == 0 ? rate * t * 1 : (k == 1 || k == 2) ? rate * t * (-nu) : 0.0) - te;
+      if (k == 0) { stress += E * rate * t; u_new = E * rate * t; }
+      break;
+    case STZ_LOAD_COMPRESSION:
+      de = (k == 0 ? -rate * t * 2 : k == 1 ? rate * t * nu * 2 : 0.0) - te;
+      if (k == 0) { stress += -E * rate * t; u_new = -E * rate * t; }
+      break;
+    case STZ_LOAD_SHEAR:
+      de = k == STZ_XY ? rate * t : -te;
+      if (k == STZ_XY) { stress += 2 * mu * rate * t; u_new = 2 * mu * rate * t; }
+      break;
+    case STZ_LOAD_STRESS: {
+      const double d = own ? kp.applied[k] - stress : 0.0;
+      de = lane_Cinv(kp, d, k);
+      u_new = d;
+      stress = own ? kp.applied[k] : 0.0;
+      break;
+    }
+  }
+  if (own) {
+    c->U[k] = CdA - u_old + u_new;
+    c->eps_avg_applied[k] = ebar;
+    c->eps_avg[k] = ebar + de;
+    c->u[k] = u_new;
+    c->stress[k] = stress;
+  }
+  __syncwarp();
+}
+
+// Search of the mixed form: the group and block levels in FP64 as in
+// search_event; the in-block level sums each thread's FP32 rates once, scans
+// those sums in FP64 and locates the site in FP32 relative to the thread's
+// FP64 offset (the rates themselves are FP32).
+__device__ void search_mixed(const KParams& kp, const Fields& f, double T, const double* sh_inc,
+                             long long* site_out, int* mode_out, double* margin_out) {
+  __shared__ double sh_inc2[TH];
+  __shared__ long long sh_p;
+  __shared__ double sh_cb;
+  __shared__ long long sh_site;
+  __shared__ double sh_margin;
+  const int t = threadIdx.x;
+  const long long P = (long long)STZ_MODES * kp.ngroups;
+  const long long ch = (P + TH - 1) / TH;
+  const long long p0 = t * ch, p1 = min(p0 + ch, P);
+  if (t == 0) { sh_p = -1; sh_site = -1; sh_margin = 0; }
+  __syncthreads();
+  const double I = sh_inc[t];
+  const double E = t > 0 ? sh_inc[t - 1] : 0.0;
+  double Tq = T;
+  if (Tq > sh_inc[TH - 1]) Tq = sh_inc[TH - 1];
+  if (E < Tq && Tq <= I) {
+    double run = E;
+    long long hit = -1, lastpos = -1;
+    double hb = E, lastbefore = E;
+    for (long long q = p0; q < p1; q++) {
+      const double v = f.gsum[q];
+      const double before = run;
+      run += v;
+      if (v > 0) { lastpos = q; lastbefore = before; }
+      if (hit < 0 && v > 0 && run >= Tq) { hit = q; hb = before; }
+    }
+    if (hit < 0) { hit = lastpos; hb = lastbefore; }
+    sh_p = hit;
+    sh_cb = hb;
+  }
+  __syncthreads();
+  const long long pg = sh_p;
+  if (pg < 0) {
+    if (t == 0) { *site_out = -1; *mode_out = -1; }
+    return;
+  }
+  const int m = (int)(pg / kp.ngroups);
+  const int g = (int)(pg - (long long)m * kp.ngroups);
+  if (t < 32) {
+    const int g0 = g * kGroup, g1 = min(g0 + kGroup, kp.nblk);
+    const double v = (g0 + t < g1) ? f.part[(long long)m * kp.nblk + g0 + t] : 0.0;
+    double x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double y = __shfl_up_sync(FULL, x, off);
+      if (t >= off) x += y;
+    }
+    const double before = __shfl_up_sync(FULL, x, 1);
+    const double ex = t > 0 ? before : 0.0;
+    const double Tg = Tq - sh_cb;
+    const unsigned ok = __ballot_sync(FULL, v > 0 && x >= Tg);
+    const unsigned posb = __ballot_sync(FULL, v > 0);
+    const int lane = ok ? __ffs(ok) - 1 : (posb ? 31 - __clz(posb) : -1);
+    if (lane >= 0) {
+      const double exl = __shfl_sync(FULL, ex, lane);
+      if (t == 0) { sh_p = g0 + lane; sh_cb = sh_cb + exl; }
+    } else if (t == 0) {
+      sh_p = -1;
+    }
+  }
+  __syncthreads();
+  if (sh_p < 0) {
+    if (t == 0) { *site_out = -1; *mode_out = -1; }
+    return;
+  }
+  const int b = (int)sh_p;
+  double T2 = Tq - sh_cb;
+  const long long s0 = (long long)b * kp.bsites;
+  const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
+  const long long per = (s1 - s0 + TH - 1) / TH;
+  const long long a0 = s0 + t * per;
+  float rr[kSptMixed];
+  float locf = 0.f;
+  double zero[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < kSptMixed; k++) {
+    const long long s = a0 + k;
+    rr[k] = (k < per && s < s1) ? (float)site_rate<2>(kp, f, zero, 0.0, s, m) : 0.f;
+    locf += rr[k];
+  }
+  const double I2 = block_incl_scan((double)locf, sh_inc2);
+  const double E2 = t > 0 ? sh_inc2[t - 1] : 0.0;
+  const double tot2 = sh_inc2[TH - 1];
+  if (T2 > tot2) T2 = tot2;
+  if (!(T2 > 0)) T2 = DBL_MIN;
+  if (E2 < T2 && T2 <= I2) {
+    const float rem = (float)(T2 - E2);
+    float run = 0.f;
+    int hit = -1, lastk = -1;
+    float hb = 0.f, ha = 0.f, lb = 0.f, la = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSptMixed; k++) {
+      const float before = run;
+      run += rr[k];
+      const bool pos = rr[k] > 0.f;
+      if (pos) { lastk = k; lb = before; la = run; }
+      if (hit < 0 && pos && run >= rem) { hit = k; hb = before; ha = run; }
+    }
+    if (hit < 0) { hit = lastk; hb = lb; ha = la; }
+    sh_site = hit < 0 ? -1 : a0 + hit;
+    sh_margin = (double)fminf(rem - hb, ha - rem);
+  }
+  __syncthreads();
+  if (t == 0) {
+    *site_out = sh_site;
+    *mode_out = m;
+    *margin_out = sh_margin;
+  }
+}
+
+// The scalar part of the control block (everything before the generator).
+constexpr int kCtlScalarWords = (int)(offsetof(Ctl, rng) / 4);
+
+// One block after the grid of k_mixed: total rate, step kind, dice, search,
+// commit, log and the halt conditions of the mixed form.
+__global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int update_only) {
+  Ctl* const g = f.ctl;
+  if (update_only) {
+    if (threadIdx.x < 6) g->U[threadIdx.x] = 0;
+    if (threadIdx.x == 0) g->has_pend = 0;
+    return;
+  }
+  if (g->halt) return;
+  const unsigned long long t_tail = gtimer();
+  __shared__ Ctl sc;
+  __shared__ double sh_inc[TH];
+  __shared__ int sh_kind;
+  __shared__ double sh_T, sh_R;
+  __shared__ long long sh_site;
+  __shared__ int sh_mode;
+  __shared__ double sh_margin;
+  {
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(g);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
+    for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
+  }
+  const long long P = (long long)STZ_MODES * kp.ngroups;
+  const long long ch = (P + TH - 1) / TH;
+  const long long p0 = threadIdx.x * ch, p1 = min(p0 + ch, P);
+  double S = 0;
+  for (long long p = p0; p < p1; p++) S += f.gsum[p];
+  block_incl_scan(S, sh_inc);
+  const unsigned long long t_sums = gtimer();
+  block_twist_if_needed(&g->rng);
+  Ctl* c = &sc;
+  if (threadIdx.x == 0) {
+    c->step++;
+    c->has_pend = 0;
+    for (int k = 0; k < 6; k++) c->U[k] = 0;
+    const double Rraw = sh_inc[TH - 1];
+    const double R = Rraw * kp.rate_scale;
+    sh_R = Rraw;
+    c->total_rate = R;
+    int kind;
+    if (c->neg_count > 0) {
+      kind = kAthermal;
+      c->halt = 1;
+      c->halt_reason = kHaltAthermal;
+    } else if (!(R > 0) || !isfinite(R)) {
+      kind = kNone;
+      c->status = STZ_ERR_NAN;
+      c->halt = 1;
+      c->halt_reason = kHaltError;
+    } else {
+      const double t_kmc = 1 / R;
+      if (t_kmc < kp.dt) {
+        kind = kThermal;
+        c->kstep++;
+        // one draw: the word at mti, tempered (the block refilled the state above)
+        const int i = g->rng.mti;
+        uint32_t y = g->rng.mt[i];
+        g->rng.mti = i + 1;
+        y ^= (y >> 11);
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= (y >> 18);
+        const double dice = y / 4294967296.0;
+        sh_T = dice * Rraw;
+        c->t_kmc = t_kmc;
+        if (!(dice > 0)) {
+          kind = kNone;
+          c->status = STZ_ERR_NO_EVENT;
+          c->halt = 1;
+          c->halt_reason = kHaltError;
+        }
+      } else {
+        kind = kElastic;
+      }
+    }
+    c->neg_count = 0;
+    c->step_kind = kind;
+    sh_kind = kind;
+  }
+  __syncthreads();
+  const unsigned long long t_dec = gtimer();
+  const int kind = sh_kind;
+  if (kind == kThermal) {
+    search_mixed(kp, f, sh_T, sh_inc, &sh_site, &sh_mode, &sh_margin);
+    __syncthreads();
+  }
+  const unsigned long long t_search = gtimer();
+  if (threadIdx.x < 32) {
+    const long long s = sh_site;
+    const int m = sh_mode;
+    if (kind == kThermal && s >= 0) mixed_commit_lanes(kp, f, c, s, m);
+    if (threadIdx.x == 0) {
+      const double Rtrue = sh_R * kp.rate_scale;
+      if (kind == kThermal) {
+        if (s < 0) {
+          c->status = STZ_ERR_NO_EVENT;
+          c->halt = 1;
+          c->halt_reason = kHaltError;
+          c->step_kind = kNone;
+        } else {
+          if (sh_margin < 1e-12 * sh_R) c->near_ties++;
+          float sv[5];
+          for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+          const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
+          const double q = (double)kp.q_ref - (double)mx_x(kp, sv, a, m) * kp.inv_a_scale;
+          c->sel_site = s;
+          c->sel_mode = m;
+          c->sel_q = q;
+          c->has_pend = 1;
+          c->pend_site = s;
+          c->pend_mode = m;
+          c->totime += c->t_kmc;
+          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime, c->t_kmc, q, Rtrue);
+          if (kp.resolve_period > 0 && c->kstep >= c->next_resolve) {
+            c->halt = 1;
+            c->halt_reason = kHaltResolve;
+          }
+        }
+      } else if (kind == kElastic) {
+        c->estep++;
+        c->totime += kp.dt;
+        double u0[6];
+        for (int k = 0; k < 6; k++) u0[k] = c->u[k];
+        elastic_step(kp, c);
+        for (int k = 0; k < 6; k++) c->U[k] = c->u[k] - u0[k];
+        log_event(kp, f, c, STZ_EV_ELASTIC, -1, -1, c->totime, kp.dt, 0.0, Rtrue);
+      }
+      if ((kind == kThermal || kind == kElastic) && c->step_kind != kNone) {
+        if (print_check(kp, c)) {
+          c->print_done = 1;
+          c->halt = 1;
+          c->halt_reason = kHaltPrint;
+        } else {
+          if (!c->halt) stop_check(kp, c);
+          c->step_kind = kNone;
+        }
+      }
+      const unsigned long long t_end = gtimer();
+      c->prof_main_ns += t_tail - c->prof_t0;
+      c->prof_tail_ns += t_end - t_tail;
+      c->prof_part_ns[0] += t_sums - t_tail;
+      c->prof_part_ns[1] += t_dec - t_sums;
+      c->prof_part_ns[2] += t_search - t_dec;
+      c->prof_part_ns[3] += t_end - t_search;
+      c->prof_n++;
+    }
+  }
+  __syncthreads();
+  {
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(&sc);
+    uint32_t* d = reinterpret_cast<uint32_t*>(g);
+    for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
+  }
 }
 
 // After a full FP64 re-solve into sdev (mixed form).
@@ -1189,9 +1576,18 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st) {
   else k_rate64<1><<<kp.nblk, TH, 0, st>>>(kp, f);
 }
 
-void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
+void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed<1><<<kp.nblk, TH, 0, st>>>(kp, f);
   else k_mixed<0><<<kp.nblk, TH, 0, st>>>(kp, f);
+}
+
+void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
+  k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
+}
+
+void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
+  launch_mixed_main(kp, f, update_only, st);
+  launch_mixed_tail(kp, f, update_only, st);
 }
 
 void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t st) {

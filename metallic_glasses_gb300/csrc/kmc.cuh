@@ -17,6 +17,10 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
 // Mixed form: incremental stress update + rates + selection/commit.
 // update_only: apply the pending transformation and uniform change, nothing else.
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
+// The two halves of launch_mixed: the grid-wide update/rate kernel and the
+// one-block selection/commit kernel.
+void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
+void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
 // Athermal avalanche (evolution.c:47-100): mark sites, then commit in order.
 void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t st);
 // Bookkeeping after the solve of a step (loading, clock, print check) and

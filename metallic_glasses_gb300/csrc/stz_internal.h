@@ -72,6 +72,9 @@ struct Ctl {
   int sel_mode;
   long long sel_site;
   int ath_count;
+  // device-clock phase times of the mixed-form kernel (globaltimer, ns)
+  unsigned long long prof_t0, prof_main_ns, prof_tail_ns, prof_n;
+  unsigned long long prof_part_ns[8];  // tail: copy-in+sums, twist+decision, search, commit
   MT rng;
 };
 
@@ -107,8 +110,9 @@ struct KParams {
   long long N, Nk;
   int nblk, bsites;          // rate kernel: blocks and sites per block
   int ngroups;               // groups of kGroup blocks
+  int adv_q2, adv_r2;        // kRateThreads sites = adv_q2 rows of n2 plus adv_r2 sites
   int fast_inv;              // mixed form: precomputed compliance coefficients
-  double inv_2mu, inv_lam_coef, invN;
+  double inv_2mu, inv_lam_coef, invN, inv_a_scale;
   int loading, softening, sf_scheme, no_subtract_error, shear_quirk;
   double lambda, mu, young, poisson;
   double kT, vt, V0, dt, gamma0;
