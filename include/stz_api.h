@@ -225,6 +225,21 @@ int stz_run(stz_ctx* ctx, int64_t max_steps, int64_t max_events);
  * reference's elastic solve). */
 int stz_solve(stz_ctx* ctx);
 
+/* The same solve without any device allocation, for callers that cannot call
+ * cudaMalloc (code running inside another framework's memory pool or budget,
+ * or inside a region recorded for replay). No counterpart in the reference.
+ * The caller passes device buffers eps0_dev [nc][N] and sigma_dev [nc][N]
+ * (nc = 3 for dim 2 with n0 == 1, 6 for dim 3), the mean strain eps_avg
+ * (nc host doubles) and a cudaStream_t (or NULL); sigma = C:(eps - eps*)
+ * with <eps> = eps_avg. Scratch is one fixed device array (about 13 MB, held
+ * by every GPU that loads the library until exit) that fits at most six
+ * components of 64^3 (2D up to 512^2); larger grids return STZ_ERR_INVALID.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. All calls share the array: calls
+ * that overlap on the GPU race. Synchronises the stream before returning. */
+int stz_solve_noalloc(int32_t dim, int32_t n0, int32_t n1, int32_t n2, double lambda, double mu,
+                      const double* eps0_dev, const double* eps_avg, double* sigma_dev, void* stream);
+
 int stz_get_scalars(stz_ctx* ctx, stz_scalars* out);
 /* Copy out log entries [first, first+cap) ; *n receives the number copied. */
 int stz_get_events(stz_ctx* ctx, int64_t first, stz_event* out, int64_t cap, int64_t* n);

@@ -100,6 +100,8 @@ def load_library(path=None):
     lib.stz_kernel_time.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.stz_transfer_bytes.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.stz_phase_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    lib.stz_solve_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                      vp, C.POINTER(C.c_double), vp, vp]
     lib.stz_sizeof.argtypes = [C.c_int32]
     lib.stz_sizeof.restype = C.c_int64
     for name, s in ((0, Params), (1, Event), (2, Scalars)):

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libstz_gb300.so")
-SOURCES = ["fft.cu", "kmc.cu", "engine.cu", "params.cpp"]
+SOURCES = ["fft.cu", "kmc.cu", "engine.cu", "noalloc.cu", "params.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-diag-suppress", "177,128"]

@@ -28,6 +28,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
+#include <algorithm>
 
 #include "fft.cuh"
 
@@ -678,6 +680,58 @@ int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
   size_t sc_max = p->smem_c2r + sizeof(double) * nc * p->L_x * n2;
   set_smem_attrs<double>(p->smem_x, p->smem_y, p->smem_g, sc_max);
   set_smem_attrs<float>(p->smem_x, p->smem_y, p->smem_g, sc_max);
+  return STZ_OK;
+}
+
+// Plan whose twiddle tables live in caller-provided device storage (for the
+// allocation-free entry point). FP64 transforms only; no device allocation.
+size_t fft_twiddle_count(int n0, int n1, int n2) { return (size_t)(n2 / 2) + n1 + n0 + (n2 / 2 + 1); }
+
+int fft_plan_init_in(FFTPlan* p, int n0, int n1, int n2, int nc, double2* storage, size_t cap, cudaStream_t st) {
+  std::memset((void*)p, 0, sizeof(*p));
+  if (n2 < 2 || n2 % 2 != 0 || n1 < 1 || n0 < 1) return STZ_ERR_INVALID;
+  p->n0 = n0; p->n1 = n1; p->n2 = n2; p->nc = nc;
+  p->h = n2 / 2;
+  p->nh = p->h + 1;
+  p->N = (long long)n0 * n1 * n2;
+  p->Nk = (long long)n0 * n1 * p->nh;
+  p->sh = make_sched(p->h);
+  p->s1 = make_sched(n1);
+  p->s0 = make_sched(n0);
+  if (p->sh.nst < 0 || p->s1.nst < 0 || p->s0.nst < 0) return STZ_ERR_INVALID;
+  if (p->h > 4096 || n1 > 1024 || n0 > 1024) return STZ_ERR_INVALID;
+  if (fft_twiddle_count(n0, n1, n2) > cap) return STZ_ERR_INVALID;
+  const int lens[4] = {p->h, n1, n0, n2};
+  const int counts[4] = {p->h, n1, n0, p->nh};
+  double2** dst[4] = {&p->tw_h, &p->tw_1, &p->tw_0, &p->tw_p};
+  std::vector<double2> host(fft_twiddle_count(n0, n1, n2));
+  size_t off = 0;
+  for (int t = 0; t < 4; t++) {
+    for (int k = 0; k < counts[t]; k++) {
+      const double ang = -2.0 * M_PI * (double)k / (double)lens[t];
+      host[off + k] = make_double2(std::cos(ang), std::sin(ang));
+    }
+    *dst[t] = storage + off;
+    off += counts[t];
+  }
+  if (cudaMemcpyAsync(storage, host.data(), sizeof(double2) * host.size(), cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
+    return STZ_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return STZ_ERR_CUDA;
+  const size_t cz = sizeof(double2);
+  p->L_x = std::max(1, 1024 / p->h);
+  while (p->L_x > 1 && 2 * (size_t)p->L_x * (p->h + 2) * cz + sizeof(double) * nc * p->L_x * n2 > 200 * 1024) p->L_x /= 2;
+  p->L_y = 8;
+  while (p->L_y > 1 && 2 * (size_t)p->L_y * (n1 + 1) * cz > 100 * 1024) p->L_y /= 2;
+  const int ng = n0 > 1 ? n0 : n1;
+  p->L_g = 8;
+  while (p->L_g > 1 && 2 * (size_t)nc * p->L_g * (ng + 1) * cz > 200 * 1024) p->L_g /= 2;
+  p->smem_x = 2 * (size_t)p->L_x * (p->h + 1) * cz;
+  p->smem_c2r = 2 * (size_t)p->L_x * (p->h + 2) * cz;
+  p->smem_y = 2 * (size_t)p->L_y * (n1 + 1) * cz;
+  p->smem_g = 2 * (size_t)nc * p->L_g * (ng + 1) * cz;
+  if (p->smem_g > 227 * 1024) return STZ_ERR_INVALID;
+  set_smem_attrs<double>(p->smem_x, p->smem_y, p->smem_g, p->smem_c2r + sizeof(double) * nc * p->L_x * n2);
   return STZ_OK;
 }
 

@@ -37,6 +37,10 @@ struct FFTPlan {
 };
 
 int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc);
+// A plan whose twiddle tables are written into caller-provided device storage
+// of at least fft_twiddle_count() elements (FP64 transforms only).
+size_t fft_twiddle_count(int n0, int n1, int n2);
+int fft_plan_init_in(FFTPlan* p, int n0, int n1, int n2, int nc, double2* storage, size_t cap, cudaStream_t st);
 // number of blocks of the C2R pass (the length of one component's msum row)
 int fft_c2r_blocks(const FFTPlan& p);
 void fft_plan_destroy(FFTPlan* p);
