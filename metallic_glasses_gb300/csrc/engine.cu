@@ -209,14 +209,21 @@ void mixed_constants(stz_ctx* c) {
   kp.a_scale = (float)(l2e / kp.kT);
   kp.inv_a_scale = 1.0 / (double)kp.a_scale;
   kp.rate_scale = kp.vt * std::exp(-(double)kp.q_ref / kp.kT);
+  double nmax = 0;
   for (int m = 0; m < STZ_MODES; m++) {
-    double d[5];
+    double d[5], n2 = 0;
     dev_coords(kp.modes[m], d);
     for (int k = 0; k < 5; k++) {
       kp.mdev_raw[m][k] = (float)d[k];
       kp.mdev[m][k] = (float)(d[k] * cW * 0.5 * l2e / kp.kT);
+      n2 += (double)kp.mdev[m][k] * kp.mdev[m][k];
     }
+    nmax = std::max(nmax, std::sqrt(n2));
   }
+  for (int j = 0; j < STZ_MODES / 2; j++)
+    for (int k = 0; k < 5; k++) kp.mdev2[j][k] = make_float2(kp.mdev[2 * j][k], kp.mdev[2 * j + 1][k]);
+  kp.inv_mdev_norm = (float)(1.0 / std::max(nmax, 1e-300));
+  kp.bound_slack = 1.001f;  // covers FP32 rounding of the bound itself
 }
 
 // ------------------------------------------------------------- solves
@@ -261,7 +268,7 @@ int build_response_table(stz_ctx* c) {
   const long long N = kp.N;
   const long long tn = (long long)kp.kt0 * kp.kt1 * kp.kt2;
   int st;
-  if ((st = dalloc(&c->f.ktab, (size_t)15 * tn))) return st;
+  if ((st = dalloc(&c->f.ktab, (size_t)16 * tn))) return st;
   double *eps = nullptr, *sig = nullptr;
   if ((st = dalloc(&eps, (size_t)6 * N))) return st;
   if ((st = dalloc(&sig, (size_t)6 * N))) { cudaFree(eps); return st; }
@@ -488,8 +495,18 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   kp.nh = kp.n2 / 2 + 1;
   kp.N = (long long)kp.n0 * kp.n1 * kp.n2;
   kp.Nk = (long long)kp.n0 * kp.n1 * kp.nh;
-  const int spt = mixed ? kSptMixed : kSptFp64;
-  kp.bsites = kRateThreads * spt;
+  if (mixed) {
+    // one wave of resident blocks, each owning a contiguous run of sites
+    // (at most kMaxPerMixed per thread; larger grids take several waves)
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device);
+    const long long wave = (long long)std::max(sms, 1) * mixed_blocks_per_sm();
+    long long per = (kp.N + wave * kRateThreads - 1) / (wave * kRateThreads);
+    per = std::max(1LL, std::min(per, (long long)kMaxPerMixed));
+    kp.bsites = (int)(kRateThreads * per);
+  } else {
+    kp.bsites = kRateThreads * kSptFp64;
+  }
   kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
   kp.ngroups = (kp.nblk + kGroup - 1) / kGroup;
   kp.adv_q2 = kRateThreads / kp.n2;

@@ -308,6 +308,13 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
+// Programmatic dependent launch: wait until the preceding kernel of the
+// stream has completed and its writes are visible (a no-op when the kernel
+// was launched without the attribute), and let the following kernel be
+// scheduled early (it still waits for this one before touching memory).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -600,7 +607,7 @@ __device__ void search_event(const KParams& kp, const Fields& f, const double* u
   const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
   const long long per = (s1 - s0 + TH - 1) / TH;
   const long long a0 = s0 + t * per;
-  constexpr int kMaxPer = MODEL == 2 ? kSptMixed : kSptFp64;  // sites per thread
+  constexpr int kMaxPer = MODEL == 2 ? kMaxPerMixed : kSptFp64;  // sites per thread
   double rr[kMaxPer];
   double loc = 0;
 #pragma unroll
@@ -1041,6 +1048,7 @@ __device__ __forceinline__ int fold(int d, int n, int* flip) {
 template <int UPDATE_ONLY>
 __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
+  pdl_wait();
   if (ctl->halt && !UPDATE_ONLY) return;
   if (!UPDATE_ONLY && blockIdx.x == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
   const int b = blockIdx.x;
@@ -1068,12 +1076,12 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
     ud[4] = q2 * U6[5];
     for (int k = 0; k < 5; k++) Ud[k] = (float)ud[k];
   }
-  const int ts = kp.kt1 * kp.kt2, tstride = kp.kt0 * ts;
-  float acc[STZ_MODES];
+  const int ts = kp.kt1 * kp.kt2;
+  float2 acc2[STZ_MODES / 2];
 #pragma unroll
-  for (int m = 0; m < STZ_MODES; m++) acc[m] = 0.f;
+  for (int j = 0; j < STZ_MODES / 2; j++) acc2[j] = make_float2(0.f, 0.f);
   const float thr_neg = kp.q_ref * kp.a_scale;
-  float xmax = -INFINITY;
+  unsigned neg = 0;
   // site coordinates, advanced incrementally by TH sites per iteration
   const int N32 = (int)N;
   int s = (int)s0 + (int)threadIdx.x;
@@ -1090,10 +1098,14 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
       const int d2 = fold(i2 - p2, kp.n2, &fx);
       const float sx = fx ? -1.f : 1.f, sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
       const float sg[5] = {1.f, 1.f, sy * sz, sx * sz, sx * sy};
-      const float* tp = f.ktab + d0 * ts + d1 * kp.kt2 + d2;
-      float K[15];
+      // one 64-byte record per octant point: the 15 packed entries + padding
+      const float4* tp = reinterpret_cast<const float4*>(f.ktab) + 4 * (d0 * ts + d1 * kp.kt2 + d2);
+      float K[16];
 #pragma unroll
-      for (int j = 0; j < 15; j++) K[j] = __ldg(tp + j * tstride);
+      for (int j = 0; j < 4; j++) {
+        const float4 v = __ldg(tp + j);
+        K[4 * j] = v.x; K[4 * j + 1] = v.y; K[4 * j + 2] = v.z; K[4 * j + 3] = v.w;
+      }
       float e[5];
 #pragma unroll
       for (int k = 0; k < 5; k++) e[k] = sg[k] * de[k];
@@ -1115,12 +1127,22 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
       f.sdev[k * N32 + s] = sv[k];
     }
     if (!UPDATE_ONLY) {
-      const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
+      const float dFs = f.dF32[s];
+      const float a = (kp.q_ref - dFs) * kp.a_scale;
+      // two modes per packed FMA; each lane is the scalar chain of mx_x
 #pragma unroll
-      for (int m = 0; m < STZ_MODES; m++) {
-        const float x = mx_x(kp, sv, a, m);
-        xmax = fmaxf(xmax, x);
-        acc[m] += ex2_approx(x);
+      for (int j = 0; j < STZ_MODES / 2; j++) {
+        float2 x = make_float2(a, a);
+#pragma unroll
+        for (int k = 0; k < 5; k++) x = __ffma2_rn(make_float2(sv[k], sv[k]), kp.mdev2[j][k], x);
+        acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(x.x), ex2_approx(x.y)));
+      }
+      // Q < 0 for some mode needs |W|/2 > dF; |W| <= |s| |deps| bounds it
+      const float n2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] + sv[3] * sv[3] + sv[4] * sv[4];
+      const float lim = dFs * kp.a_scale * kp.inv_mdev_norm;
+      if (n2 * kp.bound_slack >= lim * lim || lim <= 0.f) {
+#pragma unroll 1
+        for (int m = 0; m < STZ_MODES; m++) neg |= mx_x(kp, sv, a, m) > thr_neg ? 1u : 0u;
       }
     }
     // advance (i0, i1, i2) by TH sites
@@ -1130,9 +1152,14 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
     i1 += kp.adv_q2 + carry;
     while (i1 >= kp.n1) { i1 -= kp.n1; i0++; }
   }
-  // Q < 0 for some mode of some site of this thread
-  const unsigned neg = xmax > thr_neg ? 1u : 0u;
   if (UPDATE_ONLY) return;
+  pdl_release();
+  float acc[STZ_MODES];
+#pragma unroll
+  for (int j = 0; j < STZ_MODES / 2; j++) {
+    acc[2 * j] = acc2[j].x;
+    acc[2 * j + 1] = acc2[j].y;
+  }
   block_mode_sums_f32(acc, f.part, kp.nblk, b);
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
@@ -1296,11 +1323,11 @@ __device__ void search_mixed(const KParams& kp, const Fields& f, double T, const
   const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
   const long long per = (s1 - s0 + TH - 1) / TH;
   const long long a0 = s0 + t * per;
-  float rr[kSptMixed];
+  float rr[kMaxPerMixed];
   float locf = 0.f;
   double zero[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
-  for (int k = 0; k < kSptMixed; k++) {
+  for (int k = 0; k < kMaxPerMixed; k++) {
     const long long s = a0 + k;
     rr[k] = (k < per && s < s1) ? (float)site_rate<2>(kp, f, zero, 0.0, s, m) : 0.f;
     locf += rr[k];
@@ -1316,7 +1343,7 @@ __device__ void search_mixed(const KParams& kp, const Fields& f, double T, const
     int hit = -1, lastk = -1;
     float hb = 0.f, ha = 0.f, lb = 0.f, la = 0.f;
 #pragma unroll
-    for (int k = 0; k < kSptMixed; k++) {
+    for (int k = 0; k < kMaxPerMixed; k++) {
       const float before = run;
       run += rr[k];
       const bool pos = rr[k] > 0.f;
@@ -1342,6 +1369,8 @@ constexpr int kCtlScalarWords = (int)(offsetof(Ctl, rng) / 4);
 // commit, log and the halt conditions of the mixed form.
 __global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int update_only) {
   Ctl* const g = f.ctl;
+  pdl_wait();
+  pdl_release();
   if (update_only) {
     if (threadIdx.x < 6) g->U[threadIdx.x] = 0;
     if (threadIdx.x == 0) g->has_pend = 0;
@@ -1554,7 +1583,7 @@ __global__ void k_ktab_column(KParams kp, const double* sig, float* ktab, int b)
     for (int a = 0; a <= b; a++) {
       // packed index of (a, b), a <= b, row-major upper triangle
       const int idx = a * 5 - a * (a - 1) / 2 + (b - a);
-      ktab[idx * tn + t] = (float)d[a];
+      ktab[16 * t + idx] = (float)d[a];
     }
   }
 }
@@ -1576,13 +1605,40 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st) {
   else k_rate64<1><<<kp.nblk, TH, 0, st>>>(kp, f);
 }
 
+int mixed_blocks_per_sm() {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed<0>, TH, 0) != cudaSuccess || occ < 1) occ = 1;
+  return occ;
+}
+
+namespace {
+// Launch with the programmatic-stream-serialization attribute: the kernel may
+// be scheduled while the previous kernel of the stream finishes; it waits for
+// it with griddepcontrol.wait.
+template <typename... A>
+void launch_pdl(void (*kern)(A...), int grid, cudaStream_t st, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(TH);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+}  // namespace
+
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed<1><<<kp.nblk, TH, 0, st>>>(kp, f);
-  else k_mixed<0><<<kp.nblk, TH, 0, st>>>(kp, f);
+  else launch_pdl(k_mixed<0>, kp.nblk, st, kp, f);
 }
 
 void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
-  k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
+  if (update_only) k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
+  else launch_pdl(k_mixed_tail, 1, st, kp, f, update_only);
 }
 
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {

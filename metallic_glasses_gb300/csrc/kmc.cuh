@@ -7,7 +7,7 @@
 namespace stz {
 
 constexpr int kRateThreads = 256;
-constexpr int kSptMixed = 8;   // sites per thread of the mixed-form kernel
+constexpr int kMaxPerMixed = 24;  // most sites per thread of the mixed-form kernel
 constexpr int kSptFp64 = 4;    // sites per thread of the FP64 rate kernels
 constexpr int kGroup = 32;     // blocks per group in the two-level rate sums
 
@@ -17,6 +17,8 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
 // Mixed form: incremental stress update + rates + selection/commit.
 // update_only: apply the pending transformation and uniform change, nothing else.
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
+// Resident blocks per SM of the mixed-form kernel (occupancy query).
+int mixed_blocks_per_sm();
 // The two halves of launch_mixed: the grid-wide update/rate kernel and the
 // one-block selection/commit kernel.
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);

@@ -11,6 +11,7 @@
 #ifdef __CUDACC__
 #include <cuda_runtime.h>
 #else
+#include <vector_types.h>
 typedef struct CUstream_st* cudaStream_t;
 typedef struct CUevent_st* cudaEvent_t;
 typedef struct CUgraphExec_st* cudaGraphExec_t;
@@ -97,7 +98,7 @@ struct Fields {
   double* gsum = nullptr;    // [MODES][ngroups] per (mode, group of blocks) sums
   unsigned* gticket = nullptr;  // [ngroups] last-block counters of the groups
   void* spec = nullptr;      // [nc][Nk] complex FP64 spectrum
-  float* ktab = nullptr;     // mixed: [15][kt0][kt1][kt2] response table
+  float* ktab = nullptr;     // mixed: [kt0][kt1][kt2][16] response table (15 used)
   stz_event* log = nullptr;  // event ring
   Ctl* ctl = nullptr;
   double* scratch = nullptr;  // small scratch (error statistics nobody reads)
@@ -122,6 +123,9 @@ struct KParams {
   double modes[STZ_MODES][6];      // GLOBAL3D mode table (Voigt, tensor shear)
   // mixed form
   float mdev[STZ_MODES][5];        // mode deviatoric coords * (c/2) * log2(e)/kT
+  float2 mdev2[STZ_MODES / 2][5];  // the same, modes paired (2j, 2j+1) for packed FMA
+  float inv_mdev_norm;             // 1 / max_m |mdev[m]|
+  float bound_slack;               // > 1: margin of the |W| bound test
   float a_scale;                   // log2(e)/kT
   float q_ref;                     // reference barrier of the scaled rates
   double rate_scale;               // vt * exp(-q_ref/kT): true rate per scaled unit
