@@ -142,7 +142,8 @@ typedef struct stz_params {
   int32_t solver;            /* STZ_SOLVER_* */
   int32_t resolve_period;    /* mixed: FP64 full re-solve every this many events (0 = never) */
   int32_t device;            /* CUDA device ordinal */
-  int32_t reserved[8];
+  int32_t log_capacity;      /* device event-ring entries (0: 1 << 20) */
+  int32_t reserved[7];
 } stz_params;
 
 /* kinds of stz_event */
@@ -220,6 +221,21 @@ const char* stz_last_error(void);   /* thread-local message of the last failure 
  * events have been done, or the run stops (end strain / instability). The
  * event log keeps every thermal, athermal and elastic step of the run. */
 int stz_run(stz_ctx* ctx, int64_t max_steps, int64_t max_events);
+
+/* ---- batches of independent replicas (mixed form, 3D) ---------------------
+ * Every replica keeps its own state, seed, grid, temperature and loading; one
+ * round advances every replica that is not done by one driver step, with one
+ * grid-wide launch over all replicas' sites and one selection block per
+ * replica. Rounds are captured in CUDA graphs. */
+typedef struct stz_batch stz_batch;
+int  stz_batch_create(const stz_params* params, int32_t count, stz_batch** out);
+void stz_batch_destroy(stz_batch* b);
+/* Advance every replica by up to `events` thermal events (fewer when it stops). */
+int  stz_batch_run(stz_batch* b, int64_t events);
+int  stz_batch_size(stz_batch* b);
+/* The context of replica i (for stz_get_scalars / stz_get_events / stz_get_field).
+ * It stays owned by the batch. */
+stz_ctx* stz_batch_replica(stz_batch* b, int32_t i);
 
 /* Re-solve the stress field from the accumulated eigenstrain in FP64 (the
  * reference's elastic solve). */

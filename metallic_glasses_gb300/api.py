@@ -43,7 +43,7 @@ class Params(C.Structure):
         ("xmro_frac", C.c_double), ("xq0amp", C.c_double), ("random_ratio", C.c_double),
         ("init_mro", C.c_int32), ("print_period", C.c_int32), ("seed", C.c_uint64),
         ("precision", C.c_int32), ("solver", C.c_int32), ("resolve_period", C.c_int32), ("device", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("log_capacity", C.c_int32), ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -102,6 +102,13 @@ def load_library(path=None):
     lib.stz_phase_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.stz_solve_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
                                       vp, C.POINTER(C.c_double), vp, vp]
+    lib.stz_batch_create.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(vp)]
+    lib.stz_batch_destroy.argtypes = [vp]
+    lib.stz_batch_destroy.restype = None
+    lib.stz_batch_run.argtypes = [vp, C.c_int64]
+    lib.stz_batch_size.argtypes = [vp]
+    lib.stz_batch_replica.argtypes = [vp, C.c_int32]
+    lib.stz_batch_replica.restype = vp
     lib.stz_sizeof.argtypes = [C.c_int32]
     lib.stz_sizeof.restype = C.c_int64
     for name, s in ((0, Params), (1, Event), (2, Scalars)):
@@ -157,9 +164,9 @@ class Engine:
         self.nc = 3 if params.model == MODEL_REF2D else 6
 
     def close(self):
-        if self.h:
+        if self.h and not getattr(self, "_borrowed", False):
             self.lib.stz_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -228,8 +235,50 @@ class Engine:
         _check(self.lib.stz_transfer_bytes(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    @classmethod
+    def _borrow(cls, lib, handle, params):
+        e = cls.__new__(cls)
+        e.lib = lib
+        e.params = params
+        e.h = C.c_void_p(handle)
+        e.N = params.n[0] * params.n[1] * params.n[2]
+        e.nc = 3 if params.model == MODEL_REF2D else 6
+        e._borrowed = True
+        return e
+
     def kernel_time(self, steps=64, which=0):
         ms = C.c_double()
         n = C.c_int64(steps)
         _check(self.lib.stz_kernel_time(self.h, which, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+
+class Batch:
+    """Independent replicas advanced together (mixed form, 3D)."""
+
+    def __init__(self, params_list):
+        self.lib = load_library()
+        n = len(params_list)
+        arr = (Params * n)(*params_list)
+        self.params = list(params_list)
+        h = C.c_void_p()
+        _check(self.lib.stz_batch_create(arr, n, C.byref(h)))
+        self.h = h
+        self.replicas = [Engine._borrow(self.lib, self.lib.stz_batch_replica(h, i), params_list[i])
+                         for i in range(n)]
+
+    def run(self, events):
+        _check(self.lib.stz_batch_run(self.h, events))
+
+    def close(self):
+        if self.h:
+            for r in self.replicas:
+                r.h = None
+            self.lib.stz_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -315,6 +315,8 @@ void enqueue_plain_step(stz_ctx* c) {
 }
 
 int sync_ctl(stz_ctx* c) {
+  // a failed launch (configuration or resources) leaves an error here
+  CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&c->host_ctl, c->f.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   c->d2h_bytes += sizeof(Ctl);
@@ -456,7 +458,13 @@ using namespace stz;
 // ============================================================= C ABI
 extern "C" const char* stz_last_error(void) { return g_err; }
 
-extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
+namespace stz {
+int create_ctx(const stz_params* pin, stz_ctx** out, int per_override);
+}
+
+extern "C" int stz_create(const stz_params* pin, stz_ctx** out) { return stz::create_ctx(pin, out, 0); }
+
+int stz::create_ctx(const stz_params* pin, stz_ctx** out, int per_override) {
   if (!pin || !out) return STZ_ERR_INVALID;
   *out = nullptr;
   const stz_params& p = *pin;
@@ -502,6 +510,7 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device);
     const long long wave = (long long)std::max(sms, 1) * mixed_blocks_per_sm();
     long long per = (kp.N + wave * kRateThreads - 1) / (wave * kRateThreads);
+    if (per_override > 0) per = per_override;
     per = std::max(1LL, std::min(per, (long long)kMaxPerMixed));
     kp.bsites = (int)(kRateThreads * per);
   } else {
@@ -529,7 +538,7 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
   kp.print_thr = p.print_period * p.strain_increment * 0.99;
   for (int i = 0; i < 6; i++) kp.applied[i] = p.applied_stress[i];
   kp.kt0 = kp.n0 / 2 + 1; kp.kt1 = kp.n1 / 2 + 1; kp.kt2 = kp.n2 / 2 + 1;
-  kp.log_cap = 1 << 20;
+  kp.log_cap = p.log_capacity > 0 ? p.log_capacity : (1 << 20);
   kp.fast_inv = mixed ? 1 : 0;
   kp.inv_2mu = 1.0 / (2.0 * p.mu);
   kp.inv_lam_coef = p.lambda / (2.0 * p.mu * ((ref2d ? 2.0 : 3.0) * p.lambda + 2.0 * p.mu));
@@ -621,9 +630,6 @@ extern "C" int stz_create(const stz_params* pin, stz_ctx** out) {
     set_error("initial solve failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail(STZ_ERR_CUDA);
   }
-  // L2 flush buffer (larger than the 126 MB L2)
-  c->l2flush_bytes = (size_t)256 << 20;
-  if (cudaMalloc(&c->l2buf, c->l2flush_bytes) != cudaSuccess) { c->l2buf = nullptr; c->l2flush_bytes = 0; }
   c->launches = 0;
   *out = c;
   return STZ_OK;
@@ -912,7 +918,16 @@ extern "C" int stz_timer_stop(stz_ctx* c, float* ms) {
 
 extern "C" int stz_flush_l2(stz_ctx* c) {
   if (!c) return STZ_ERR_INVALID;
-  if (!c->l2buf) return STZ_ERR_NOMEM;
+  if (!c->l2buf) {
+    // a buffer larger than the 126 MB L2, allocated on first use
+    c->l2flush_bytes = (size_t)256 << 20;
+    if (cudaMalloc(&c->l2buf, c->l2flush_bytes) != cudaSuccess) {
+      c->l2buf = nullptr;
+      c->l2flush_bytes = 0;
+      set_error("L2 flush buffer allocation failed");
+      return STZ_ERR_NOMEM;
+    }
+  }
   launch_l2_flush(c->l2buf, c->l2flush_bytes, c->stream);
   c->launches += 1;
   return STZ_OK;
@@ -1007,5 +1022,168 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
   c->launches += 2 * steps;
   *ms_avg = n ? tot / n : 0;
   if (launches) *launches = n;
+  return STZ_OK;
+}
+
+// ============================================================= batches
+struct stz_batch {
+  std::vector<stz_ctx*> reps;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  stz::BatchDesc* d_desc = nullptr;
+  int* d_blk_rep = nullptr;
+  int* d_rep_first = nullptr;
+  stz::BatchStatus* d_status = nullptr;
+  std::vector<stz::BatchStatus> h_status;
+  int total_blocks = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_rounds = 0;
+  int64_t launches = 0;
+  int64_t min_log_cap = 0;
+};
+
+extern "C" void stz_batch_destroy(stz_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (stz_ctx* c : b->reps) stz_destroy(c);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_desc);
+  cudaFree(b->d_blk_rep);
+  cudaFree(b->d_rep_first);
+  cudaFree(b->d_status);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_batch** out) {
+  if (!params || count < 1 || !out) return STZ_ERR_INVALID;
+  *out = nullptr;
+  stz_batch* b = new stz_batch();
+  b->device = params[0].device;
+  for (int i = 0; i < count; i++) {
+    stz_params p = params[i];
+    if (p.model != STZ_MODEL_GLOBAL3D || p.precision != STZ_PREC_MIXED || p.device != b->device) {
+      set_error("batch replica %d: batches hold mixed-form 3D replicas on one device", i);
+      stz_batch_destroy(b);
+      return STZ_ERR_UNSUPPORTED;
+    }
+    if (p.log_capacity <= 0) p.log_capacity = 1 << 15;
+    stz_ctx* c = nullptr;
+    // batches favour few blocks per replica: the most sites per thread
+    const int st = stz::create_ctx(&p, &c, kMaxPerMixed);
+    if (st) {
+      stz_batch_destroy(b);
+      return st;
+    }
+    c->use_graph = 0;
+    b->reps.push_back(c);
+  }
+  cudaSetDevice(b->device);
+  cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  std::vector<stz::BatchDesc> desc(count);
+  std::vector<int> blk_rep, first(count);
+  for (int i = 0; i < count; i++) {
+    desc[i].kp = b->reps[i]->kp;
+    desc[i].f = b->reps[i]->f;
+    first[i] = (int)blk_rep.size();
+    for (int k = 0; k < b->reps[i]->kp.nblk; k++) blk_rep.push_back(i);
+    b->min_log_cap = i == 0 ? b->reps[i]->kp.log_cap : std::min<int64_t>(b->min_log_cap, b->reps[i]->kp.log_cap);
+  }
+  b->total_blocks = (int)blk_rep.size();
+  int st = STZ_OK;
+  if ((st = dalloc(&b->d_desc, (size_t)count)) || (st = dalloc(&b->d_blk_rep, blk_rep.size())) ||
+      (st = dalloc(&b->d_rep_first, (size_t)count)) || (st = dalloc(&b->d_status, (size_t)count))) {
+    stz_batch_destroy(b);
+    return st;
+  }
+  cudaMemcpy(b->d_desc, desc.data(), sizeof(stz::BatchDesc) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_blk_rep, blk_rep.data(), sizeof(int) * blk_rep.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_rep_first, first.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+  b->h_status.resize(count);
+  *out = b;
+  return STZ_OK;
+}
+
+extern "C" int stz_batch_size(stz_batch* b) { return b ? (int)b->reps.size() : 0; }
+
+extern "C" stz_ctx* stz_batch_replica(stz_batch* b, int32_t i) {
+  if (!b || i < 0 || i >= (int)b->reps.size()) return nullptr;
+  return b->reps[(size_t)i];
+}
+
+namespace {
+int batch_capture(stz_batch* b, int rounds) {
+  if (b->graph && b->graph_rounds == rounds) return STZ_OK;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  for (int r = 0; r < rounds; r++)
+    launch_mixed_batched(b->d_desc, b->d_blk_rep, b->d_rep_first, b->total_blocks, b->d_status,
+                         (int)b->reps.size(), b->stream);
+  CK(cudaStreamEndCapture(b->stream, &g));
+  CK(cudaGraphInstantiate(&b->graph, g, 0));
+  cudaGraphDestroy(g);
+  b->graph_rounds = rounds;
+  return STZ_OK;
+}
+}  // namespace
+
+extern "C" int stz_batch_run(stz_batch* b, int64_t events) {
+  if (!b || events < 1) return STZ_ERR_INVALID;
+  cudaSetDevice(b->device);
+  int st;
+  const int n = (int)b->reps.size();
+  for (stz_ctx* c : b->reps) {
+    if ((st = sync_ctl(c))) return st;
+    if (c->host_ctl.status) return c->host_ctl.status;
+    if ((st = set_targets(c, c->host_ctl.kstep + events, -1))) return st;
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  const int rounds = 16;
+  if ((st = batch_capture(b, rounds))) return st;
+  int64_t since_drain = 0;
+  for (;;) {
+    if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) {
+      set_error("batch graph launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return STZ_ERR_CUDA;
+    }
+    b->launches += 2 * rounds;
+    for (stz_ctx* c : b->reps) c->launches += 2 * rounds;
+    since_drain += rounds;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(b->h_status.data(), b->d_status, sizeof(stz::BatchStatus) * n, cudaMemcpyDeviceToHost,
+                       b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    bool active = false;
+    const bool drain_all = since_drain * 2 >= b->min_log_cap;
+    for (int i = 0; i < n; i++) {
+      stz_ctx* c = b->reps[(size_t)i];
+      const stz::BatchStatus& s = b->h_status[(size_t)i];
+      if (s.status) {
+        set_error("batch replica %d: device status %d", i, s.status);
+        return s.status;
+      }
+      if (!s.halt) {
+        active = true;
+        if (drain_all) {
+          if ((st = sync_ctl(c)) || (st = drain_log(c))) return st;
+        }
+        continue;
+      }
+      if ((st = sync_ctl(c))) return st;
+      if ((st = drain_log(c))) return st;
+      if (s.stopped || s.halt_reason == stz::kHaltTarget || s.halt_reason == stz::kHaltStop) continue;
+      int done = 0;
+      if ((st = mixed_service(c, &done))) return st;
+      if ((st = drain_log(c))) return st;
+      if (!done) active = true;
+    }
+    if (drain_all) since_drain = 0;
+    if (!active) break;
+  }
+  for (stz_ctx* c : b->reps) {
+    if ((st = sync_ctl(c)) || (st = drain_log(c))) return st;
+  }
   return STZ_OK;
 }

@@ -555,15 +555,39 @@ int upload_twiddles(int n, int count, double2** d64, float2** d32) {
   return STZ_OK;
 }
 
+// The dynamic shared-memory limit is a property of each kernel, shared by
+// every plan in the process: raise it once to the device's opt-in maximum
+// (requests below it cost nothing) instead of per plan.
+template <typename K>
+void raise_smem_limit(K kernel, int optin) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) { (void)cudaGetLastError(); return; }
+  int bytes = optin - (int)fa.sharedSizeBytes;
+  // a refusal here is not sticky; clear it so that it is not reported as a
+  // launch failure later (a launch that needs more then fails on its own)
+  if (bytes > 0 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+    (void)cudaGetLastError();
+}
+
+template <typename T>
+void set_smem_attrs_max(int optin) {
+  raise_smem_limit(k_r2c_x<T>, optin);
+  raise_smem_limit(k_c2c_axis<T, -1>, optin);
+  raise_smem_limit(k_c2c_axis<T, +1>, optin);
+  raise_smem_limit(k_green<T>, optin);
+  raise_smem_limit(k_c2r_x<T, kOutSig64>, optin);
+  raise_smem_limit(k_c2r_x<T, kOutSig32>, optin);
+  raise_smem_limit(k_c2r_x<T, kOutDev32>, optin);
+}
+
 template <typename T>
 void set_smem_attrs(size_t sx, size_t sy, size_t sg, size_t sc) {
-  cudaFuncSetAttribute(k_r2c_x<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
-  cudaFuncSetAttribute(k_c2c_axis<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy);
-  cudaFuncSetAttribute(k_c2c_axis<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy);
-  cudaFuncSetAttribute(k_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sg);
-  cudaFuncSetAttribute(k_c2r_x<T, kOutSig64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
-  cudaFuncSetAttribute(k_c2r_x<T, kOutSig32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
-  cudaFuncSetAttribute(k_c2r_x<T, kOutDev32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc);
+  (void)sx; (void)sy; (void)sg; (void)sc;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || optin <= 0)
+    optin = 227 * 1024;
+  set_smem_attrs_max<T>(optin);
 }
 
 template <typename T>
@@ -766,8 +790,6 @@ int fft_filter_gaussian(const FFTPlan& p, double* field, double corr_len, void* 
   const int ntile0 = (int)((inner0 + p.L_y - 1) / p.L_y);
   size_t s0 = 2 * (size_t)p.L_y * (p.n0 + 1) * sizeof(V);
   if (p.n0 > 1) {
-    cudaFuncSetAttribute(k_c2c_axis<double, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s0, p.smem_y));
-    cudaFuncSetAttribute(k_c2c_axis<double, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s0, p.smem_y));
     k_c2c_axis<double, -1><<<ntile0, TH, s0, st>>>(sp, p.n0, inner0, inner0, 0, ntile0, p.Nk, p.L_y, p.s0, p.tw_0,
                                                    nullptr);
   }

@@ -1045,13 +1045,13 @@ __device__ __forceinline__ int fold(int d, int n, int* flip) {
   return d;
 }
 
+// Body of the grid-wide mixed-form kernel for block b of one replica (kp may
+// live in kernel parameters or, for batches, in shared memory).
 template <int UPDATE_ONLY>
-__global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
+__device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b) {
   Ctl* ctl = f.ctl;
-  pdl_wait();
   if (ctl->halt && !UPDATE_ONLY) return;
-  if (!UPDATE_ONLY && blockIdx.x == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
-  const int b = blockIdx.x;
+  if (!UPDATE_ONLY && b == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
   const long long N = kp.N;
   const long long s0 = (long long)b * kp.bsites;
   const long long s1 = min(s0 + (long long)kp.bsites, N);
@@ -1164,6 +1164,12 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
   group_reduce(kp, f, b);
+}
+
+template <int UPDATE_ONLY>
+__global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
+  pdl_wait();
+  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x);
 }
 
 // ------------------------------------------------------- mixed-form tail
@@ -1367,10 +1373,8 @@ constexpr int kCtlScalarWords = (int)(offsetof(Ctl, rng) / 4);
 
 // One block after the grid of k_mixed: total rate, step kind, dice, search,
 // commit, log and the halt conditions of the mixed form.
-__global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int update_only) {
+__device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields& f, int update_only) {
   Ctl* const g = f.ctl;
-  pdl_wait();
-  pdl_release();
   if (update_only) {
     if (threadIdx.x < 6) g->U[threadIdx.x] = 0;
     if (threadIdx.x == 0) g->has_pend = 0;
@@ -1523,6 +1527,57 @@ __global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int upd
   }
 }
 
+__global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int update_only) {
+  pdl_wait();
+  pdl_release();
+  mixed_tail_body(kp, f, update_only);
+}
+
+// ------------------------------------------------------------ batches
+// Replicas of a batch: grid-wide kernel over every replica's blocks (block ->
+// replica map), then one tail block per replica. Each block copies its
+// replica's constants to shared memory.
+__device__ __forceinline__ void load_desc(const BatchDesc* d, int r, KParams* skp, Fields* sf) {
+  const uint32_t* a = reinterpret_cast<const uint32_t*>(&d[r]);
+  uint32_t* k = reinterpret_cast<uint32_t*>(skp);
+  for (int i = threadIdx.x; i < (int)(sizeof(KParams) / 4); i += blockDim.x) k[i] = a[i];
+  const uint32_t* a2 = reinterpret_cast<const uint32_t*>(&d[r].f);
+  uint32_t* k2 = reinterpret_cast<uint32_t*>(sf);
+  for (int i = threadIdx.x; i < (int)(sizeof(Fields) / 4); i += blockDim.x) k2[i] = a2[i];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __restrict__ d,
+                                                          const int* __restrict__ blk_rep,
+                                                          const int* __restrict__ rep_first) {
+  __shared__ KParams skp;
+  __shared__ Fields sf;
+  pdl_wait();
+  const int r = blk_rep[blockIdx.x];
+  load_desc(d, r, &skp, &sf);
+  mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r]);
+}
+
+__global__ void __launch_bounds__(TH) k_mixed_tail_batched(const BatchDesc* __restrict__ d,
+                                                           BatchStatus* __restrict__ st) {
+  __shared__ KParams skp;
+  __shared__ Fields sf;
+  pdl_wait();
+  pdl_release();
+  const int r = blockIdx.x;
+  load_desc(d, r, &skp, &sf);
+  mixed_tail_body(skp, sf, 0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const Ctl* c = sf.ctl;
+    st[r].halt = c->halt;
+    st[r].halt_reason = c->halt_reason;
+    st[r].stopped = c->stopped;
+    st[r].status = c->status;
+    st[r].kstep = c->kstep;
+  }
+}
+
 // After a full FP64 re-solve into sdev (mixed form).
 __global__ void k_mixed_after_resolve(KParams kp, Fields f, int kind) {
   Ctl* ctl = f.ctl;
@@ -1630,6 +1685,12 @@ void launch_pdl(void (*kern)(A...), int grid, cudaStream_t st, A... args) {
   cudaLaunchKernelEx(&cfg, kern, args...);
 }
 }  // namespace
+
+void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
+                          BatchStatus* status, int nrep, cudaStream_t st) {
+  launch_pdl(k_mixed_batched, total_blocks, st, d, blk_rep, rep_first);
+  launch_pdl(k_mixed_tail_batched, nrep, st, d, status);
+}
 
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed<1><<<kp.nblk, TH, 0, st>>>(kp, f);

@@ -17,6 +17,10 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
 // Mixed form: incremental stress update + rates + selection/commit.
 // update_only: apply the pending transformation and uniform change, nothing else.
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
+// One round of a batch: every replica's update/rate blocks in one grid, then
+// one selection/commit block per replica.
+void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
+                          BatchStatus* status, int nrep, cudaStream_t st);
 // Resident blocks per SM of the mixed-form kernel (occupancy query).
 int mixed_blocks_per_sm();
 // The two halves of launch_mixed: the grid-wide update/rate kernel and the

@@ -136,6 +136,19 @@ struct KParams {
   int c2r_blocks;                  // blocks of the FFT's C2R pass (msum row length)
 };
 
+// One replica of a batch as the batched kernels see it.
+struct BatchDesc {
+  KParams kp;
+  Fields f;
+};
+
+// Per-replica summary written by the batched selection kernel.
+struct BatchStatus {
+  int halt, halt_reason, stopped, status;
+  long long kstep;
+  long long pad;
+};
+
 }  // namespace stz
 
 struct stz_ctx {

@@ -1,0 +1,49 @@
+"""Batches of independent replicas (uneven grids, temperatures, strain rates
+and seeds) advanced together: each replica's trajectory must be exactly the
+one it follows alone, and the stress error bar of the mixed form holds."""
+import numpy as np
+import pytest
+
+from metallic_glasses_gb300 import api, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def _replicas():
+    ps = configs.replicas(count=4, sizes=(16, 24, 32))
+    for p in ps:
+        p.resolve_period = 100
+    return ps
+
+
+def test_batch_matches_replicas_run_alone(engine_lib):
+    ps = _replicas()
+    batch = api.Batch(ps)
+    batch.run(60)
+    for i, p in enumerate(ps):
+        alone = api.Batch([p])
+        alone.run(60)
+        a = batch.replicas[i].events()
+        b = alone.replicas[0].events()
+        assert len(a) == len(b) > 0
+        for k in ("step", "kind", "site", "mode"):
+            assert np.array_equal(a[k], b[k]), (i, k)
+        assert np.array_equal(a["time"], b["time"])
+        sa, sb = batch.replicas[i].scalars(), alone.replicas[0].scalars()
+        assert sa["kstep"] == sb["kstep"]
+        assert sa["eps_avg"] == sb["eps_avg"]
+        alone.close()
+    batch.close()
+
+
+def test_batch_replicas_advance_and_stay_accurate(engine_lib):
+    ps = _replicas()
+    batch = api.Batch(ps)
+    batch.run(250)
+    for r in batch.replicas:
+        sc = r.scalars()
+        assert sc["status"] == 0
+        assert sc["kstep"] == 250 or sc["stopped"]
+        if sc["n_resolves"]:
+            assert sc["stress_err_rms_worst"] < 1e-5
+    batch.close()
