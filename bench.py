@@ -148,6 +148,8 @@ def main():
     ap.add_argument("--events-per-step", type=int, default=1000)
     ap.add_argument("--grid", type=int, default=GRID)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-replicas", type=int, default=256)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -274,6 +276,15 @@ def main():
             "stress_err": stress_err,
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
             "wall_s": t_wall}
+    if not args.no_batch:
+        # independent replicas of uneven sizes advanced together vs one at a time
+        from metallic_glasses_gb300 import timing
+        bt = timing.batch(args.batch_replicas, events=128, alone=16)
+        bt["workload"] = ("%d replicas, grids uniform over 32^3/48^3/64^3/96^3, T uniform in [325, 585] K, "
+                          "strain rate log-uniform in [1e-5, 1e-2] /s, seeds 0..%d; 128 thermal events each; "
+                          "one at a time = the first 16 replicas, each alone through stz_run"
+                          % (args.batch_replicas, args.batch_replicas - 1))
+        line["batched"] = bt
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
     print(json.dumps(line), flush=True)

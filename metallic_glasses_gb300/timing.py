@@ -1,0 +1,87 @@
+"""Kernel and throughput timing of the STZ step on one GPU.
+
+  python -m metallic_glasses_gb300.timing kernel --grid 128 --which 0 --steps 8
+  python -m metallic_glasses_gb300.timing batch --replicas 256 --events 32
+
+`kernel` times one per-event kernel of the mixed form launch by launch with
+CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
+only, 2: a whole event including selection). `batch` advances independent
+replicas (grid sizes 32^3..96^3, temperatures and strain rates drawn from the
+seed) together in one batch, then the first few of them one at a time, and
+prints both aggregate rates (one at a time = each replica in its own
+context through stz_run, the single-run path). Both are the commands the ncu summaries are
+taken on.
+"""
+import argparse
+import json
+import time
+
+from . import api, configs
+
+
+def kernel(grid, which, steps, resolve_period=0):
+    eng = api.Engine(configs.mixed128(n=grid, resolve_period=resolve_period))
+    ms, n = eng.kernel_time(steps=steps, which=which)
+    eng.close()
+    return {"grid": grid, "which": which, "launch_ms": ms, "launches": n}
+
+
+def batch(replicas, events, alone=16, seed0=0):
+    """Aggregate replica-events/s batched vs the same replicas one at a time.
+
+    Every replica advances `events` thermal events in both arms (the warm-up
+    of 4 events and the creation are outside the timed regions; a batch run
+    returns when every replica has reached its target)."""
+    ps = configs.replicas(count=replicas, seed_base=seed0)
+    t0 = time.perf_counter()
+    b = api.Batch(ps)
+    create_s = time.perf_counter() - t0
+    b.run(4)
+    k0 = sum(r.scalars()["kstep"] for r in b.replicas)
+    t0 = time.perf_counter()
+    b.run(events)
+    dt = time.perf_counter() - t0
+    done = sum(r.scalars()["kstep"] for r in b.replicas) - k0
+    sites = sum(p.n[0] * p.n[1] * p.n[2] for p in ps)
+    b.close()
+    n1 = min(alone, replicas)
+    t1 = 0.0
+    done1 = 0
+    for p in ps[:n1]:
+        a = api.Engine(p)
+        a.run(max_events=4)
+        k = a.scalars()["kstep"]
+        a.sync()
+        t0 = time.perf_counter()
+        a.run(max_events=events)
+        a.sync()
+        t1 += time.perf_counter() - t0
+        done1 += a.scalars()["kstep"] - k
+        a.close()
+    return {"replicas": replicas, "sites": sites, "events_per_replica": events, "create_s": create_s,
+            "batched_events_per_s": done / dt, "alone_events_per_s": done1 / t1 if t1 > 0 else None,
+            "alone_sample": n1}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m metallic_glasses_gb300.timing")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    k = sub.add_parser("kernel")
+    k.add_argument("--grid", type=int, default=128)
+    k.add_argument("--which", type=int, default=0)
+    k.add_argument("--steps", type=int, default=8)
+    b = sub.add_parser("batch")
+    b.add_argument("--replicas", type=int, default=256)
+    b.add_argument("--events", type=int, default=32)
+    b.add_argument("--alone", type=int, default=16)
+    a = ap.parse_args(argv)
+    if a.cmd == "kernel":
+        out = kernel(a.grid, a.which, a.steps)
+    else:
+        out = batch(a.replicas, a.events, a.alone)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
