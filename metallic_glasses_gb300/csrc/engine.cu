@@ -368,7 +368,7 @@ int capture_plain_graph(stz_ctx* c, int steps) {
   for (int i = 0; i < steps; i++) {
     if (c->kp.nc == 6 && c->f.sdev) {
       launch_mixed(c->kp, c->f, 0, c->stream);
-      c->launches += 2;
+      c->launches += kMixedLaunches;
     } else {
       enqueue_plain_step(c);
     }
@@ -459,12 +459,12 @@ using namespace stz;
 extern "C" const char* stz_last_error(void) { return g_err; }
 
 namespace stz {
-int create_ctx(const stz_params* pin, stz_ctx** out, int per_override);
+int create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block);
 }
 
 extern "C" int stz_create(const stz_params* pin, stz_ctx** out) { return stz::create_ctx(pin, out, 0); }
 
-int stz::create_ctx(const stz_params* pin, stz_ctx** out, int per_override) {
+int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   if (!pin || !out) return STZ_ERR_INVALID;
   *out = nullptr;
   const stz_params& p = *pin;
@@ -479,6 +479,11 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int per_override) {
   if (!ref2d && p.softening) { set_error("softening is implemented for the reference 2D model only"); return STZ_ERR_UNSUPPORTED; }
   const bool mixed = p.precision == STZ_PREC_MIXED;
   if (mixed && ref2d) { set_error("the mixed form is implemented for the 3D model"); return STZ_ERR_UNSUPPORTED; }
+  if (mixed && (p.n[2] % 4 || p.n[2] > 512)) {
+    // lines are staged by 16-byte bulk copies into shared memory, two per warp
+    set_error("the mixed form needs the fastest extent a multiple of 4, at most 512 (got %d)", p.n[2]);
+    return STZ_ERR_UNSUPPORTED;
+  }
   int solver = p.solver;
   if (solver == STZ_SOLVER_AUTO) solver = mixed ? STZ_SOLVER_KERNEL : STZ_SOLVER_FFT;
   if (mixed && solver != STZ_SOLVER_KERNEL) { set_error("the mixed form uses the incremental (kernel) solver"); return STZ_ERR_UNSUPPORTED; }
@@ -504,19 +509,23 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int per_override) {
   kp.N = (long long)kp.n0 * kp.n1 * kp.n2;
   kp.Nk = (long long)kp.n0 * kp.n1 * kp.nh;
   if (mixed) {
-    // one wave of resident blocks, each owning a contiguous run of sites
-    // (at most kMaxPerMixed per thread; larger grids take several waves)
+    // Units of mirror-grouped lines (one d0, two d1); one wave of resident
+    // blocks walks them, or, with units_per_block > 0 (batch members, where
+    // the other replicas fill the GPU), that many units per block.
+    const int kt0 = kp.n0 / 2 + 1, kt1 = kp.n1 / 2 + 1;
+    kp.mx_c1 = (kt1 + 1) / 2;
+    kp.mx_units = kt0 * kp.mx_c1;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device);
-    const long long wave = (long long)std::max(sms, 1) * mixed_blocks_per_sm();
-    long long per = (kp.N + wave * kRateThreads - 1) / (wave * kRateThreads);
-    if (per_override > 0) per = per_override;
-    per = std::max(1LL, std::min(per, (long long)kMaxPerMixed));
-    kp.bsites = (int)(kRateThreads * per);
+    const long long wave = (long long)std::max(sms, 1) * mixed_blocks_per_sm(kp.n2);
+    const long long nb = units_per_block > 0 ? (kp.mx_units + units_per_block - 1) / units_per_block
+                                             : std::min<long long>(kp.mx_units, wave);
+    kp.nblk = (int)std::max(1LL, nb);
+    kp.bsites = 0;
   } else {
     kp.bsites = kRateThreads * kSptFp64;
+    kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
   }
-  kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
   kp.ngroups = (kp.nblk + kGroup - 1) / kGroup;
   kp.adv_q2 = kRateThreads / kp.n2;
   kp.adv_r2 = kRateThreads % kp.n2;
@@ -555,9 +564,14 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int per_override) {
   if ((st = dalloc(&f.eps0, (size_t)nc * N))) return fail(st);
   if ((st = dalloc(&f.prev_deps, (size_t)nc * N))) return fail(st);
   if ((st = dalloc(&f.amark, (size_t)N))) return fail(st);
-  if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
-  if ((st = dalloc(&f.gsum, (size_t)STZ_MODES * kp.ngroups))) return fail(st);
-  if ((st = dalloc(&f.gticket, (size_t)kp.ngroups))) return fail(st);
+  if (mixed) {
+    if ((st = dalloc(&f.lsum, (size_t)STZ_MODES * kp.n0 * kp.n1))) return fail(st);
+    if ((st = dalloc(&f.psum, (size_t)STZ_MODES * kp.n0))) return fail(st);
+  } else {
+    if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
+    if ((st = dalloc(&f.gsum, (size_t)STZ_MODES * kp.ngroups))) return fail(st);
+    if ((st = dalloc(&f.gticket, (size_t)kp.ngroups))) return fail(st);
+  }
   if ((st = dalloc(&f.log, (size_t)kp.log_cap))) return fail(st);
   if ((st = dalloc(&c->err_dev, 4))) return fail(st);
   {
@@ -641,8 +655,8 @@ extern "C" void stz_destroy(stz_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
-                  f.tlast, f.amark, f.part, f.gsum, f.gticket, f.spec, f.ktab, f.log, f.ctl, f.scratch, f.msum,
-                  c->err_dev, c->l2buf};
+                  f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.psum, f.spec, f.ktab, f.log,
+                  f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fft) {
@@ -680,7 +694,7 @@ extern "C" int stz_run(stz_ctx* c, int64_t max_steps, int64_t max_events) {
       c->launches += c->graph_launches;
     } else {
       for (int i = 0; i < batch; i++) {
-        if (mixed) { launch_mixed(c->kp, c->f, 0, c->stream); c->launches += 2; }
+        if (mixed) { launch_mixed(c->kp, c->f, 0, c->stream); c->launches += kMixedLaunches; }
         else enqueue_plain_step(c);
       }
     }
@@ -1019,7 +1033,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
     tot += ms;
     n++;
   }
-  c->launches += 2 * steps;
+  c->launches += kMixedLaunches * steps;
   *ms_avg = n ? tot / n : 0;
   if (launches) *launches = n;
   return STZ_OK;
@@ -1036,6 +1050,8 @@ struct stz_batch {
   stz::BatchStatus* d_status = nullptr;
   std::vector<stz::BatchStatus> h_status;
   int total_blocks = 0;
+  int max_n0 = 1;  // largest plane count (grid x of the plane-sum kernel)
+  int max_n2 = 4;  // longest line (shared memory of the batched main kernel)
   cudaGraphExec_t graph = nullptr;
   int graph_rounds = 0;
   int64_t launches = 0;
@@ -1070,8 +1086,8 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
     }
     if (p.log_capacity <= 0) p.log_capacity = 1 << 15;
     stz_ctx* c = nullptr;
-    // batches favour few blocks per replica: the most sites per thread
-    const int st = stz::create_ctx(&p, &c, kMaxPerMixed);
+    // batches: four line units per block
+    const int st = stz::create_ctx(&p, &c, 4);
     if (st) {
       stz_batch_destroy(b);
       return st;
@@ -1091,6 +1107,12 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
     b->min_log_cap = i == 0 ? b->reps[i]->kp.log_cap : std::min<int64_t>(b->min_log_cap, b->reps[i]->kp.log_cap);
   }
   b->total_blocks = (int)blk_rep.size();
+  b->max_n0 = 1;
+  b->max_n2 = 4;
+  for (auto* c : b->reps) {
+    b->max_n0 = std::max(b->max_n0, c->kp.n0);
+    b->max_n2 = std::max(b->max_n2, c->kp.n2);
+  }
   int st = STZ_OK;
   if ((st = dalloc(&b->d_desc, (size_t)count)) || (st = dalloc(&b->d_blk_rep, blk_rep.size())) ||
       (st = dalloc(&b->d_rep_first, (size_t)count)) || (st = dalloc(&b->d_status, (size_t)count))) {
@@ -1120,7 +1142,7 @@ int batch_capture(stz_batch* b, int rounds) {
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < rounds; r++)
     launch_mixed_batched(b->d_desc, b->d_blk_rep, b->d_rep_first, b->total_blocks, b->d_status,
-                         (int)b->reps.size(), b->stream);
+                         (int)b->reps.size(), b->max_n0, b->max_n2, b->stream);
   CK(cudaStreamEndCapture(b->stream, &g));
   CK(cudaGraphInstantiate(&b->graph, g, 0));
   cudaGraphDestroy(g);
@@ -1148,8 +1170,8 @@ extern "C" int stz_batch_run(stz_batch* b, int64_t events) {
       set_error("batch graph launch failed: %s", cudaGetErrorString(cudaGetLastError()));
       return STZ_ERR_CUDA;
     }
-    b->launches += 2 * rounds;
-    for (stz_ctx* c : b->reps) c->launches += 2 * rounds;
+    b->launches += kMixedLaunches * rounds;
+    for (stz_ctx* c : b->reps) c->launches += kMixedLaunches * rounds;
     since_drain += rounds;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(b->h_status.data(), b->d_status, sizeof(stz::BatchStatus) * n, cudaMemcpyDeviceToHost,

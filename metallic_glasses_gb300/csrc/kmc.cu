@@ -246,6 +246,23 @@ __device__ __forceinline__ void site_coords(const KParams& kp, long long s, int*
   *i0 = (int)q;
 }
 
+// The mixed-form main pass's header from U, has_pend, pend_site and
+// pend_mode (one thread; FP64 here, FP32 for the pass).
+__device__ void set_mixed_head(const KParams& kp, Ctl* c) {
+  MixHead& h = c->head;
+  const double* U = c->U;
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
+  h.Ud[0] = (float)((U[0] - U[1]) * r2);
+  h.Ud[1] = (float)((2.0 * U[2] - U[0] - U[1]) * r6);
+  h.Ud[2] = (float)(q2 * U[3]);
+  h.Ud[3] = (float)(q2 * U[4]);
+  h.Ud[4] = (float)(q2 * U[5]);
+  h.has_pend = c->has_pend;
+  h.pend_mode = c->has_pend ? c->pend_mode : 0;
+  if (c->has_pend) site_coords(kp, c->pend_site, &h.p0, &h.p1, &h.p2);
+  else h.p0 = h.p1 = h.p2 = 0;
+}
+
 // Direction modifier of the softening schemes (init.c:590-642)
 __device__ __forceinline__ double dire_modifier(int scheme, double dot, double n1, double n2) {
   double DM;
@@ -300,8 +317,6 @@ __device__ __forceinline__ void g3_load(const KParams& kp, const Fields& f, cons
   for (int c = 0; c < 6; c++) sg[c] = f.sig[c * kp.N + s] + u[c];
 }
 
-// 2^x with the hardware approximation (PTX ex2.approx.ftz.f32: one MUFU
-// operation, relative error below 2^-22; results under 2^-126 flush to 0).
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -315,6 +330,8 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// 2^x with the hardware approximation (PTX ex2.approx.ftz.f32: one MUFU
+// operation, relative error below 2^-22; results under 2^-126 flush to 0).
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -371,26 +388,6 @@ __device__ void block_mode_sums(const double* acc, double* part, int nblk, int b
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
     if (lane == 0) red[w][m] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < STZ_MODES) {
-    double s = 0;
-    for (int k = 0; k < TH / 32; k++) s += red[k][threadIdx.x];
-    part[(long long)threadIdx.x * nblk + b] = s;
-  }
-}
-
-// Mixed form: the per-thread FP32 sums are reduced within each warp in FP32
-// (32 values), then across the warps of the block in FP64.
-__device__ void block_mode_sums_f32(const float* acc, double* part, int nblk, int b) {
-  __shared__ double red[TH / 32][STZ_MODES];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int m = 0; m < STZ_MODES; m++) {
-    float v = acc[m];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
-    if (lane == 0) red[w][m] = (double)v;
   }
   __syncthreads();
   if (threadIdx.x < STZ_MODES) {
@@ -607,7 +604,7 @@ __device__ void search_event(const KParams& kp, const Fields& f, const double* u
   const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
   const long long per = (s1 - s0 + TH - 1) / TH;
   const long long a0 = s0 + t * per;
-  constexpr int kMaxPer = MODEL == 2 ? kMaxPerMixed : kSptFp64;  // sites per thread
+  constexpr int kMaxPer = kSptFp64;  // sites per thread
   double rr[kMaxPer];
   double loc = 0;
 #pragma unroll
@@ -689,33 +686,8 @@ __device__ __forceinline__ void ctl_copy(Ctl* dst, const Ctl* src) {
   for (int i = threadIdx.x; i < (int)(sizeof(Ctl) / 4); i += blockDim.x) d[i] = a[i];
 }
 
-// Incremental "solve" of a thermal event in the mixed form, then the
-// loading of evolution.c:262-317 (thread 0, on the shared control block).
-__device__ void mixed_commit(const KParams& kp, const Fields& f, Ctl* c, long long s, int m) {
-  const long long N = kp.N;
-  for (int k = 0; k < 6; k++) {
-    f.prev_deps[k * N + s] = kp.modes[m][k];
-    f.eps0[k * N + s] += kp.modes[m][k];
-    c->eps0_sum[k] += kp.modes[m][k];
-  }
-  double dA[6], CdA[6];
-  for (int k = 0; k < 6; k++) dA[k] = c->eps_avg[k] - c->eps_avg_applied[k];
-  apply_C(kp, dA, CdA);
-  for (int k = 0; k < 6; k++) {
-    c->U[k] = CdA[k] - c->u[k];
-    c->eps_avg_applied[k] = c->eps_avg[k];
-    c->u[k] = 0;
-  }
-  solved_mean_stress(kp, c, c->eps_avg_applied, c->stress);
-  load_after_event(kp, c, c->t_kmc);
-  for (int k = 0; k < 6; k++) c->U[k] += c->u[k];
-  c->has_pend = 1;
-  c->pend_site = s;
-  c->pend_mode = m;
-}
-
 // Last block of a rate kernel: total rate, step kind, dice, event search and
-// commit. MODEL 0 REF2D FP64, 1 GLOBAL3D FP64, 2 mixed form.
+// commit. MODEL 0 REF2D FP64, 1 GLOBAL3D FP64.
 template <int MODEL>
 __device__ void finish_step(const KParams& kp, const Fields& f) {
   __shared__ Ctl sc;
@@ -743,12 +715,8 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
   if (threadIdx.x == 0) {
     c->ticket = 0;
     c->step++;
-    if (MODEL == 2) {
-      c->has_pend = 0;
-      for (int k = 0; k < 6; k++) c->U[k] = 0;
-    }
     const double Rraw = sh_inc[TH - 1];
-    const double R = MODEL == 2 ? Rraw * kp.rate_scale : Rraw;
+    const double R = Rraw;
     sh_R = Rraw;
     for (int k = 0; k < 6; k++) sh_u[k] = c->u[k];
     sh_tot = c->totime;
@@ -756,7 +724,6 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
     int kind;
     if (c->neg_count > 0) {
       kind = kAthermal;
-      if (MODEL == 2) { c->halt = 1; c->halt_reason = kHaltAthermal; }
     } else if (!(R > 0) || !isfinite(R)) {
       kind = kNone;
       c->status = STZ_ERR_NAN;
@@ -793,7 +760,7 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
   }
   const unsigned long long t_search = gtimer();
   if (threadIdx.x == 0) {
-    const double Rtrue = MODEL == 2 ? sh_R * kp.rate_scale : sh_R;
+    const double Rtrue = sh_R;
     if (kind == kThermal) {
       const long long s = sh_site;
       const int m = sh_mode;
@@ -808,53 +775,18 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
         c->sel_site = s;
         c->sel_mode = m;
         c->sel_q = q;
-        if (MODEL == 2) {
-          mixed_commit(kp, f, c, s, m);
-          c->totime += c->t_kmc;
-          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime, c->t_kmc, q, Rtrue);
-          if (kp.resolve_period > 0 && c->kstep >= c->next_resolve) {
-            c->halt = 1;
-            c->halt_reason = kHaltResolve;
-          }
-        } else {
-          transform<MODEL>(kp, f, c, m, s, &c->rng);
-          c->solve_req = 1;
-          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue);
-        }
+        transform<MODEL>(kp, f, c, m, s, &c->rng);
+        c->solve_req = 1;
+        log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue);
       }
     } else if (kind == kElastic) {
       c->estep++;
       c->totime += kp.dt;
-      double u0[6];
-      for (int k = 0; k < 6; k++) u0[k] = c->u[k];
       elastic_step(kp, c);
-      if (MODEL == 2)
-        for (int k = 0; k < 6; k++) c->U[k] = c->u[k] - u0[k];
-      else
-        c->solve_req = 0;
+      c->solve_req = 0;
       log_event(kp, f, c, STZ_EV_ELASTIC, -1, -1, c->totime, kp.dt, 0.0, Rtrue);
-    } else if (kind == kAthermal && MODEL != 2) {
+    } else if (kind == kAthermal) {
       c->solve_req = 0;  // the athermal commit requests the solve
-    }
-    if (MODEL == 2) {
-      const unsigned long long t_end = gtimer();
-      c->prof_main_ns += t_tail - c->prof_t0;
-      c->prof_tail_ns += t_end - t_tail;
-      c->prof_part_ns[0] += t_sums - t_tail;
-      c->prof_part_ns[1] += t_dec - t_sums;
-      c->prof_part_ns[2] += t_search - t_dec;
-      c->prof_part_ns[3] += t_end - t_search;
-      c->prof_n++;
-    }
-    if (MODEL == 2 && (kind == kThermal || kind == kElastic) && c->step_kind != kNone) {
-      if (print_check(kp, c)) {
-        c->print_done = 1;
-        c->halt = 1;
-        c->halt_reason = kHaltPrint;
-      } else {
-        if (!c->halt) stop_check(kp, c);
-        c->step_kind = kNone;
-      }
     }
   }
   __syncthreads();
@@ -1034,10 +966,6 @@ __global__ void k_post_b(KParams kp, Fields f) {
 }
 
 // ------------------------------------------------------------ mixed form
-struct TabLoad {
-  float k[15];
-};
-
 __device__ __forceinline__ int fold(int d, int n, int* flip) {
   if (d < 0) d += n;
   if (2 * d > n) { *flip = 1; return n - d; }
@@ -1045,131 +973,364 @@ __device__ __forceinline__ int fold(int d, int n, int* flip) {
   return d;
 }
 
-// Body of the grid-wide mixed-form kernel for block b of one replica (kp may
-// live in kernel parameters or, for batches, in shared memory).
-template <int UPDATE_ONLY>
-__device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b) {
-  Ctl* ctl = f.ctl;
-  if (ctl->halt && !UPDATE_ONLY) return;
-  if (!UPDATE_ONLY && b == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
-  const long long N = kp.N;
-  const long long s0 = (long long)b * kp.bsites;
-  const long long s1 = min(s0 + (long long)kp.bsites, N);
-  // pending transformation and uniform change
-  const int hp = ctl->has_pend;
-  int pm = 0, p0 = 0, p1 = 0, p2 = 0;
-  float de[5] = {0, 0, 0, 0, 0};
+// ---------------------------------------------------- mixed-form main pass
+// Work decomposition. A line of the grid is (i0, i1) with its n2 contiguous
+// sites; one warp owns one line, lane l its sites i2 = l, l + 32, ... Lines
+// are grouped by their folded distance (d0, d1) to the transformed site p:
+// the lines (p0 +- d0, p1 +- d1) read the same row (d0, d1, *) of the response
+// table, and each record of a row twice along a line, so a unit of up to eight
+// lines (one d0, d1 in {2c, 2c + 1}, both signs of each) fetches each record
+// of its two rows from L2 once and serves the other reads from L1. Unit
+// u = d0 * mx_c1 + c; warp w of the unit takes sign0 = w & 1, d1 = 2c + (w >> 1
+// & 1), sign1 = w >> 2, and idles where that line coincides with another one
+// (d = 0 or d = n/2) or d1 is past the table. Every line belongs to exactly
+// one (unit, warp).
+struct LineOf {
+  int i0, i1, valid;
+};
+
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__device__ __forceinline__ LineOf unit_line(const KParams& kp, int u, int w, int p0, int p1) {
+  const int d0 = u / kp.mx_c1, c = u - d0 * kp.mx_c1;
+  const int s0 = w & 1, s1 = w >> 2;
+  const int d1 = 2 * c + ((w >> 1) & 1);
+  LineOf L;
+  L.valid = d1 < kp.kt1 && (!s0 || (d0 != 0 && 2 * d0 != kp.n0)) && (!s1 || (d1 != 0 && 2 * d1 != kp.n1));
+  L.i0 = wrap1(s0 ? p0 - d0 : p0 + d0, kp.n0);
+  L.i1 = wrap1(s1 ? p1 - d1 : p1 + d1, kp.n1);
+  return L;
+}
+
+// Stress update of one site (sv holds its coordinates): the pending
+// transformation's response S K(|x - p|) S de (S the reflection signs, K the
+// folded table record at rec) plus the uniform change Ud; stores the new
+// coordinates and leaves them in sv. dl holds
+// de (5), then the sign of coordinate 2 (y z) and the z and y flips that,
+// times the site's x flip sx, give the signs of coordinates 3 (x z) and 4 (x y).
+__device__ __forceinline__ void mixed_update(const Fields& f, int N32, int s, int hp, const float4* rec, float sx,
+                                             const float* dl, const float* Ud, float* sv) {
   if (hp) {
-    pm = ctl->pend_mode;
-    site_coords(kp, ctl->pend_site, &p0, &p1, &p2);
-    for (int k = 0; k < 5; k++) de[k] = kp.mdev_raw[pm][k];
+    const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2), q3 = __ldg(rec + 3);
+    const float K[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                         q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+    const float g2 = dl[5], g3 = dl[6] * sx, g4 = dl[7] * sx;
+    const float e[5] = {dl[0], dl[1], dl[2] * g2, dl[3] * g3, dl[4] * g4};
+    // symmetric 5x5 from the packed upper triangle (row-major, a <= b)
+    const float y0 = K[0] * e[0] + K[1] * e[1] + K[2] * e[2] + K[3] * e[3] + K[4] * e[4];
+    const float y1 = K[1] * e[0] + K[5] * e[1] + K[6] * e[2] + K[7] * e[3] + K[8] * e[4];
+    const float y2 = K[2] * e[0] + K[6] * e[1] + K[9] * e[2] + K[10] * e[3] + K[11] * e[4];
+    const float y3 = K[3] * e[0] + K[7] * e[1] + K[10] * e[2] + K[12] * e[3] + K[13] * e[4];
+    const float y4 = K[4] * e[0] + K[8] * e[1] + K[11] * e[2] + K[13] * e[3] + K[14] * e[4];
+    // the small increments are added together first, so the field takes one
+    // rounding per event
+    sv[0] += y0 + Ud[0];
+    sv[1] += y1 + Ud[1];
+    sv[2] += __fmaf_rn(g2, y2, Ud[2]);
+    sv[3] += __fmaf_rn(g3, y3, Ud[3]);
+    sv[4] += __fmaf_rn(g4, y4, Ud[4]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; k++) sv[k] += Ud[k];
   }
-  float Ud[5];
-  {
-    double U6[6], ud[5];
-    for (int c = 0; c < 6; c++) U6[c] = ctl->U[c];
-    const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
-    ud[0] = (U6[0] - U6[1]) * r2;
-    ud[1] = (2.0 * U6[2] - U6[0] - U6[1]) * r6;
-    ud[2] = q2 * U6[3];
-    ud[3] = q2 * U6[4];
-    ud[4] = q2 * U6[5];
-    for (int k = 0; k < 5; k++) Ud[k] = (float)ud[k];
-  }
-  const int ts = kp.kt1 * kp.kt2;
-  float2 acc2[STZ_MODES / 2];
 #pragma unroll
-  for (int j = 0; j < STZ_MODES / 2; j++) acc2[j] = make_float2(0.f, 0.f);
-  const float thr_neg = kp.q_ref * kp.a_scale;
-  unsigned neg = 0;
-  // site coordinates, advanced incrementally by TH sites per iteration
-  const int N32 = (int)N;
-  int s = (int)s0 + (int)threadIdx.x;
-  int i0, i1, i2;
-  site_coords(kp, s, &i0, &i1, &i2);
-  for (; s < (int)s1; s += TH) {
-    float sv[5];
+  for (int k = 0; k < 5; k++) f.sdev[k * N32 + s] = sv[k];
+}
+
+// The 20 rates of two sites (b may be absent), packed two modes per FP32x2
+// FMA; each lane of a pair is the scalar chain of mx_x, so the search sees the
+// same bits. One load of each mode coefficient serves both sites.
+__device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const float* sb, float ab, bool hb,
+                                             const float2* md, float2* acc2) {
 #pragma unroll
-    for (int k = 0; k < 5; k++) sv[k] = f.sdev[k * N32 + s];
-    if (hp) {
-      int fx, fy, fz;
-      const int d0 = fold(i0 - p0, kp.n0, &fz);
-      const int d1 = fold(i1 - p1, kp.n1, &fy);
-      const int d2 = fold(i2 - p2, kp.n2, &fx);
-      const float sx = fx ? -1.f : 1.f, sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
-      const float sg[5] = {1.f, 1.f, sy * sz, sx * sz, sx * sy};
-      // one 64-byte record per octant point: the 15 packed entries + padding
-      const float4* tp = reinterpret_cast<const float4*>(f.ktab) + 4 * (d0 * ts + d1 * kp.kt2 + d2);
-      float K[16];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const float4 v = __ldg(tp + j);
-        K[4 * j] = v.x; K[4 * j + 1] = v.y; K[4 * j + 2] = v.z; K[4 * j + 3] = v.w;
-      }
-      float e[5];
-#pragma unroll
-      for (int k = 0; k < 5; k++) e[k] = sg[k] * de[k];
-      // symmetric 5x5 from the packed upper triangle (row-major, a <= b)
-      const float y0 = K[0] * e[0] + K[1] * e[1] + K[2] * e[2] + K[3] * e[3] + K[4] * e[4];
-      const float y1 = K[1] * e[0] + K[5] * e[1] + K[6] * e[2] + K[7] * e[3] + K[8] * e[4];
-      const float y2 = K[2] * e[0] + K[6] * e[1] + K[9] * e[2] + K[10] * e[3] + K[11] * e[4];
-      const float y3 = K[3] * e[0] + K[7] * e[1] + K[10] * e[2] + K[12] * e[3] + K[13] * e[4];
-      const float y4 = K[4] * e[0] + K[8] * e[1] + K[11] * e[2] + K[13] * e[3] + K[14] * e[4];
-      sv[0] += y0;
-      sv[1] += y1;
-      sv[2] += sg[2] * y2;
-      sv[3] += sg[3] * y3;
-      sv[4] += sg[4] * y4;
-    }
+  for (int j = 0; j < STZ_MODES / 2; j++) {
+    float2 xa = make_float2(aa, aa), xb = make_float2(ab, ab);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-      sv[k] += Ud[k];
-      f.sdev[k * N32 + s] = sv[k];
+      const float2 c = md[5 * j + k];
+      xa = __ffma2_rn(make_float2(sa[k], sa[k]), c, xa);
+      xb = __ffma2_rn(make_float2(sb[k], sb[k]), c, xb);
+    }
+    acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
+    if (hb) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xb.x), ex2_approx(xb.y)));
+  }
+}
+
+// Q < 0 for some mode needs |W|/2 > dF; |W| <= |s| |deps| bounds it, and only
+// sites past the bound evaluate the 20 exact tests.
+__device__ __forceinline__ unsigned mixed_neg(const KParams& kp, const float* sv, float a, float dFs, float thr_neg) {
+  const float n2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] + sv[3] * sv[3] + sv[4] * sv[4];
+  const float lim = dFs * kp.a_scale * kp.inv_mdev_norm;
+  unsigned neg = 0;
+  if (n2 * kp.bound_slack >= lim * lim || lim <= 0.f) {
+#pragma unroll 1
+    for (int m = 0; m < STZ_MODES; m++) neg |= mx_x(kp, sv, a, m) > thr_neg ? 1u : 0u;
+  }
+  return neg;
+}
+
+// ------------------------------------------ bulk-copy staging of a line
+// One lane of each warp copies the next line's five stress components and
+// barrier (contiguous runs of n2 floats) into the warp's other stage with
+// cp.async.bulk, tracked by that stage's mbarrier (expected bytes), while the
+// warp computes the current line from shared memory. The copies need 16-byte
+// aligned runs: n2 is a multiple of 4 for the mixed form.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait (each try_wait suspends for a hardware-chosen interval); false
+// after kMbarTries attempts.
+constexpr int kMbarTries = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (int it = 0; it < kMbarTries; it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Floats of one stage: 6 runs of n2 (stress, barrier); at least 32 x 20 so
+// the stage just consumed can hold the line-sum transpose.
+__host__ __device__ __forceinline__ int mix_stage_floats(int n2) {
+  const int a = 6 * n2, r = 32 * STZ_MODES;
+  return a > r ? a : r;
+}
+// Dynamic shared memory of a mixed-form main block: 8 warps x 2 stages.
+__host__ __device__ __forceinline__ size_t mix_smem_bytes(int n2) {
+  return (size_t)(TH / 32) * 2 * mix_stage_floats(n2) * sizeof(float);
+}
+
+template <int UPDATE_ONLY>
+__device__ __forceinline__ void issue_line(const KParams& kp, const Fields& f, int i0, int i1, float* stage,
+                                           unsigned long long* bar) {
+  const long long base = ((long long)i0 * kp.n1 + i1) * kp.n2;
+  const unsigned bytes = (unsigned)kp.n2 * 4u;
+  // the generic-proxy reads and writes of this stage are done (syncwarp by
+  // the caller); order them before the asynchronous writes
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(bar, (UPDATE_ONLY ? 5u : 6u) * bytes);
+#pragma unroll
+  for (int k = 0; k < 5; k++) bulk_g2s(stage + k * kp.n2, f.sdev + (long long)k * kp.N + base, bytes, bar);
+  if (!UPDATE_ONLY) bulk_g2s(stage + 5 * kp.n2, f.dF32 + base, bytes, bar);
+}
+
+// One line (i0, i1) by one warp from its staged inputs: update every site,
+// and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2.
+template <int UPDATE_ONLY>
+__device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, int N32, int hp, int i0, int i1,
+                                           int p0, int p1, int p2, const float* de, const float* Ud,
+                                           const float2* md, const float* stage, float2* acc2, unsigned& neg,
+                                           float thr_neg) {
+  const int lane = threadIdx.x & 31;
+  const int n2 = kp.n2;
+  int fz, fy;
+  const int d0 = fold(i0 - p0, kp.n0, &fz);
+  const int d1 = fold(i1 - p1, kp.n1, &fy);
+  const float4* row = reinterpret_cast<const float4*>(f.ktab) + 4LL * ((d0 * kp.kt1 + d1) * kp.kt2);
+  // per-line signs: coordinate 2 takes y z, 3 takes x z, 4 takes x y; the x
+  // flip varies along the line and is applied per site
+  const float sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
+  float dl[8];
+#pragma unroll
+  for (int k = 0; k < 5; k++) dl[k] = de[k];
+  dl[5] = sy * sz;
+  dl[6] = sz;
+  dl[7] = sy;
+  const int base = (i0 * kp.n1 + i1) * n2;
+  for (int i2 = lane; i2 < n2; i2 += 64) {
+    const int i2b = i2 + 32;
+    const bool hb = i2b < n2;
+    float sa[5], sb[5];
+    {
+      int fx;
+      const int d2 = fold(i2 - p2, n2, &fx);
+#pragma unroll
+      for (int k = 0; k < 5; k++) sa[k] = stage[k * n2 + i2];
+      mixed_update(f, N32, base + i2, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sa);
+    }
+    if (hb) {
+      int fx;
+      const int d2 = fold(i2b - p2, n2, &fx);
+#pragma unroll
+      for (int k = 0; k < 5; k++) sb[k] = stage[k * n2 + i2b];
+      mixed_update(f, N32, base + i2b, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sb);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 5; k++) sb[k] = sa[k];
     }
     if (!UPDATE_ONLY) {
-      const float dFs = f.dF32[s];
-      const float a = (kp.q_ref - dFs) * kp.a_scale;
-      // two modes per packed FMA; each lane is the scalar chain of mx_x
-#pragma unroll
-      for (int j = 0; j < STZ_MODES / 2; j++) {
-        float2 x = make_float2(a, a);
-#pragma unroll
-        for (int k = 0; k < 5; k++) x = __ffma2_rn(make_float2(sv[k], sv[k]), kp.mdev2[j][k], x);
-        acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(x.x), ex2_approx(x.y)));
-      }
-      // Q < 0 for some mode needs |W|/2 > dF; |W| <= |s| |deps| bounds it
-      const float n2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] + sv[3] * sv[3] + sv[4] * sv[4];
-      const float lim = dFs * kp.a_scale * kp.inv_mdev_norm;
-      if (n2 * kp.bound_slack >= lim * lim || lim <= 0.f) {
-#pragma unroll 1
-        for (int m = 0; m < STZ_MODES; m++) neg |= mx_x(kp, sv, a, m) > thr_neg ? 1u : 0u;
-      }
+      const float dFa = stage[5 * n2 + i2];
+      const float dFb = hb ? stage[5 * n2 + i2b] : dFa;
+      const float aa = (kp.q_ref - dFa) * kp.a_scale, ab = (kp.q_ref - dFb) * kp.a_scale;
+      mixed_rates2(sa, aa, sb, ab, hb, md, acc2);
+      neg |= mixed_neg(kp, sa, aa, dFa, thr_neg);
+      if (hb) neg |= mixed_neg(kp, sb, ab, dFb, thr_neg);
     }
-    // advance (i0, i1, i2) by TH sites
-    i2 += kp.adv_r2;
-    int carry = 0;
-    if (i2 >= kp.n2) { i2 -= kp.n2; carry = 1; }
-    i1 += kp.adv_q2 + carry;
-    while (i1 >= kp.n1) { i1 -= kp.n1; i0++; }
+  }
+}
+
+// Per-line sums: each lane parks its 20 sums in shared memory and lanes
+// 0..19 add one mode each over the 32 lanes (a fixed order), written to
+// lsum[line][m].
+__device__ __forceinline__ void line_sums(const float2* acc2, float (*red)[STZ_MODES], float* lsum_line) {
+  const int lane = threadIdx.x & 31;
+  float4* my = reinterpret_cast<float4*>(red[lane]);
+#pragma unroll
+  for (int j = 0; j < STZ_MODES / 4; j++)
+    my[j] = make_float4(acc2[2 * j].x, acc2[2 * j].y, acc2[2 * j + 1].x, acc2[2 * j + 1].y);
+  __syncwarp();
+  if (lane < STZ_MODES) {
+    float t = 0.f;
+#pragma unroll 8
+    for (int r = 0; r < 32; r++) t += red[r][lane];
+    lsum_line[lane] = t;
+  }
+  __syncwarp();
+}
+
+// Plane sums psum[m][i0] = sum over i1 of lsum[i0 n1 + i1][m] in FP64 for
+// plane i0, by one block: warp w adds modes w, w + 8, w + 16 with its lanes
+// striding the lines, then a fixed shuffle tree.
+__device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, double* psum, int i0) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float* ls = lsum + (long long)i0 * n1 * STZ_MODES;
+  for (int m = w; m < STZ_MODES; m += TH / 32) {
+    double v = 0.0;
+    for (int i1 = lane; i1 < n1; i1 += 32) v += (double)ls[i1 * STZ_MODES + m];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+    if (lane == 0) psum[(long long)m * n0 + i0] = v;
+  }
+}
+
+// Body of the grid-wide mixed-form kernel for block b of one replica (kp may
+// live in kernel parameters or, for batches, in shared memory); the block
+// takes units b, b + nblk, ... and its warps run through them independently.
+template <int UPDATE_ONLY>
+__device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b, const float2* md,
+                                                float* mix_smem) {
+  __shared__ __align__(8) unsigned long long mbar[TH / 32][2];
+  Ctl* ctl = f.ctl;
+  // the header and the halt flag in independent loads
+  const int4* hq = reinterpret_cast<const int4*>(&ctl->head);
+  const int4 h0 = hq[0], h1 = hq[1], h2 = hq[2];
+  const int halted = ctl->halt;
+  if (halted && !UPDATE_ONLY) return;
+  if (!UPDATE_ONLY && b == 0 && threadIdx.x == 0) ctl->prof_t0 = gtimer();
+  // pending transformation and uniform change
+  const float Ud[5] = {__int_as_float(h0.x), __int_as_float(h0.y), __int_as_float(h0.z), __int_as_float(h0.w),
+                       __int_as_float(h1.x)};
+  const int hp = h1.y;
+  const int p0 = h1.z, p1 = h1.w;
+  const int p2 = h2.x, pm = h2.y;  // MixHead: Ud[5], has_pend, p0, p1, p2, pend_mode
+  float de[5] = {0, 0, 0, 0, 0};
+  if (hp) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) de[k] = kp.mdev_raw[pm][k];
+  }
+  const float thr_neg = kp.q_ref * kp.a_scale;
+  unsigned neg = 0;
+  const int N32 = (int)kp.N;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sf = mix_stage_floats(kp.n2);
+  float* stages = mix_smem + (size_t)w * 2 * sf;
+  unsigned long long* bar = &mbar[w][0];
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  // this warp's lines: units b, b + nblk, ... (skipping the ones where the
+  // warp idles); line j lives in stage j & 1
+  int u = b;
+  LineOf L{0, 0, 0};
+  for (; u < kp.mx_units; u += kp.nblk)
+    if ((L = unit_line(kp, u, w, p0, p1)).valid) break;
+  if (u < kp.mx_units && lane == 0) issue_line<UPDATE_ONLY>(kp, f, L.i0, L.i1, stages, &bar[0]);
+  unsigned pending = u < kp.mx_units ? 1u : 0u;  // stages with a copy in flight
+  unsigned ppar = 0;                                // bit k: parity the copy of stage k completes
+  bool timed_out = false;
+  for (int j = 0; u < kp.mx_units; j++) {
+    int un = u + kp.nblk;
+    LineOf Ln{0, 0, 0};
+    for (; un < kp.mx_units; un += kp.nblk)
+      if ((Ln = unit_line(kp, un, w, p0, p1)).valid) break;
+    float* cur = stages + (j & 1) * sf;
+    float* nxt = stages + ((j + 1) & 1) * sf;
+    __syncwarp();
+    if (un < kp.mx_units) {
+      if (lane == 0) issue_line<UPDATE_ONLY>(kp, f, Ln.i0, Ln.i1, nxt, &bar[(j + 1) & 1]);
+      pending |= 1u << ((j + 1) & 1);
+      ppar = (ppar & ~(1u << ((j + 1) & 1))) | ((((unsigned)(j + 1) >> 1) & 1u) << ((j + 1) & 1));
+    }
+    if (!mbar_wait(&bar[j & 1], (unsigned)(j >> 1) & 1u)) {
+      pending &= ~(1u << (j & 1));  // waited for already, to the limit
+      timed_out = true;
+      break;
+    }
+    pending &= ~(1u << (j & 1));
+    float2 acc2[STZ_MODES / 2];
+#pragma unroll
+    for (int q = 0; q < STZ_MODES / 2; q++) acc2[q] = make_float2(0.f, 0.f);
+    mixed_line<UPDATE_ONLY>(kp, f, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
+    if (!UPDATE_ONLY) {
+      // the consumed stage holds the transpose
+      __syncwarp();
+      line_sums(acc2, reinterpret_cast<float(*)[STZ_MODES]>(cur),
+                f.lsum + ((long long)L.i0 * kp.n1 + L.i1) * STZ_MODES);
+    }
+    u = un;
+    L = Ln;
+  }
+  if (timed_out) {
+    // record the error and wait (bounded) for this warp's copies in flight,
+    // so no copy lands in shared memory after the block has left
+    if (lane == 0) {
+      f.ctl->status = STZ_ERR_TIMEOUT;
+      f.ctl->halt_reason = kHaltError;
+      f.ctl->halt = 1;
+    }
+    for (int k = 0; k < 2; k++)
+      if (pending & (1u << k)) (void)mbar_wait(&bar[k], (ppar >> k) & 1u);
   }
   if (UPDATE_ONLY) return;
   pdl_release();
-  float acc[STZ_MODES];
-#pragma unroll
-  for (int j = 0; j < STZ_MODES / 2; j++) {
-    acc[2 * j] = acc2[j].x;
-    acc[2 * j + 1] = acc2[j].y;
-  }
-  block_mode_sums_f32(acc, f.part, kp.nblk, b);
   const unsigned nb = block_sum_u(neg);
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
-  group_reduce(kp, f, b);
 }
 
 template <int UPDATE_ONLY>
 __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
+  extern __shared__ __align__(128) float mix_smem[];
   pdl_wait();
-  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x);
+  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x, &kp.mdev2[0][0], mix_smem);
+}
+
+// One block per plane: the plane sums the selection reads.
+__global__ void __launch_bounds__(TH) k_mixed_planes(KParams kp, Fields f) {
+  pdl_wait();
+  pdl_release();
+  if (f.ctl->halt) return;
+  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x);
 }
 
 // ------------------------------------------------------- mixed-form tail
@@ -1252,112 +1413,120 @@ __device__ void mixed_commit_lanes(const KParams& kp, const Fields& f, Ctl* c, l
   __syncwarp();
 }
 
-// Search of the mixed form: the group and block levels in FP64 as in
-// search_event; the in-block level sums each thread's FP32 rates once, scans
-// those sums in FP64 and locates the site in FP32 relative to the thread's
-// FP64 offset (the rates themselves are FP32).
+// Search of the mixed form in the mode-major site order (event m N + s), in
+// three levels: (mode, plane) over the FP64 plane sums, whose per-thread
+// chunk sums were scanned into sh_inc when the total was formed; the lines of
+// that plane from their FP32 sums, scanned in FP64; the sites of that line
+// with their rates recomputed exactly as the main pass computed them, scanned
+// per thread in FP64 and located in FP32 within the thread. Where rounding
+// leaves the target past the last entry of a level, the last positive entry
+// is taken.
 __device__ void search_mixed(const KParams& kp, const Fields& f, double T, const double* sh_inc,
                              long long* site_out, int* mode_out, double* margin_out) {
   __shared__ double sh_inc2[TH];
-  __shared__ long long sh_p;
-  __shared__ double sh_cb;
+  __shared__ long long sh_p1;
+  __shared__ int sh_p2;
+  __shared__ double sh_cb1, sh_cb2;
   __shared__ long long sh_site;
   __shared__ double sh_margin;
   const int t = threadIdx.x;
-  const long long P = (long long)STZ_MODES * kp.ngroups;
-  const long long ch = (P + TH - 1) / TH;
-  const long long p0 = t * ch, p1 = min(p0 + ch, P);
-  if (t == 0) { sh_p = -1; sh_site = -1; sh_margin = 0; }
+  if (t == 0) { sh_p1 = -1; sh_p2 = -1; sh_site = -1; sh_margin = 0; sh_cb1 = 0; sh_cb2 = 0; }
   __syncthreads();
-  const double I = sh_inc[t];
-  const double E = t > 0 ? sh_inc[t - 1] : 0.0;
-  double Tq = T;
-  if (Tq > sh_inc[TH - 1]) Tq = sh_inc[TH - 1];
-  if (E < Tq && Tq <= I) {
-    double run = E;
-    long long hit = -1, lastpos = -1;
-    double hb = E, lastbefore = E;
-    for (long long q = p0; q < p1; q++) {
-      const double v = f.gsum[q];
-      const double before = run;
-      run += v;
-      if (v > 0) { lastpos = q; lastbefore = before; }
-      if (hit < 0 && v > 0 && run >= Tq) { hit = q; hb = before; }
+  // level 1: entries q = m n0 + i0
+  const long long P = (long long)STZ_MODES * kp.n0;
+  const long long ch = (P + TH - 1) / TH;
+  const long long q0 = t * ch, q1 = min(q0 + ch, P);
+  {
+    const double I = sh_inc[t];
+    const double E = t > 0 ? sh_inc[t - 1] : 0.0;
+    double Tq = T;
+    if (Tq > sh_inc[TH - 1]) Tq = sh_inc[TH - 1];
+    if (E < Tq && Tq <= I) {
+      double run = E;
+      long long hit = -1, lastpos = -1;
+      double hb = E, lastbefore = E;
+      for (long long q = q0; q < q1; q++) {
+        const double v = f.psum[q];
+        const double before = run;
+        run += v;
+        if (v > 0) { lastpos = q; lastbefore = before; }
+        if (hit < 0 && v > 0 && run >= Tq) { hit = q; hb = before; }
+      }
+      if (hit < 0) { hit = lastpos; hb = lastbefore; }
+      sh_p1 = hit;
+      sh_cb1 = Tq - hb;  // the target left for the lines of entry hit
     }
-    if (hit < 0) { hit = lastpos; hb = lastbefore; }
-    sh_p = hit;
-    sh_cb = hb;
   }
   __syncthreads();
-  const long long pg = sh_p;
+  const long long pg = sh_p1;
   if (pg < 0) {
     if (t == 0) { *site_out = -1; *mode_out = -1; }
     return;
   }
-  const int m = (int)(pg / kp.ngroups);
-  const int g = (int)(pg - (long long)m * kp.ngroups);
-  if (t < 32) {
-    const int g0 = g * kGroup, g1 = min(g0 + kGroup, kp.nblk);
-    const double v = (g0 + t < g1) ? f.part[(long long)m * kp.nblk + g0 + t] : 0.0;
-    double x = v;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const double y = __shfl_up_sync(FULL, x, off);
-      if (t >= off) x += y;
-    }
-    const double before = __shfl_up_sync(FULL, x, 1);
-    const double ex = t > 0 ? before : 0.0;
-    const double Tg = Tq - sh_cb;
-    const unsigned ok = __ballot_sync(FULL, v > 0 && x >= Tg);
-    const unsigned posb = __ballot_sync(FULL, v > 0);
-    const int lane = ok ? __ffs(ok) - 1 : (posb ? 31 - __clz(posb) : -1);
-    if (lane >= 0) {
-      const double exl = __shfl_sync(FULL, ex, lane);
-      if (t == 0) { sh_p = g0 + lane; sh_cb = sh_cb + exl; }
-    } else if (t == 0) {
-      sh_p = -1;
+  const int m = (int)(pg / kp.n0);
+  const int i0 = (int)(pg - (long long)m * kp.n0);
+  // level 2: lines i1 of plane i0 for mode m
+  const int n1 = kp.n1;
+  const int ch1 = (n1 + TH - 1) / TH;
+  const int a1 = t * ch1, b1 = min(a1 + ch1, n1);
+  const float* lp = f.lsum + (long long)i0 * n1 * STZ_MODES + m;
+  double S1 = 0.0;
+  for (int i1 = a1; i1 < b1; i1++) S1 += (double)lp[i1 * STZ_MODES];
+  {
+    const double I1 = block_incl_scan(S1, sh_inc2);
+    const double E1 = t > 0 ? sh_inc2[t - 1] : 0.0;
+    double T1 = sh_cb1;
+    if (T1 > sh_inc2[TH - 1]) T1 = sh_inc2[TH - 1];
+    if (!(T1 > 0)) T1 = DBL_MIN;
+    if (E1 < T1 && T1 <= I1) {
+      double run = E1;
+      int hit = -1, lastpos = -1;
+      double hb = E1, lastbefore = E1;
+      for (int i1 = a1; i1 < b1; i1++) {
+        const double v = (double)lp[i1 * STZ_MODES];
+        const double before = run;
+        run += v;
+        if (v > 0) { lastpos = i1; lastbefore = before; }
+        if (hit < 0 && v > 0 && run >= T1) { hit = i1; hb = before; }
+      }
+      if (hit < 0) { hit = lastpos; hb = lastbefore; }
+      sh_p2 = hit;
+      sh_cb2 = T1 - hb;
     }
   }
   __syncthreads();
-  if (sh_p < 0) {
+  const int i1 = sh_p2;
+  if (i1 < 0) {
     if (t == 0) { *site_out = -1; *mode_out = -1; }
     return;
   }
-  const int b = (int)sh_p;
-  double T2 = Tq - sh_cb;
-  const long long s0 = (long long)b * kp.bsites;
-  const long long s1 = min(s0 + (long long)kp.bsites, kp.N);
-  const long long per = (s1 - s0 + TH - 1) / TH;
-  const long long a0 = s0 + t * per;
-  float rr[kMaxPerMixed];
+  // level 3: sites of line (i0, i1)
+  const int n2 = kp.n2;
+  const int ch2 = (n2 + TH - 1) / TH;
+  const int a2 = t * ch2, b2 = min(a2 + ch2, n2);
+  const long long base = ((long long)i0 * n1 + i1) * n2;
+  const double zero[6] = {0, 0, 0, 0, 0, 0};
   float locf = 0.f;
-  double zero[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-  for (int k = 0; k < kMaxPerMixed; k++) {
-    const long long s = a0 + k;
-    rr[k] = (k < per && s < s1) ? (float)site_rate<2>(kp, f, zero, 0.0, s, m) : 0.f;
-    locf += rr[k];
-  }
+  for (int i2 = a2; i2 < b2; i2++) locf += (float)site_rate<2>(kp, f, zero, 0.0, base + i2, m);
   const double I2 = block_incl_scan((double)locf, sh_inc2);
   const double E2 = t > 0 ? sh_inc2[t - 1] : 0.0;
-  const double tot2 = sh_inc2[TH - 1];
-  if (T2 > tot2) T2 = tot2;
+  double T2 = sh_cb2;
+  if (T2 > sh_inc2[TH - 1]) T2 = sh_inc2[TH - 1];
   if (!(T2 > 0)) T2 = DBL_MIN;
   if (E2 < T2 && T2 <= I2) {
     const float rem = (float)(T2 - E2);
     float run = 0.f;
     int hit = -1, lastk = -1;
     float hb = 0.f, ha = 0.f, lb = 0.f, la = 0.f;
-#pragma unroll
-    for (int k = 0; k < kMaxPerMixed; k++) {
+    for (int i2 = a2; i2 < b2; i2++) {
+      const float r = (float)site_rate<2>(kp, f, zero, 0.0, base + i2, m);
       const float before = run;
-      run += rr[k];
-      const bool pos = rr[k] > 0.f;
-      if (pos) { lastk = k; lb = before; la = run; }
-      if (hit < 0 && pos && run >= rem) { hit = k; hb = before; ha = run; }
+      run += r;
+      if (r > 0.f) { lastk = i2; lb = before; la = run; }
+      if (hit < 0 && r > 0.f && run >= rem) { hit = i2; hb = before; ha = run; }
     }
     if (hit < 0) { hit = lastk; hb = lb; ha = la; }
-    sh_site = hit < 0 ? -1 : a0 + hit;
+    sh_site = hit < 0 ? -1 : base + hit;
     sh_margin = (double)fminf(rem - hb, ha - rem);
   }
   __syncthreads();
@@ -1376,8 +1545,11 @@ constexpr int kCtlScalarWords = (int)(offsetof(Ctl, rng) / 4);
 __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields& f, int update_only) {
   Ctl* const g = f.ctl;
   if (update_only) {
-    if (threadIdx.x < 6) g->U[threadIdx.x] = 0;
-    if (threadIdx.x == 0) g->has_pend = 0;
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < 6; k++) g->U[k] = 0;
+      g->has_pend = 0;
+      set_mixed_head(kp, g);
+    }
     return;
   }
   if (g->halt) return;
@@ -1394,11 +1566,13 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
     for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
   }
-  const long long P = (long long)STZ_MODES * kp.ngroups;
+  // total rate: the FP64 plane sums, per-thread contiguous chunks (the chunks
+  // the first search level walks again)
+  const long long P = (long long)STZ_MODES * kp.n0;
   const long long ch = (P + TH - 1) / TH;
   const long long p0 = threadIdx.x * ch, p1 = min(p0 + ch, P);
   double S = 0;
-  for (long long p = p0; p < p1; p++) S += f.gsum[p];
+  for (long long p = p0; p < p1; p++) S += f.psum[p];
   block_incl_scan(S, sh_inc);
   const unsigned long long t_sums = gtimer();
   block_twist_if_needed(&g->rng);
@@ -1519,6 +1693,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       c->prof_n++;
     }
   }
+  if (threadIdx.x == 0) set_mixed_head(kp, c);
   __syncthreads();
   {
     const uint32_t* a = reinterpret_cast<const uint32_t*>(&sc);
@@ -1555,7 +1730,18 @@ __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __rest
   pdl_wait();
   const int r = blk_rep[blockIdx.x];
   load_desc(d, r, &skp, &sf);
-  mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r]);
+  extern __shared__ __align__(128) float mix_smem[];
+  mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], mix_smem);
+}
+
+// Plane sums of a batch: block (x, r) sums plane x of replica r.
+__global__ void __launch_bounds__(TH) k_mixed_planes_batched(const BatchDesc* __restrict__ d) {
+  pdl_wait();
+  pdl_release();
+  const BatchDesc& e = d[blockIdx.y];
+  const int n0 = e.kp.n0;
+  if ((int)blockIdx.x >= n0 || e.f.ctl->halt) return;
+  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(TH) k_mixed_tail_batched(const BatchDesc* __restrict__ d,
@@ -1583,13 +1769,13 @@ __global__ void k_mixed_after_resolve(KParams kp, Fields f, int kind) {
   Ctl* ctl = f.ctl;
   ctl->has_pend = 0;
   for (int c = 0; c < 6; c++) ctl->U[c] = 0;
+  set_mixed_head(kp, ctl);
   if (kind == 0) {
     for (int c = 0; c < 6; c++) {
       ctl->eps_avg_applied[c] = ctl->eps_avg[c];
       ctl->u[c] = 0;
     }
   }
-  (void)kp;
 }
 
 // ------------------------------------------------------------ misc
@@ -1660,9 +1846,39 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st) {
   else k_rate64<1><<<kp.nblk, TH, 0, st>>>(kp, f);
 }
 
-int mixed_blocks_per_sm() {
+// The staged lines of the mixed-form main kernels are dynamic shared memory,
+// above the 48 KB default for long lines: raise their limit once per device
+// to what the device allows next to their static shared memory.
+static void mixed_smem_init() {
+  static bool done_dev[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (done_dev[dev & 63]) return;
+  done_dev[dev & 63] = true;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 48 * 1024;
+  auto raise = [&](const void* k) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k) != cudaSuccess) { (void)cudaGetLastError(); return; }
+    const int bytes = optin - (int)fa.sharedSizeBytes;
+    if (bytes > 0 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+      (void)cudaGetLastError();
+  };
+  raise((const void*)k_mixed<0>);
+  raise((const void*)k_mixed<1>);
+  raise((const void*)k_mixed_batched);
+}
+
+size_t mixed_smem(int n2) { return mix_smem_bytes(n2); }
+
+int mixed_blocks_per_sm(int n2) {
+  mixed_smem_init();
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed<0>, TH, 0) != cudaSuccess || occ < 1) occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed<0>, TH, mix_smem_bytes(n2)) != cudaSuccess ||
+      occ < 1) {
+    (void)cudaGetLastError();
+    occ = 1;
+  }
   return occ;
 }
 
@@ -1671,11 +1887,11 @@ namespace {
 // be scheduled while the previous kernel of the stream finishes; it waits for
 // it with griddepcontrol.wait.
 template <typename... A>
-void launch_pdl(void (*kern)(A...), int grid, cudaStream_t st, A... args) {
+void launch_pdl(void (*kern)(A...), dim3 grid, size_t smem, cudaStream_t st, A... args) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
+  cfg.gridDim = grid;
   cfg.blockDim = dim3(TH);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1687,19 +1903,25 @@ void launch_pdl(void (*kern)(A...), int grid, cudaStream_t st, A... args) {
 }  // namespace
 
 void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, cudaStream_t st) {
-  launch_pdl(k_mixed_batched, total_blocks, st, d, blk_rep, rep_first);
-  launch_pdl(k_mixed_tail_batched, nrep, st, d, status);
+                          BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st) {
+  mixed_smem_init();
+  launch_pdl(k_mixed_batched, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first);
+  launch_pdl(k_mixed_planes_batched, dim3(max_n0, nrep), 0, st, d);
+  launch_pdl(k_mixed_tail_batched, dim3(nrep), 0, st, d, status);
 }
 
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
-  if (update_only) k_mixed<1><<<kp.nblk, TH, 0, st>>>(kp, f);
-  else launch_pdl(k_mixed<0>, kp.nblk, st, kp, f);
+  mixed_smem_init();
+  if (update_only) k_mixed<1><<<kp.nblk, TH, mix_smem_bytes(kp.n2), st>>>(kp, f);
+  else launch_pdl(k_mixed<0>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
 }
 
 void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
-  else launch_pdl(k_mixed_tail, 1, st, kp, f, update_only);
+  else {
+    launch_pdl(k_mixed_planes, dim3(kp.n0), 0, st, kp, f);
+    launch_pdl(k_mixed_tail, dim3(1), 0, st, kp, f, update_only);
+  }
 }
 
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {

@@ -7,7 +7,6 @@
 namespace stz {
 
 constexpr int kRateThreads = 256;
-constexpr int kMaxPerMixed = 24;  // most sites per thread of the mixed-form kernel
 constexpr int kSptFp64 = 4;    // sites per thread of the FP64 rate kernels
 constexpr int kGroup = 32;     // blocks per group in the two-level rate sums
 
@@ -19,10 +18,14 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
 // One round of a batch: every replica's update/rate blocks in one grid, then
 // one selection/commit block per replica.
+// Kernels per thermal event of the mixed form: main pass, plane sums, tail.
+constexpr int kMixedLaunches = 3;
 void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, cudaStream_t st);
+                          BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st);
 // Resident blocks per SM of the mixed-form kernel (occupancy query).
-int mixed_blocks_per_sm();
+int mixed_blocks_per_sm(int n2);
+// Dynamic shared memory of one mixed-form main block for lines of n2 sites.
+size_t mixed_smem(int n2);
 // The two halves of launch_mixed: the grid-wide update/rate kernel and the
 // one-block selection/commit kernel.
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);

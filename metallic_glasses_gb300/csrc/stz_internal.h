@@ -41,7 +41,20 @@ enum HaltReason {
 
 // Device-resident control block: every scalar of the simulation state plus
 // the per-step flags that steer the kernels of a step. One per context.
+// What the mixed-form main pass reads at its start, prepared by the kernel
+// that last changed the pending state: the deviatoric coordinates of the
+// uniform change U in FP32 and the pending transformation (site coordinates
+// and mode), so that pass does no FP64 arithmetic and no dependent loads.
+struct __align__(16) MixHead {  // read as three 16-byte words; keep the order
+  float Ud[5];
+  int has_pend;
+  int p0, p1, p2, pend_mode;
+  int pad[2];
+};
+static_assert(sizeof(MixHead) == 48, "MixHead is three 16-byte words");
+
 struct Ctl {
+  MixHead head;
   double totime;
   double eps_avg[6];         // EpsAvg
   double eps_avg_applied[6]; // mean strain the stored field was solved with
@@ -97,6 +110,8 @@ struct Fields {
   double* part = nullptr;    // [MODES][nblk] per (mode, block) rate sums
   double* gsum = nullptr;    // [MODES][ngroups] per (mode, group of blocks) sums
   unsigned* gticket = nullptr;  // [ngroups] last-block counters of the groups
+  float* lsum = nullptr;     // mixed: [n0 n1][MODES] per-line rate sums
+  double* psum = nullptr;    // mixed: [MODES][n0] per-plane rate sums
   void* spec = nullptr;      // [nc][Nk] complex FP64 spectrum
   float* ktab = nullptr;     // mixed: [kt0][kt1][kt2][16] response table (15 used)
   stz_event* log = nullptr;  // event ring
@@ -111,6 +126,7 @@ struct KParams {
   long long N, Nk;
   int nblk, bsites;          // rate kernel: blocks and sites per block
   int ngroups;               // groups of kGroup blocks
+  int mx_c1, mx_units;       // mixed form: d1 chunks per d0, units (kt0 * mx_c1)
   int adv_q2, adv_r2;        // kRateThreads sites = adv_q2 rows of n2 plus adv_r2 sites
   int fast_inv;              // mixed form: precomputed compliance coefficients
   double inv_2mu, inv_lam_coef, invN, inv_a_scale;
