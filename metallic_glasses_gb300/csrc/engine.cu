@@ -479,9 +479,11 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   if (!ref2d && p.softening) { set_error("softening is implemented for the reference 2D model only"); return STZ_ERR_UNSUPPORTED; }
   const bool mixed = p.precision == STZ_PREC_MIXED;
   if (mixed && ref2d) { set_error("the mixed form is implemented for the 3D model"); return STZ_ERR_UNSUPPORTED; }
-  if (mixed && (p.n[2] % 4 || p.n[2] > 512)) {
-    // lines are staged by 16-byte bulk copies into shared memory, two per warp
-    set_error("the mixed form needs the fastest extent a multiple of 4, at most 512 (got %d)", p.n[2]);
+  if (mixed && (p.n[2] % 4 || p.n[2] > 512 || p.n[1] > 512)) {
+    // lines are staged by 16-byte bulk copies into shared memory, two per
+    // warp; the selection walks a line or a plane's lines with one warp
+    set_error("the mixed form needs the fastest extent a multiple of 4 and n1, n2 at most 512 (got %dx%dx%d)",
+              p.n[0], p.n[1], p.n[2]);
     return STZ_ERR_UNSUPPORTED;
   }
   int solver = p.solver;
@@ -959,8 +961,11 @@ extern "C" int stz_phase_times(stz_ctx* c, double* main_us, double* tail_us, int
   if (tail_us) *tail_us = (double)h.prof_tail_ns * k;
   if (n) *n = (int64_t)h.prof_n;
   if (std::getenv("STZ_PHASE_DETAIL"))
-    std::fprintf(stderr, "stz tail parts (us): sums %.2f decide %.2f search %.2f commit %.2f\n",
-                 h.prof_part_ns[0] * k, h.prof_part_ns[1] * k, h.prof_part_ns[2] * k, h.prof_part_ns[3] * k);
+    std::fprintf(stderr,
+                 "stz tail parts (us): sums %.2f decide %.2f search %.2f (planes %.2f lines %.2f sites %.2f) "
+                 "commit %.2f\n",
+                 h.prof_part_ns[0] * k, h.prof_part_ns[1] * k, h.prof_part_ns[2] * k, h.prof_part_ns[4] * k,
+                 h.prof_part_ns[5] * k, h.prof_part_ns[6] * k, h.prof_part_ns[3] * k);
   return STZ_OK;
 }
 

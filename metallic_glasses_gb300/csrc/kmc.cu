@@ -1039,9 +1039,12 @@ __device__ __forceinline__ void mixed_update(const Fields& f, int N32, int s, in
 
 // The 20 rates of two sites (b may be absent), packed two modes per FP32x2
 // FMA; each lane of a pair is the scalar chain of mx_x, so the search sees the
-// same bits. One load of each mode coefficient serves both sites.
+// same bits. One load of each mode coefficient serves both sites. Returns the
+// largest argument of site a in *xma and of site b in *xmb (an argument above
+// q_ref a_scale is a negative barrier, the athermal trigger).
 __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const float* sb, float ab, bool hb,
-                                             const float2* md, float2* acc2) {
+                                             const float2* md, float2* acc2, float* xma, float* xmb) {
+  float2 mx = make_float2(-INFINITY, -INFINITY);
 #pragma unroll
   for (int j = 0; j < STZ_MODES / 2; j++) {
     float2 xa = make_float2(aa, aa), xb = make_float2(ab, ab);
@@ -1053,20 +1056,11 @@ __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const fl
     }
     acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
     if (hb) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xb.x), ex2_approx(xb.y)));
+    mx.x = fmaxf(mx.x, fmaxf(xa.x, xa.y));
+    mx.y = fmaxf(mx.y, fmaxf(xb.x, xb.y));
   }
-}
-
-// Q < 0 for some mode needs |W|/2 > dF; |W| <= |s| |deps| bounds it, and only
-// sites past the bound evaluate the 20 exact tests.
-__device__ __forceinline__ unsigned mixed_neg(const KParams& kp, const float* sv, float a, float dFs, float thr_neg) {
-  const float n2 = sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] + sv[3] * sv[3] + sv[4] * sv[4];
-  const float lim = dFs * kp.a_scale * kp.inv_mdev_norm;
-  unsigned neg = 0;
-  if (n2 * kp.bound_slack >= lim * lim || lim <= 0.f) {
-#pragma unroll 1
-    for (int m = 0; m < STZ_MODES; m++) neg |= mx_x(kp, sv, a, m) > thr_neg ? 1u : 0u;
-  }
-  return neg;
+  *xma = mx.x;
+  *xmb = mx.y;
 }
 
 // ------------------------------------------ bulk-copy staging of a line
@@ -1180,9 +1174,9 @@ __device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, i
       const float dFa = stage[5 * n2 + i2];
       const float dFb = hb ? stage[5 * n2 + i2b] : dFa;
       const float aa = (kp.q_ref - dFa) * kp.a_scale, ab = (kp.q_ref - dFb) * kp.a_scale;
-      mixed_rates2(sa, aa, sb, ab, hb, md, acc2);
-      neg |= mixed_neg(kp, sa, aa, dFa, thr_neg);
-      if (hb) neg |= mixed_neg(kp, sb, ab, dFb, thr_neg);
+      float xma, xmb;
+      mixed_rates2(sa, aa, sb, ab, hb, md, acc2, &xma, &xmb);
+      neg |= (xma > thr_neg || (hb && xmb > thr_neg)) ? 1u : 0u;
     }
   }
 }
@@ -1210,14 +1204,30 @@ __device__ __forceinline__ void line_sums(const float2* acc2, float (*red)[STZ_M
 // plane i0, by one block: warp w adds modes w, w + 8, w + 16 with its lanes
 // striding the lines, then a fixed shuffle tree.
 __device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, double* psum, int i0) {
+  constexpr int kModesPerWarp = (STZ_MODES + TH / 32 - 1) / (TH / 32);  // 3
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float* ls = lsum + (long long)i0 * n1 * STZ_MODES;
-  for (int m = w; m < STZ_MODES; m += TH / 32) {
-    double v = 0.0;
-    for (int i1 = lane; i1 < n1; i1 += 32) v += (double)ls[i1 * STZ_MODES + m];
+  double v[kModesPerWarp];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
-    if (lane == 0) psum[(long long)m * n0 + i0] = v;
+  for (int j = 0; j < kModesPerWarp; j++) v[j] = 0.0;
+  // all loads of a line before the adds: one memory round trip per 32 lines
+  for (int i1 = lane; i1 < n1; i1 += 32) {
+    float x[kModesPerWarp];
+#pragma unroll
+    for (int j = 0; j < kModesPerWarp; j++) {
+      const int m = w + j * (TH / 32);
+      x[j] = m < STZ_MODES ? ls[i1 * STZ_MODES + m] : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < kModesPerWarp; j++) v[j] += (double)x[j];
+  }
+#pragma unroll
+  for (int j = 0; j < kModesPerWarp; j++) {
+    double t = v[j];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(FULL, t, off);
+    const int m = w + j * (TH / 32);
+    if (lane == 0 && m < STZ_MODES) psum[(long long)m * n0 + i0] = t;
   }
 }
 
@@ -1413,128 +1423,181 @@ __device__ void mixed_commit_lanes(const KParams& kp, const Fields& f, Ctl* c, l
   __syncwarp();
 }
 
-// Search of the mixed form in the mode-major site order (event m N + s), in
-// three levels: (mode, plane) over the FP64 plane sums, whose per-thread
-// chunk sums were scanned into sh_inc when the total was formed; the lines of
-// that plane from their FP32 sums, scanned in FP64; the sites of that line
-// with their rates recomputed exactly as the main pass computed them, scanned
-// per thread in FP64 and located in FP32 within the thread. Where rounding
-// leaves the target past the last entry of a level, the last positive entry
-// is taken.
-__device__ void search_mixed(const KParams& kp, const Fields& f, double T, const double* sh_inc,
-                             long long* site_out, int* mode_out, double* margin_out) {
-  __shared__ double sh_inc2[TH];
-  __shared__ long long sh_p1;
-  __shared__ int sh_p2;
-  __shared__ double sh_cb1, sh_cb2;
-  __shared__ long long sh_site;
-  __shared__ double sh_margin;
-  const int t = threadIdx.x;
-  if (t == 0) { sh_p1 = -1; sh_p2 = -1; sh_site = -1; sh_margin = 0; sh_cb1 = 0; sh_cb2 = 0; }
+// ------------------------------------------------ fixed-point selection
+// The selection of the mixed form runs in exact 64-bit fixed point: every
+// plane, line and site rate is held as floor(v 2^e) for one power of two e
+// per event, chosen so that the total stays below 2^62. Sums of integers do
+// not depend on their order and take integer adds, where the FP64 sums they
+// replace cost this part's FP64 units tens of cycles each; the quantum
+// 2^-e is about 2^-50 of the largest plane sum, finer than FP64 for every
+// partial sum the search compares.
+constexpr long long kFixMax = 1LL << 62;
+__device__ __forceinline__ long long fix_d(double v, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)(b >> 52) & 0x7ff;
+  if (ex == 0 || (b >> 63)) return 0;  // zero, subnormal or negative
+  const unsigned long long mant = (b & 0xfffffffffffffULL) | (1ULL << 52);
+  const int sh = ex - 1075 + e;
+  if (sh >= 9) return kFixMax;
+  if (sh <= -53) return 0;
+  return (long long)(sh >= 0 ? mant << sh : mant >> -sh);
+}
+__device__ __forceinline__ long long fix_f(float v, int e) {
+  const unsigned b = __float_as_uint(v);
+  const int ex = (int)(b >> 23) & 0xff;
+  if (ex == 0 || (b >> 31)) return 0;
+  const unsigned long long mant = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = ex - 150 + e;
+  if (sh >= 38) return kFixMax;
+  if (sh <= -24) return 0;
+  return (long long)(sh >= 0 ? mant << sh : mant >> -sh);
+}
+// ceil(log2(n)) for n >= 1
+__device__ __forceinline__ int clog2(long long n) { return n <= 1 ? 0 : 64 - __clzll(n - 1); }
+
+__device__ __forceinline__ long long shfl_up_i64(long long v, int off) {
+  return (long long)__shfl_up_sync(FULL, (unsigned long long)v, off);
+}
+
+// Inclusive scan of one value per thread over the 256-thread block; returns
+// the inclusive value and leaves every thread's in sh_inc.
+__device__ long long block_incl_scan_i64(long long v, long long* sh_inc) {
+  __shared__ long long wsum[TH / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const long long y = shfl_up_i64(x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
   __syncthreads();
-  // level 1: entries q = m n0 + i0
-  const long long P = (long long)STZ_MODES * kp.n0;
-  const long long ch = (P + TH - 1) / TH;
-  const long long q0 = t * ch, q1 = min(q0 + ch, P);
-  {
-    const double I = sh_inc[t];
-    const double E = t > 0 ? sh_inc[t - 1] : 0.0;
-    double Tq = T;
-    if (Tq > sh_inc[TH - 1]) Tq = sh_inc[TH - 1];
-    if (E < Tq && Tq <= I) {
-      double run = E;
-      long long hit = -1, lastpos = -1;
-      double hb = E, lastbefore = E;
-      for (long long q = q0; q < q1; q++) {
-        const double v = f.psum[q];
-        const double before = run;
-        run += v;
-        if (v > 0) { lastpos = q; lastbefore = before; }
-        if (hit < 0 && v > 0 && run >= Tq) { hit = q; hb = before; }
-      }
-      if (hit < 0) { hit = lastpos; hb = lastbefore; }
-      sh_p1 = hit;
-      sh_cb1 = Tq - hb;  // the target left for the lines of entry hit
+  if (w == 0) {
+    long long t = lane < TH / 32 ? wsum[lane] : 0;
+#pragma unroll
+    for (int off = 1; off < TH / 32; off <<= 1) {
+      const long long y = shfl_up_i64(t, off);
+      if (lane >= off) t += y;
     }
+    if (lane < TH / 32) wsum[lane] = t;
   }
   __syncthreads();
-  const long long pg = sh_p1;
-  if (pg < 0) {
-    if (t == 0) { *site_out = -1; *mode_out = -1; }
-    return;
+  const long long incl = (w > 0 ? wsum[w - 1] : 0) + x;
+  sh_inc[threadIdx.x] = incl;
+  __syncthreads();
+  return incl;
+}
+
+// Warp search over per-lane contiguous chunks with sums v: the lane whose
+// inclusive prefix first reaches T (T clamped to the total, so that the last
+// positive chunk is taken when the finer level sums to less than the coarser
+// one), its exclusive prefix in *excl and the clamped target in *tq; -1 when
+// every chunk is empty.
+__device__ __forceinline__ int warp_find_i64(long long v, long long T, long long* excl, long long* tq) {
+  const int lane = threadIdx.x & 31;
+  long long x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const long long y = shfl_up_i64(x, off);
+    if (lane >= off) x += y;
   }
-  const int m = (int)(pg / kp.n0);
-  const int i0 = (int)(pg - (long long)m * kp.n0);
-  // level 2: lines i1 of plane i0 for mode m
+  const long long tot = (long long)__shfl_sync(FULL, (unsigned long long)x, 31);
+  long long Tq = T > tot ? tot : T;
+  if (Tq < 1) Tq = 1;
+  const long long Eu = shfl_up_i64(x, 1);  // every lane takes part in the shuffle
+  const long long El = lane ? Eu : 0;
+  const unsigned hit = __ballot_sync(FULL, v > 0 && El < Tq && Tq <= x);
+  const int L = hit ? __ffs(hit) - 1 : -1;
+  *excl = (long long)__shfl_sync(FULL, (unsigned long long)El, L < 0 ? 0 : L);
+  *tq = Tq;
+  return L;
+}
+
+// Within one lane's chunk of n values (registers, unrolled): the first
+// positive entry whose running sum from E reaches T; its index, the running
+// sum before it and after it.
+template <int K>
+__device__ __forceinline__ int chunk_find(const long long* v, long long E, long long T, long long* before,
+                                          long long* after) {
+  long long run = E;
+  int hit = -1, lastpos = -1;
+  long long hb = E, ha = E, lb = E, la = E;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const long long b0 = run;
+    run += v[k];
+    if (v[k] > 0) { lastpos = k; lb = b0; la = run; }
+    if (hit < 0 && v[k] > 0 && run >= T) { hit = k; hb = b0; ha = run; }
+  }
+  if (hit < 0) { hit = lastpos; hb = lb; ha = la; }
+  *before = hb;
+  *after = ha;
+  return hit;
+}
+
+// Levels 2 and 3 of the mixed-form search, by warp 0 alone: the lines of
+// plane i0 for mode m from their FP32 sums, then the sites of the chosen line
+// with their rates recomputed exactly as the main pass computed them, both in
+// the fixed point of scale e. T is the target left within (m, i0). Returns
+// the site (or -1) in every lane and the distance of the target from the
+// nearer edge of the chosen site's interval in *margin.
+constexpr int kLaneChunk = 16;  // lines or sites per lane: n1, n2 <= 512
+__device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
+                                      long long* margin, unsigned long long* t_lines) {
+  const int lane = threadIdx.x & 31;
+  // level 2: lines
   const int n1 = kp.n1;
-  const int ch1 = (n1 + TH - 1) / TH;
-  const int a1 = t * ch1, b1 = min(a1 + ch1, n1);
+  const int c2 = (n1 + 31) / 32;
+  const int a1 = lane * c2;
   const float* lp = f.lsum + (long long)i0 * n1 * STZ_MODES + m;
-  double S1 = 0.0;
-  for (int i1 = a1; i1 < b1; i1++) S1 += (double)lp[i1 * STZ_MODES];
-  {
-    const double I1 = block_incl_scan(S1, sh_inc2);
-    const double E1 = t > 0 ? sh_inc2[t - 1] : 0.0;
-    double T1 = sh_cb1;
-    if (T1 > sh_inc2[TH - 1]) T1 = sh_inc2[TH - 1];
-    if (!(T1 > 0)) T1 = DBL_MIN;
-    if (E1 < T1 && T1 <= I1) {
-      double run = E1;
-      int hit = -1, lastpos = -1;
-      double hb = E1, lastbefore = E1;
-      for (int i1 = a1; i1 < b1; i1++) {
-        const double v = (double)lp[i1 * STZ_MODES];
-        const double before = run;
-        run += v;
-        if (v > 0) { lastpos = i1; lastbefore = before; }
-        if (hit < 0 && v > 0 && run >= T1) { hit = i1; hb = before; }
-      }
-      if (hit < 0) { hit = lastpos; hb = lastbefore; }
-      sh_p2 = hit;
-      sh_cb2 = T1 - hb;
-    }
+  long long lv[kLaneChunk];
+  long long S1 = 0;
+#pragma unroll
+  for (int q = 0; q < kLaneChunk; q++) {
+    lv[q] = (q < c2 && a1 + q < n1) ? fix_f(lp[(a1 + q) * STZ_MODES], e) : 0;
+    S1 += lv[q];
   }
-  __syncthreads();
-  const int i1 = sh_p2;
-  if (i1 < 0) {
-    if (t == 0) { *site_out = -1; *mode_out = -1; }
-    return;
+  long long E1, T1;
+  const int L1 = warp_find_i64(S1, T, &E1, &T1);
+  if (lane == 0) *t_lines = gtimer();
+  if (L1 < 0) return -1;
+  int i1 = -1;
+  long long rem2 = 0;
+  if (lane == L1) {
+    long long hb, ha;
+    const int h = chunk_find<kLaneChunk>(lv, E1, T1, &hb, &ha);
+    i1 = h < 0 ? -1 : a1 + h;
+    rem2 = T1 - hb;
   }
-  // level 3: sites of line (i0, i1)
+  i1 = __shfl_sync(FULL, i1, L1);
+  rem2 = (long long)__shfl_sync(FULL, (unsigned long long)rem2, L1);
+  if (i1 < 0) return -1;
+  // level 3: sites of line (i0, i1), rates recomputed with the main pass's chain
   const int n2 = kp.n2;
-  const int ch2 = (n2 + TH - 1) / TH;
-  const int a2 = t * ch2, b2 = min(a2 + ch2, n2);
   const long long base = ((long long)i0 * n1 + i1) * n2;
   const double zero[6] = {0, 0, 0, 0, 0, 0};
-  float locf = 0.f;
-  for (int i2 = a2; i2 < b2; i2++) locf += (float)site_rate<2>(kp, f, zero, 0.0, base + i2, m);
-  const double I2 = block_incl_scan((double)locf, sh_inc2);
-  const double E2 = t > 0 ? sh_inc2[t - 1] : 0.0;
-  double T2 = sh_cb2;
-  if (T2 > sh_inc2[TH - 1]) T2 = sh_inc2[TH - 1];
-  if (!(T2 > 0)) T2 = DBL_MIN;
-  if (E2 < T2 && T2 <= I2) {
-    const float rem = (float)(T2 - E2);
-    float run = 0.f;
-    int hit = -1, lastk = -1;
-    float hb = 0.f, ha = 0.f, lb = 0.f, la = 0.f;
-    for (int i2 = a2; i2 < b2; i2++) {
-      const float r = (float)site_rate<2>(kp, f, zero, 0.0, base + i2, m);
-      const float before = run;
-      run += r;
-      if (r > 0.f) { lastk = i2; lb = before; la = run; }
-      if (hit < 0 && r > 0.f && run >= rem) { hit = i2; hb = before; ha = run; }
-    }
-    if (hit < 0) { hit = lastk; hb = lb; ha = la; }
-    sh_site = hit < 0 ? -1 : base + hit;
-    sh_margin = (double)fminf(rem - hb, ha - rem);
+  const int c3 = (n2 + 31) / 32;
+  const int a2 = lane * c3;
+  long long rv[kLaneChunk];
+  long long S2 = 0;
+#pragma unroll
+  for (int q = 0; q < kLaneChunk; q++) {
+    rv[q] = (q < c3 && a2 + q < n2) ? fix_f((float)site_rate<2>(kp, f, zero, 0.0, base + a2 + q, m), e) : 0;
+    S2 += rv[q];
   }
-  __syncthreads();
-  if (t == 0) {
-    *site_out = sh_site;
-    *mode_out = m;
-    *margin_out = sh_margin;
+  long long E2, T2;
+  const int L2 = warp_find_i64(S2, rem2, &E2, &T2);
+  if (L2 < 0) return -1;
+  long long site = -1, mg = 0;
+  if (lane == L2) {
+    long long hb, ha;
+    const int h = chunk_find<kLaneChunk>(rv, E2, T2, &hb, &ha);
+    site = h < 0 ? -1 : base + a2 + h;
+    mg = min(T2 - hb, ha - T2);
   }
+  site = (long long)__shfl_sync(FULL, (unsigned long long)site, L2);
+  *margin = (long long)__shfl_sync(FULL, (unsigned long long)mg, L2);
+  return site;
 }
 
 // The scalar part of the control block (everything before the generator).
@@ -1555,25 +1618,52 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   if (g->halt) return;
   const unsigned long long t_tail = gtimer();
   __shared__ Ctl sc;
-  __shared__ double sh_inc[TH];
   __shared__ int sh_kind;
-  __shared__ double sh_T, sh_R;
+  __shared__ double sh_R;
   __shared__ long long sh_site;
   __shared__ int sh_mode;
   __shared__ double sh_margin;
+  __shared__ long long sh_p1, sh_rem1, sh_Tint, sh_Rint;
+  __shared__ long long sh_inc_i[TH];
+  __shared__ int sh_emax;
+  __shared__ unsigned long long sh_tl[2];  // search clock: level 1 done, level 2 done
+  // total rate: the FP64 plane sums q = m n0 + i0 in per-thread contiguous
+  // chunks (loaded before the control-block copy so that the two overlap),
+  // turned into the event's fixed point
+  const long long P = (long long)STZ_MODES * kp.n0;
+  const int ch = (int)((P + TH - 1) / TH);
+  const long long q0 = (long long)threadIdx.x * ch, q1 = min(q0 + ch, P);
+  double pv[kLaneChunk];
+#pragma unroll
+  for (int k = 0; k < kLaneChunk; k++) pv[k] = (q0 + k < q1) ? f.psum[q0 + k] : 0.0;
   {
     const uint32_t* a = reinterpret_cast<const uint32_t*>(g);
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
     for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
   }
-  // total rate: the FP64 plane sums, per-thread contiguous chunks (the chunks
-  // the first search level walks again)
-  const long long P = (long long)STZ_MODES * kp.n0;
-  const long long ch = (P + TH - 1) / TH;
-  const long long p0 = threadIdx.x * ch, p1 = min(p0 + ch, P);
-  double S = 0;
-  for (long long p = p0; p < p1; p++) S += f.psum[p];
-  block_incl_scan(S, sh_inc);
+  // largest biased exponent (the bit patterns of non-negative doubles order
+  // like the values; 0x7ff marks a non-finite sum)
+  int emax = 0;
+#pragma unroll
+  for (int k = 0; k < kLaneChunk; k++) emax = max(emax, (int)((unsigned long long)__double_as_longlong(pv[k]) >> 52) & 0x7ff);
+  for (long long q = q0 + kLaneChunk; q < q1; q++)
+    emax = max(emax, (int)((unsigned long long)__double_as_longlong(f.psum[q]) >> 52) & 0x7ff);
+  emax = __reduce_max_sync(FULL, (unsigned)emax);
+  if (threadIdx.x == 0) { sh_emax = 0; sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) atomicMax(&sh_emax, emax);
+  __syncthreads();
+  // every value < 2^(emax - 1022): P of them sum below 2^62
+  const int e = 1084 - clog2(P) - sh_emax;
+  long long iv[kLaneChunk];
+  long long S = 0;
+#pragma unroll
+  for (int k = 0; k < kLaneChunk; k++) {
+    iv[k] = fix_d(pv[k], e);
+    S += iv[k];
+  }
+  for (long long q = q0 + kLaneChunk; q < q1; q++) S += fix_d(f.psum[q], e);
+  const long long Iq = block_incl_scan_i64(S, sh_inc_i);
   const unsigned long long t_sums = gtimer();
   block_twist_if_needed(&g->rng);
   Ctl* c = &sc;
@@ -1581,7 +1671,9 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     c->step++;
     c->has_pend = 0;
     for (int k = 0; k < 6; k++) c->U[k] = 0;
-    const double Rraw = sh_inc[TH - 1];
+    const long long Rint = sh_inc_i[TH - 1];
+    sh_Rint = Rint;
+    const double Rraw = ldexp((double)Rint, -e);
     const double R = Rraw * kp.rate_scale;
     sh_R = Rraw;
     c->total_rate = R;
@@ -1590,36 +1682,32 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       kind = kAthermal;
       c->halt = 1;
       c->halt_reason = kHaltAthermal;
-    } else if (!(R > 0) || !isfinite(R)) {
+    } else if (sh_emax == 0x7ff || Rint <= 0) {
       kind = kNone;
       c->status = STZ_ERR_NAN;
       c->halt = 1;
       c->halt_reason = kHaltError;
-    } else {
-      const double t_kmc = 1 / R;
-      if (t_kmc < kp.dt) {
-        kind = kThermal;
-        c->kstep++;
-        // one draw: the word at mti, tempered (the block refilled the state above)
-        const int i = g->rng.mti;
-        uint32_t y = g->rng.mt[i];
-        g->rng.mti = i + 1;
-        y ^= (y >> 11);
-        y ^= (y << 7) & 0x9d2c5680u;
-        y ^= (y << 15) & 0xefc60000u;
-        y ^= (y >> 18);
-        const double dice = y / 4294967296.0;
-        sh_T = dice * Rraw;
-        c->t_kmc = t_kmc;
-        if (!(dice > 0)) {
-          kind = kNone;
-          c->status = STZ_ERR_NO_EVENT;
-          c->halt = 1;
-          c->halt_reason = kHaltError;
-        }
-      } else {
-        kind = kElastic;
+    } else if (R * kp.dt > 1.0) {  // 1/R < dt without the division
+      kind = kThermal;
+      c->kstep++;
+      // one draw: the word at mti, tempered (the block refilled the state above)
+      const int i = g->rng.mti;
+      uint32_t y = g->rng.mt[i];
+      g->rng.mti = i + 1;
+      y ^= (y >> 11);
+      y ^= (y << 7) & 0x9d2c5680u;
+      y ^= (y << 15) & 0xefc60000u;
+      y ^= (y >> 18);
+      // T = dice R with dice = y / 2^32, in the fixed point
+      sh_Tint = (long long)__umul64hi((unsigned long long)Rint, (unsigned long long)y << 32);
+      if (y == 0) {
+        kind = kNone;
+        c->status = STZ_ERR_NO_EVENT;
+        c->halt = 1;
+        c->halt_reason = kHaltError;
       }
+    } else {
+      kind = kElastic;
     }
     c->neg_count = 0;
     c->step_kind = kind;
@@ -1629,7 +1717,52 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   const unsigned long long t_dec = gtimer();
   const int kind = sh_kind;
   if (kind == kThermal) {
-    search_mixed(kp, f, sh_T, sh_inc, &sh_site, &sh_mode, &sh_margin);
+    // level 1: (mode, plane), by the thread whose chunk holds the target
+    const long long Tq = sh_Tint < 1 ? 1 : sh_Tint;
+    const long long E = threadIdx.x > 0 ? sh_inc_i[threadIdx.x - 1] : 0;
+    if (E < Tq && Tq <= Iq) {
+      long long hb, ha;
+      int h = -1;
+      if (q0 + kLaneChunk >= q1) {
+        h = chunk_find<kLaneChunk>(iv, E, Tq, &hb, &ha);
+      } else {
+        // long chunks (more than kLaneChunk planes per thread): walk in memory
+        long long run = E, lastbefore = E;
+        int lastpos = -1;
+        hb = E;
+        for (long long q = q0; q < q1; q++) {
+          const long long v = fix_d(f.psum[q], e);
+          const long long b0 = run;
+          run += v;
+          if (v > 0) { lastpos = (int)(q - q0); lastbefore = b0; }
+          if (h < 0 && v > 0 && run >= Tq) { h = (int)(q - q0); hb = b0; }
+        }
+        if (h < 0) { h = lastpos; hb = lastbefore; }
+      }
+      sh_p1 = h < 0 ? -1 : q0 + h;
+      sh_rem1 = Tq - hb;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      // levels 2 and 3: warp 0
+      const long long pg = sh_p1;
+      long long site = -1, mg = 0;
+      int m = -1;
+      if (threadIdx.x == 0) sh_tl[0] = gtimer();
+      if (pg >= 0) {
+        m = (int)(pg / kp.n0);
+        const int i0 = (int)(pg - (long long)m * kp.n0);
+        site = search_line_site(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1]);
+      }
+      if (threadIdx.x == 0) {
+        sh_site = site;
+        sh_mode = m;
+        sh_margin = (double)mg;
+      }
+    } else if (threadIdx.x == 32) {
+      // the clock advance, while warp 0 searches
+      c->t_kmc = 1.0 / c->total_rate;
+    }
     __syncthreads();
   }
   const unsigned long long t_search = gtimer();
@@ -1646,7 +1779,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
           c->halt_reason = kHaltError;
           c->step_kind = kNone;
         } else {
-          if (sh_margin < 1e-12 * sh_R) c->near_ties++;
+          if (sh_margin < (double)(sh_Rint >> 40)) c->near_ties++;  // within 2^-40 R of an edge
           float sv[5];
           for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
           const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
@@ -1690,6 +1823,11 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       c->prof_part_ns[1] += t_dec - t_sums;
       c->prof_part_ns[2] += t_search - t_dec;
       c->prof_part_ns[3] += t_end - t_search;
+      if (kind == kThermal) {
+        c->prof_part_ns[4] += sh_tl[0] - t_dec;      // level 1 (mode, plane)
+        c->prof_part_ns[5] += sh_tl[1] - sh_tl[0];   // level 2 (line)
+        c->prof_part_ns[6] += t_search - sh_tl[1];   // level 3 (site)
+      }
       c->prof_n++;
     }
   }

@@ -88,7 +88,8 @@ struct Ctl {
   int ath_count;
   // device-clock phase times of the mixed-form kernel (globaltimer, ns)
   unsigned long long prof_t0, prof_main_ns, prof_tail_ns, prof_n;
-  unsigned long long prof_part_ns[8];  // tail: copy-in+sums, twist+decision, search, commit
+  unsigned long long prof_part_ns[8];  // tail: copy-in+sums, twist+decision, search, commit,
+                                       // search levels (mode, plane), line, site
   MT rng;
 };
 
