@@ -246,6 +246,26 @@ __device__ __forceinline__ void site_coords(const KParams& kp, long long s, int*
   *i0 = (int)q;
 }
 
+// The same header from warp 0: lane k < 5 forms coordinate k, lane 5 the
+// pending transformation (the FP64 steps of the five coordinates run side by
+// side instead of one after another).
+__device__ void set_mixed_head_warp(const KParams& kp, Ctl* c) {
+  const int k = threadIdx.x & 31;
+  MixHead& h = c->head;
+  const double* U = c->U;
+  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, q2 = 1.41421356237309504880;
+  if (k == 0) h.Ud[0] = (float)((U[0] - U[1]) * r2);
+  else if (k == 1) h.Ud[1] = (float)((2.0 * U[2] - U[0] - U[1]) * r6);
+  else if (k < 5) h.Ud[k] = (float)(q2 * U[k + 1]);
+  else if (k == 5) {
+    h.has_pend = c->has_pend;
+    h.pend_mode = c->has_pend ? c->pend_mode : 0;
+    if (c->has_pend) site_coords(kp, c->pend_site, &h.p0, &h.p1, &h.p2);
+    else h.p0 = h.p1 = h.p2 = 0;
+  }
+  __syncwarp();
+}
+
 // The mixed-form main pass's header from U, has_pend, pend_site and
 // pend_mode (one thread; FP64 here, FP32 for the pass).
 __device__ void set_mixed_head(const KParams& kp, Ctl* c) {
@@ -1335,13 +1355,6 @@ __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x, &kp.mdev2[0][0], mix_smem);
 }
 
-// One block per plane: the plane sums the selection reads.
-__global__ void __launch_bounds__(TH) k_mixed_planes(KParams kp, Fields f) {
-  pdl_wait();
-  pdl_release();
-  if (f.ctl->halt) return;
-  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x);
-}
 
 // ------------------------------------------------------- mixed-form tail
 // Lane-parallel scalar algebra on the shared control block: lane k of warp 0
@@ -1636,6 +1649,13 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   double pv[kLaneChunk];
 #pragma unroll
   for (int k = 0; k < kLaneChunk; k++) pv[k] = (q0 + k < q1) ? f.psum[q0 + k] : 0.0;
+  // the generator word the dice will take, unless the state is refilled first
+  int mti0 = 624;
+  uint32_t w0 = 0;
+  if (threadIdx.x == 0) {
+    mti0 = g->rng.mti;
+    if (mti0 < 624) w0 = g->rng.mt[mti0];
+  }
   {
     const uint32_t* a = reinterpret_cast<const uint32_t*>(g);
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
@@ -1691,8 +1711,8 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       kind = kThermal;
       c->kstep++;
       // one draw: the word at mti, tempered (the block refilled the state above)
-      const int i = g->rng.mti;
-      uint32_t y = g->rng.mt[i];
+      const int i = mti0 < 624 ? mti0 : g->rng.mti;
+      uint32_t y = mti0 < 624 ? w0 : g->rng.mt[i];
       g->rng.mti = i + 1;
       y ^= (y >> 11);
       y ^= (y << 7) & 0x9d2c5680u;
@@ -1831,7 +1851,10 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       c->prof_n++;
     }
   }
-  if (threadIdx.x == 0) set_mixed_head(kp, c);
+  if (threadIdx.x < 32) {
+    __syncwarp();
+    set_mixed_head_warp(kp, c);
+  }
   __syncthreads();
   {
     const uint32_t* a = reinterpret_cast<const uint32_t*>(&sc);
@@ -1844,6 +1867,33 @@ __global__ void __launch_bounds__(TH) k_mixed_tail(KParams kp, Fields f, int upd
   pdl_wait();
   pdl_release();
   mixed_tail_body(kp, f, update_only);
+}
+
+// Last of `count` blocks to pass (threadfence pattern; the counter returns to
+// zero for the next launch). That block then sees every block's writes.
+__device__ bool last_of(unsigned* counter, unsigned count) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    is_last = atomicAdd(counter, 1u) == count - 1;
+    if (is_last) *counter = 0;
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// One block per plane forms that plane's sums; the last block to finish runs
+// the selection, commit and loading of the event (one launch after the main
+// pass instead of two).
+__global__ void __launch_bounds__(TH) k_mixed_select(KParams kp, Fields f) {
+  pdl_wait();
+  pdl_release();
+  if (f.ctl->halt) return;
+  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x);
+  if (!last_of(&f.ctl->ticket, gridDim.x)) return;
+  mixed_tail_body(kp, f, 0);
 }
 
 // ------------------------------------------------------------ batches
@@ -1872,23 +1922,21 @@ __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __rest
   mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], mix_smem);
 }
 
-// Plane sums of a batch: block (x, r) sums plane x of replica r.
-__global__ void __launch_bounds__(TH) k_mixed_planes_batched(const BatchDesc* __restrict__ d) {
-  pdl_wait();
-  pdl_release();
-  const BatchDesc& e = d[blockIdx.y];
-  const int n0 = e.kp.n0;
-  if ((int)blockIdx.x >= n0 || e.f.ctl->halt) return;
-  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x);
-}
-
-__global__ void __launch_bounds__(TH) k_mixed_tail_batched(const BatchDesc* __restrict__ d,
-                                                           BatchStatus* __restrict__ st) {
+// Plane sums and selection of a batch: block (x, r) sums plane x of replica
+// r; the last of replica r's blocks runs its selection and reports its state.
+__global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __restrict__ d,
+                                                             BatchStatus* __restrict__ st) {
   __shared__ KParams skp;
   __shared__ Fields sf;
   pdl_wait();
   pdl_release();
-  const int r = blockIdx.x;
+  const int r = blockIdx.y;
+  const BatchDesc& e = d[r];
+  const int n0 = e.kp.n0;
+  Ctl* ctl = e.f.ctl;
+  if ((int)blockIdx.x >= n0 || ctl->halt) return;
+  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x);
+  if (!last_of(&ctl->ticket, (unsigned)n0)) return;
   load_desc(d, r, &skp, &sf);
   mixed_tail_body(skp, sf, 0);
   __syncthreads();
@@ -2044,8 +2092,7 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
                           BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st) {
   mixed_smem_init();
   launch_pdl(k_mixed_batched, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first);
-  launch_pdl(k_mixed_planes_batched, dim3(max_n0, nrep), 0, st, d);
-  launch_pdl(k_mixed_tail_batched, dim3(nrep), 0, st, d, status);
+  launch_pdl(k_mixed_select_batched, dim3(max_n0, nrep), 0, st, d, status);
 }
 
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
@@ -2056,10 +2103,7 @@ void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cuda
 
 void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
-  else {
-    launch_pdl(k_mixed_planes, dim3(kp.n0), 0, st, kp, f);
-    launch_pdl(k_mixed_tail, dim3(1), 0, st, kp, f, update_only);
-  }
+  else launch_pdl(k_mixed_select, dim3(kp.n0), 0, st, kp, f);
 }
 
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {

@@ -18,8 +18,9 @@ void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st);
 // One round of a batch: every replica's update/rate blocks in one grid, then
 // one selection/commit block per replica.
-// Kernels per thermal event of the mixed form: main pass, plane sums, tail.
-constexpr int kMixedLaunches = 3;
+// Kernels per thermal event of the mixed form: main pass, plane sums with the
+// selection in their last block.
+constexpr int kMixedLaunches = 2;
 void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
                           BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st);
 // Resident blocks per SM of the mixed-form kernel (occupancy query).
