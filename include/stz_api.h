@@ -261,6 +261,10 @@ int stz_get_scalars(stz_ctx* ctx, stz_scalars* out);
 int stz_get_events(stz_ctx* ctx, int64_t first, stz_event* out, int64_t cap, int64_t* n);
 int stz_get_field(stz_ctx* ctx, int32_t which, int32_t comp, double* host, int64_t count);
 int stz_set_field(stz_ctx* ctx, int32_t which, int32_t comp, const double* host, int64_t count);
+/* Sets the mean strain EpsAvg (Voigt order, tensor shear; the first 3 in 2D)
+ * that the next solve applies: the host assignment of EpsAvg before the first
+ * solve of bmg.c:114, passed to the device. */
+int stz_set_mean_strain(stz_ctx* ctx, const double* eps_avg);
 int stz_elastic_energy(stz_ctx* ctx, double* out);
 
 /* ---- timing and accounting (for benchmarks) ------------------------------ */

@@ -90,6 +90,7 @@ def load_library(path=None):
     lib.stz_get_events.argtypes = [vp, C.c_int64, vp, C.c_int64, C.POINTER(C.c_int64)]
     lib.stz_get_field.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64]
     lib.stz_set_field.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64]
+    lib.stz_set_mean_strain.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_elastic_energy.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_sync.argtypes = [vp]
     lib.stz_timer_start.argtypes = [vp]
@@ -203,6 +204,11 @@ class Engine:
         v = np.ascontiguousarray(values, dtype=np.float64)
         _check(self.lib.stz_set_field(self.h, which, comp, v.ctypes.data, self.N))
 
+
+    def set_mean_strain(self, eps_avg):
+        """EpsAvg (Voigt, tensor shear) applied by the next solve."""
+        v = (C.c_double * 6)(*(list(eps_avg) + [0.0] * (6 - len(eps_avg))))
+        _check(self.lib.stz_set_mean_strain(self.h, v))
     def elastic_energy(self):
         e = C.c_double()
         _check(self.lib.stz_elastic_energy(self.h, C.byref(e)))

@@ -658,7 +658,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
                   f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.psum, f.spec, f.ktab, f.log,
-                  f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf};
+                  f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fft) {
@@ -822,12 +822,11 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
   const long long N = c->kp.N;
   if (which == STZ_FIELD_Q) {
     if (comp < 0 || comp >= STZ_MODES) return STZ_ERR_INVALID;
-    double* tmp = nullptr;
-    if (dalloc(&tmp, (size_t)N)) return STZ_ERR_NOMEM;
-    launch_q_mode(c->kp, c->f, comp, tmp, c->stream);
-    cudaMemcpyAsync(host, tmp, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
-    cudaStreamSynchronize(c->stream);
-    cudaFree(tmp);
+    // a persistent buffer: the reference-style driver reads every mode each step
+    if (!c->qbuf && dalloc(&c->qbuf, (size_t)N)) return STZ_ERR_NOMEM;
+    launch_q_mode(c->kp, c->f, comp, c->qbuf, c->stream);
+    CK(cudaMemcpyAsync(host, c->qbuf, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return STZ_OK;
   }
   if (which == STZ_FIELD_SDEV) {
@@ -873,6 +872,17 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
     sync_ctl(c);
     for (long long s = 0; s < N; s++) host[s] += c->host_ctl.u[comp];
   }
+  return STZ_OK;
+}
+
+extern "C" int stz_set_mean_strain(stz_ctx* c, const double* eps_avg) {
+  if (!c || !eps_avg) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  int st = sync_ctl(c);
+  if (st) return st;
+  for (int k = 0; k < c->kp.nc; k++) c->host_ctl.eps_avg[k] = eps_avg[k];
+  CK(cudaMemcpyAsync(c->f.ctl->eps_avg, c->host_ctl.eps_avg, sizeof(double) * 6, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return STZ_OK;
 }
 

@@ -1,0 +1,457 @@
+/* refapi.c -- the reference's own entry points on the GB300 engine.
+ *
+ * A drop-in for the reference's init.c, elastic.c, evolution.c and io.c in
+ * the 2D model: compiled against the user's bmg.h / my_fft.h / bmgFlags.h
+ * (the grid size NX x NY, the flags and the global state come from there),
+ * it defines the functions the reference's main (bmg.c) calls, with the same
+ * names and signatures (bmg.h:149-152, 216-232, 295-311, 329, 352, 375), and
+ * runs them on one GB300 through the engine's C ABI (stz_api.h). The
+ * reference's main links against it unchanged.
+ *
+ * State. The device holds the simulation; the globals of bmg.h are host
+ * mirrors, filled where the reference's main reads them:
+ *   ActEnergy          Q[m] for every mode (main scans it for Q < 0)
+ *   KMC, athermal      totime, EpsAvg, Stress, kstep/astep/estep after the step
+ *   solvers            Sigma, Stress, EpsAvg (and TotEps = C^-1:Sigma + Eps0)
+ *   RecordPrep         Eps0, Sigma, then EqStrain / EqStress (io.c:260-273)
+ *   Energy_Init/DStrain Q0, Q1 (initial copy), DEps0
+ * A host write to EpsAvg before a solve is passed to the device; other host
+ * writes to mirrors are not (the device state stays authoritative).
+ *
+ * The KMC step of the engine takes the same branch as the reference's main
+ * (athermal when some Q < 0, else thermal or elastic), so KMC() and
+ * athermal_plasticity() both advance one driver step. The print-time re-solve
+ * (bmg.c:292-295) is the main's own solver call with uflag 2, after the step,
+ * as in the reference: the engine's internal print test is switched off, so
+ * the globals after KMC() hold the state before that re-solve.
+ *
+ * Not provided: the displacement field of the uflag-2 solve (XR is left at
+ * zero), SOC counters (UpdateSOC leaves main's arrays as they are), spatially
+ * varying Lambda/Mu (the solve is homogeneous; a non-uniform field is
+ * reported), MRO maps, residual-stress generation.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "bmg.h"
+#include "my_fft.h"
+#include "stz_api.h"
+
+static stz_ctx* g_ctx = NULL;
+static stz_params g_p;
+static int64_t g_events_seen = 0;  /* events already written to fq */
+static double g_epsavg_dev[3];     /* EpsAvg as last read from the device */
+
+static void fail(const char* what, int code) {
+  fprintf(stderr, "refapi: %s failed (%d): %s\n", what, code, stz_last_error());
+  MPI_Abort(MPI_COMM_WORLD, -1);
+}
+
+static real* alloc_field(void) {
+  real* p = (real*)calloc((size_t)NXY, sizeof(real));
+  if (!p) fail("allocation", STZ_ERR_NOMEM);
+  return p;
+}
+
+/* the engine's scalars into the reference's globals */
+static void pull_scalars(void) {
+  stz_scalars s;
+  int st = stz_get_scalars(g_ctx, &s);
+  if (st) fail("stz_get_scalars", st);
+  totime = s.time;
+  for (int c = 0; c < 3; c++) {
+    EpsAvg[c] = s.eps_avg[c];
+    g_epsavg_dev[c] = s.eps_avg[c];
+    Stress[c] = s.stress[c];
+  }
+  kstep = (int)s.kstep;
+  astep = (int)s.astep;
+  estep = (int)s.estep;
+}
+
+static void pull_field(int which, int comp, real* host) {
+  int st = stz_get_field(g_ctx, which, comp, host, (int64_t)NXY);
+  if (st) fail("stz_get_field", st);
+}
+
+/* ------------------------------------------------------------- set-up */
+
+/* io.c:4-101: the labelled input file, into the reference's globals */
+void ReadInput(FILE* in) {
+  char res[80] = {0};
+  struct {
+    const char* fmt;
+    int want;
+    void* a;
+    void* b;
+  } f[] = {
+      {"Moduli(E, nu):\n%lf %lf\n\n", 2, &E, &nu},
+      {"Stress-free energy barrier:\n%lf\n\n", 1, &Q0amp, NULL},
+      {"Applied strain rate:\n%lf\n\n", 1, &strainrate, NULL},
+      {"Strain increment:\n%lf\n\n", 1, &strainincrement, NULL},
+      {"Random seed:\n%d\n\n", 1, &seed, NULL},
+      {"Random ratio of fluctuation in energy barrier:\n%lf\n\n", 1, &RandomRatio, NULL},
+      {"Print period:\n%d\n\n", 1, &printperiod, NULL},
+      {"End Strain:\n%lf\n\n", 1, &EndStrain, NULL},
+      {"Softening Flag:\n%d\n\n", 1, &softening_FLAG, NULL},
+      {"Relaxation Time:\n%lf\n\n", 1, &RelxTime, NULL},
+      {"Characteristic Xtal shear:\n%lf\n\n", 1, &XtalShear, NULL},
+      {"Barrier for Xtal shear:\n%lf\n\n", 1, &XtalQ0amp, NULL},
+      {"Ratio for generating residual stress:\n%lf\n\n", 1, &ResiRatio, NULL},
+      {"Residual stress data file:\n%79s\n\n", 1, res, NULL},
+      {"Volume fraction of crystal-like MRO:\n%lf\n\n", 1, &xMROFrac, NULL},
+      {"Initialization condition for MRO:\n%d\n\n", 1, &InitMRO, NULL},
+      {"Stress-free energy barrier for crystal-like MRO:\n%lf\n\n", 1, &xQ0amp, NULL},
+  };
+  for (size_t i = 0; i < sizeof(f) / sizeof(f[0]); i++) {
+    int got = f[i].b ? fscanf(in, f[i].fmt, f[i].a, f[i].b) : fscanf(in, f[i].fmt, f[i].a);
+    if (got != f[i].want) fprintf(stderr, "ReadInput: could not match '%.40s'\n", f[i].fmt);
+  }
+  memcpy(ResStressDataFile, res, sizeof(res));
+}
+
+/* init.c:6-75: derived constants (the 2D LOW_T branch and the common part) */
+void Init(void) {
+#if defined(LOW_T)
+  nu *= 2;
+  mu = E / (2 + 2 * nu);
+#elif defined(XTAL_VARIANTS) || defined(HIGH_T_Vit1) || defined(HIGH_T_PdNiP)
+#error "refapi: only the LOW_T material branch of Init() is provided"
+#endif
+  lambda = E * nu / (1 - nu * nu);
+  alpha = (1 + nu) / 2;
+  beta = nu;
+  dt = strainincrement / strainrate;
+  tTemp = 1 / (TRIAL_FREQUENCY * exp(-0.37 / kT));
+  tResi = 1 / (TRIAL_FREQUENCY * exp(-1.80 / kT));
+  PermSoft = 13;
+  PermSoftmro = 20;
+  TempSoft = 39;
+  TempSoftmro = 60;
+  PermSofteningCap = -log(0.6);
+}
+
+/* single device: the whole grid is this rank's slab */
+void FFT_MPI_Init(void) {
+  lnx = NX;
+  lxs = 0;
+  lnyt = NY;
+  lyst = 0;
+  lsize = NXY;
+}
+
+void Rand_Init(void) {}  /* the engine seeds its generator from the input seed */
+void Grad(void) {}       /* wave vectors are formed on the fly by the solve */
+
+/* init.c:225-349: the fields, then the engine context (its initial draws
+ * follow the reference's order: MRO map, Q0, mode eigenstrains) */
+void Alloc(void) {
+  for (int m = 0; m < MODES; m++) {
+    Q[m] = alloc_field();
+    Q0[m] = alloc_field();
+    Q1[m] = alloc_field();
+    Work[m] = alloc_field();
+    for (int c = 0; c < DE; c++) DEps0[m][c] = alloc_field();
+  }
+  for (int c = 0; c < DE; c++) {
+    Eps0[c] = alloc_field();
+    Sigma[c] = alloc_field();
+    TotEps[c] = alloc_field();
+  }
+  XR[0] = alloc_field();
+  XR[1] = alloc_field();
+  tlast = alloc_field();
+  PermSoftening = alloc_field();
+  TempSoftening = alloc_field();
+  Softening = alloc_field();
+#ifdef INHOM_ELAST
+  Lambda = alloc_field();
+  Mu = alloc_field();
+  for (int s = 0; s < NXY; s++) {
+    Lambda[s] = lambda;
+    Mu[s] = mu;
+  }
+#endif
+
+  stz_params_default(&g_p, STZ_MODEL_REF2D);
+  g_p.n[0] = 1;
+  g_p.n[1] = NX;
+  g_p.n[2] = NY;
+  g_p.young = E;
+  g_p.poisson = nu;
+  g_p.mu = mu;
+  g_p.lambda = lambda;
+  g_p.temperature = T__K;
+  g_p.voxel_volume = VOXEL0;
+  g_p.gamma0 = GAMMA0;
+  g_p.q0_mean = Q0amp;
+  g_p.random_ratio = RandomRatio;
+  g_p.strain_rate = strainrate;
+  g_p.strain_increment = strainincrement;
+  g_p.end_strain = EndStrain;
+  /* the reference's main runs the print-time re-solve itself, after the step
+   * (bmg.c:181-295, the uflag-2 solve): the engine's own print test is off */
+  g_p.print_period = 1 << 30;
+  g_p.softening = softening_FLAG;
+  g_p.seed = (uint64_t)(uint32_t)seed;
+  g_p.perm_soft = PermSoft;
+  g_p.temp_soft = TempSoft;
+  g_p.perm_soft_cap = PermSofteningCap;
+  g_p.t_temp = tTemp;
+  g_p.xmro_frac = xMROFrac;
+  g_p.init_mro = InitMRO;
+  g_p.xq0amp = xQ0amp;
+#if defined(TENSION)
+  g_p.loading = STZ_LOAD_TENSION;
+#elif defined(SHEAR)
+  g_p.loading = STZ_LOAD_SHEAR;
+#elif defined(COMPRESSION)
+  g_p.loading = STZ_LOAD_COMPRESSION;
+#endif
+#if defined(SF_LINEAR_FWD)
+  g_p.sf_scheme = STZ_SF_LINEAR_FWD;
+#elif defined(SF_LINEAR_BWD)
+  g_p.sf_scheme = STZ_SF_LINEAR_BWD;
+#elif defined(SF_EVEN)
+  g_p.sf_scheme = STZ_SF_EVEN;
+#elif defined(SF_CUBIC_FWD)
+  g_p.sf_scheme = STZ_SF_CUBIC_FWD;
+#elif defined(SF_GAUSS_FWD)
+  g_p.sf_scheme = STZ_SF_GAUSS_FWD;
+#else
+  g_p.sf_scheme = STZ_SF_SQUARE_FWD;
+#endif
+#ifdef NO_SUBTRACT_ERROR
+  g_p.no_subtract_error = 1;
+#endif
+  g_p.log_capacity = 1 << 16;
+  int st = stz_create(&g_p, &g_ctx);
+  if (st) fail("stz_create", st);
+  g_events_seen = 0;
+}
+
+/* init.c:181-198: the barriers the engine drew, and their initial copy Q1 */
+void Energy_Init(void) {
+  for (int m = 0; m < MODES; m++) {
+    pull_field(STZ_FIELD_DF, m, Q0[m]);
+    memcpy(Q1[m], Q0[m], sizeof(real) * NXY);
+  }
+  pull_field(STZ_FIELD_TLAST, 0, tlast);
+}
+
+/* elastic.c:115-140: the mode eigenstrains the engine drew */
+void DStrain(void) {
+  for (int m = 0; m < MODES; m++)
+    for (int c = 0; c < DE; c++) pull_field(STZ_FIELD_DEPS, m * 3 + c, DEps0[m][c]);
+}
+
+/* ------------------------------------------------------------- solves */
+
+static void solve_into(real** epso, real** sigmao, real* stress, real* epsavg) {
+  int moved = 0;
+  for (int c = 0; c < 3; c++) moved |= epsavg[c] != g_epsavg_dev[c];
+  if (moved) {
+    double e6[6] = {epsavg[0], epsavg[1], epsavg[2], 0, 0, 0};
+    int st = stz_set_mean_strain(g_ctx, e6);
+    if (st) fail("stz_set_mean_strain", st);
+  }
+  int st = stz_solve(g_ctx);
+  if (st) fail("stz_solve", st);
+  for (int c = 0; c < DE; c++) pull_field(STZ_FIELD_SIGMA, c, sigmao[c]);
+  pull_scalars();
+  for (int c = 0; c < 3; c++) {
+    stress[c] = Stress[c];
+    epsavg[c] = EpsAvg[c];
+  }
+  if (epso) {
+    /* total strain = elastic strain (isotropic compliance) + eigenstrain */
+    real* e0[DE];
+    for (int c = 0; c < DE; c++) {
+      e0[c] = alloc_field();
+      pull_field(STZ_FIELD_EPS0, c, e0[c]);
+    }
+    for (int s = 0; s < NXY; s++) {
+      const real s0 = sigmao[0][s], s1 = sigmao[1][s], s2 = sigmao[2][s];
+      const real tr = s0 + s1;
+      epso[0][s] = (s0 - lambda / (2 * lambda + 2 * mu) * tr) / (2 * mu) + e0[0][s];
+      epso[1][s] = (s1 - lambda / (2 * lambda + 2 * mu) * tr) / (2 * mu) + e0[1][s];
+      epso[2][s] = s2 / (2 * mu) + e0[2][s];
+    }
+    for (int c = 0; c < DE; c++) free(e0[c]);
+  }
+}
+
+#ifdef INHOM_ELAST
+/* elastic.c:977-1066 with uniform moduli: one homogeneous solve */
+void InhomogeneousStressSolver(real* Lambdao, real* Muo, real** eps0o, real* epsavg, real lambda_, real mu_,
+                               real** uo, real** epso, real** sigmao, real* stress, int uflag) {
+  static int warned = 0;
+  (void)eps0o;
+  if (!warned) {
+    for (int s = 0; s < NXY; s++)
+      if (Lambdao[s] != lambda_ || Muo[s] != mu_) {
+        fprintf(stderr, "refapi: non-uniform Lambda/Mu; solving with the uniform lambda, mu\n");
+        warned = 1;
+        break;
+      }
+  }
+  solve_into(epso, sigmao, stress, epsavg);
+  if (uflag == 2 && uo)
+    for (int s = 0; s < NXY; s++) uo[0][s] = uo[1][s] = 0.0;
+}
+
+/* elastic.c:779-900 */
+void HomogeneousStressSolver(real lambda_, real mu_, real** eps0o, real* epsavg, real** uo, real** epso,
+                             real** sigmao, real* stress, int uflag) {
+  (void)lambda_;
+  (void)mu_;
+  (void)eps0o;
+  solve_into(epso, sigmao, stress, epsavg);
+  if (uflag == 2 && uo)
+    for (int s = 0; s < NXY; s++) uo[0][s] = uo[1][s] = 0.0;
+}
+#endif
+
+/* elastic.c: the solve on the global fields */
+void HomStressSolver(void) { solve_into(TotEps, Sigma, Stress, EpsAvg); }
+
+/* io.c: displacement field of the print step (not computed: zero) */
+void DispField(real* xr[2]) {
+  solve_into(TotEps, Sigma, Stress, EpsAvg);
+  for (int s = 0; s < NXY; s++) xr[0][s] = xr[1][s] = 0.0;
+}
+
+/* ------------------------------------------------------------- the step */
+
+void SofteningFactor(void) {}  /* computed per site inside the rate pass */
+
+/* init.c:561-690: Q for every mode at the current stress */
+void ActEnergy(int step_) {
+  (void)step_;
+  for (int m = 0; m < MODES; m++) pull_field(STZ_FIELD_Q, m, Q[m]);
+}
+
+/* one driver step on the device, then the globals and the actQ.out records
+ * of evolution.c:243 */
+static void one_step(void) {
+  int st = stz_run(g_ctx, 1, 0);
+  if (st) fail("stz_run", st);
+  pull_scalars();
+  stz_event ev[256];
+  for (;;) {
+    int64_t n = 0;
+    st = stz_get_events(g_ctx, g_events_seen, ev, 256, &n);
+    if (st) fail("stz_get_events", st);
+    if (n <= 0) break;
+    for (int64_t i = 0; i < n; i++)
+      if (ev[i].kind == STZ_EV_THERMAL && rank == 0 && fq) {
+        fprintf(fq, "%d\t%.6e\n", ev[i].mode, ev[i].q);
+        fflush(fq);
+      }
+    g_events_seen += n;
+    if (n < 256) break;
+  }
+}
+
+void KMC(void) { one_step(); }
+void athermal_plasticity(void) { one_step(); }
+
+void UpdateSOC(void) {}
+
+/* elastic.c:533-547 */
+void ElasticEnergy(void) {
+  double e = 0;
+  int st = stz_elastic_energy(g_ctx, &e);
+  if (st) fail("stz_elastic_energy", st);
+  elEnergy = e;
+}
+
+/* ------------------------------------------------------------- records */
+
+/* io.c:260-273 */
+void RecordPrep(void) {
+  for (int c = 0; c < DE; c++) {
+    pull_field(STZ_FIELD_EPS0, c, Eps0[c]);
+    pull_field(STZ_FIELD_SIGMA, c, Sigma[c]);
+  }
+  EqStrain = (real*)malloc((size_t)lsize * sizeof(real));
+  EqStress = (real*)malloc((size_t)lsize * sizeof(real));
+  for (int s = 0; s < NXY; s++) {
+    EqStrain[s] = sqrt(Eps0[0][s] * Eps0[0][s] + Eps0[2][s] * Eps0[2][s]);
+    EqStress[s] = sqrt(Sigma[0][s] * Sigma[0][s] + Sigma[2][s] * Sigma[2][s]);
+  }
+}
+
+void RecordFree(void) {
+  free(EqStrain);
+  free(EqStress);
+  EqStrain = EqStress = NULL;
+}
+
+void ParameterPrint(void) {
+  printf("\nSimulation Geometry:\n");
+  printf("System size:\t[%d x %d]\n", NX, NY);
+  printf("\nMaterial Properties at T=%f\n", (double)T__K);
+  printf("Activation energy barrier amplitude: \t%.3f\n", Q0amp);
+  printf("Young's modulus:\t%.3f\n", E);
+  printf("Shear modulus:\t%.3f\n", mu);
+  printf("Poisson's ratio:\t%.3f\n", nu);
+  printf("# of STZ modes:\t%d\n", MODES);
+  printf("Engine: GB300 (stz_api)\n");
+}
+
+void PrintFlags(void) {
+  printf("Active flags in bmgFlags.h:\n");
+#ifdef TENSION
+  printf("#define TENSION\n");
+#endif
+#ifdef SHEAR
+  printf("#define SHEAR\n");
+#endif
+#ifdef COMPRESSION
+  printf("#define COMPRESSION\n");
+#endif
+#ifdef MICRO_MEMORY
+  printf("#define MICRO_MEMORY\n");
+#endif
+#ifdef INHOM_ELAST
+  printf("#define INHOM_ELAST\n");
+#endif
+#ifdef LOW_T
+  printf("#define LOW_T\n");
+#endif
+}
+
+/* init.c:499-559 */
+void Free(void) {
+  stz_destroy(g_ctx);
+  g_ctx = NULL;
+  for (int m = 0; m < MODES; m++) {
+    free(Q[m]);
+    free(Q0[m]);
+    free(Q1[m]);
+    free(Work[m]);
+    for (int c = 0; c < DE; c++) free(DEps0[m][c]);
+  }
+  for (int c = 0; c < DE; c++) {
+    free(Eps0[c]);
+    free(Sigma[c]);
+    free(TotEps[c]);
+  }
+  free(XR[0]);
+  free(XR[1]);
+  free(tlast);
+  free(PermSoftening);
+  free(TempSoftening);
+  free(Softening);
+#ifdef INHOM_ELAST
+  free(Lambda);
+  free(Mu);
+#endif
+}
+
+/* the engine context behind the reference API (for callers that want the
+ * event log or the handle API alongside it) */
+stz_ctx* stz_refapi_context(void) { return g_ctx; }

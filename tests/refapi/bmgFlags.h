@@ -1,0 +1,16 @@
+/* Test build flags for the reference-API driver: the configuration of the
+ * 2D fixtures (tension loading, square-forward softening directions, the
+ * low-temperature material branch, micro memory, the inhomogeneous-solver
+ * entry point). Written for the tests; the names are the reference's. */
+#ifndef H_BMGFLAGS
+#define H_BMGFLAGS
+#ifdef REFAPI_TEST_SHEAR
+#define SHEAR
+#else
+#define TENSION
+#endif
+#define SF_SQUARE_FWD
+#define LOW_T
+#define MICRO_MEMORY
+#define INHOM_ELAST
+#endif

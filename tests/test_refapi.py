@@ -1,0 +1,99 @@
+"""The reference's own entry points on the GB300 engine (refapi.c).
+
+CPU: the reference's main (bmg.c), compiled unchanged from the reference
+tree against the single-rank stand-ins of oracle/shim, links against the
+drop-in layer and the engine library (only where the reference tree is
+present), and so does the test driver.
+GPU: the test driver, which follows the reference main's call sequence
+(ReadInput ... Alloc, Energy_Init, DStrain, solve, then per step ActEnergy,
+the Q < 0 scan, athermal_plasticity or KMC, ElasticEnergy, the print-time
+RecordPrep / Q0 reset / uflag-2 solve), reproduces the reference's own
+(step, kind, site, mode) sequence of the 32x32 tension fixture and its clock.
+"""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+from metallic_glasses_gb300 import build, configs
+
+REFAPI = os.path.join(ROOT, "metallic_glasses_gb300", "refapi", "refapi.c")
+TESTHDR = os.path.join(ROOT, "tests", "refapi")
+SHIM = os.path.join(ROOT, "oracle", "shim")
+REF_DIR = "/root/reference/Mesoscale simulation STZ model"
+CFLAGS = ["-O2", "-std=gnu11", "-w"]
+
+
+def _lib_args():
+    lib = build.build()
+    d = os.path.dirname(lib)
+    return ["-L", d, "-lstz_gb300", "-Wl,-rpath," + d, "-lm"]
+
+
+def _support():
+    # MPI stand-in (shim.c) and the generator it forwards to
+    return [os.path.join(SHIM, "shim.c"), os.path.join(ROOT, "oracle", "stz_oracle.c")]
+
+
+def build_driver(out, nx=32, ny=32):
+    cmd = (["gcc", *CFLAGS, "-DREFAPI_NX=%d" % nx, "-DREFAPI_NY=%d" % ny, "-I", TESTHDR, "-I", SHIM,
+            "-I", os.path.join(ROOT, "include"), os.path.join(TESTHDR, "driver.c"), REFAPI] + _support() +
+           ["-o", out] + _lib_args())
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return out
+
+
+def test_driver_links(engine_lib):
+    with tempfile.TemporaryDirectory() as d:
+        build_driver(os.path.join(d, "driver"))
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_DIR), reason="reference tree not present")
+def test_reference_main_links_unchanged(engine_lib):
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "bmg_gb300")
+        cmd = (["gcc", *CFLAGS, "-DSTZ_SHIM_NX=32", "-DSTZ_SHIM_NY=32", "-I", SHIM, "-I", REF_DIR,
+                "-I", os.path.join(ROOT, "include"), os.path.join(REF_DIR, "bmg.c"), REFAPI] + _support() +
+               ["-o", out] + _lib_args())
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        assert os.path.getsize(out) > 0
+
+
+@pytest.mark.gpu
+def test_driver_reproduces_reference_events(engine_lib):
+    g = golden("ref2d_32_tension_nosoft_s5")
+    hdr = g["hdr"]
+    with tempfile.TemporaryDirectory() as d:
+        exe = build_driver(os.path.join(d, "driver"))
+        configs.write_input(os.path.join(d, "input"), end="0.5", seed="5", soft="0")
+        env = dict(os.environ, REFAPI_MAX_EVENTS=str(int(hdr[2])))
+        r = subprocess.run([exe], cwd=d, env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
+        ev = np.loadtxt(os.path.join(d, "events.txt"), dtype=np.int64, ndmin=2)
+        steps = np.loadtxt(os.path.join(d, "steps.txt"), ndmin=2)
+        actq = np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2)
+    X = g["X"]
+    assert ev.shape == X.shape
+    for col, name in enumerate(("step", "kind", "site", "mode")):
+        bad = np.nonzero(ev[:, col] != X[:, col])[0]
+        assert bad.size == 0, "first mismatch in %s at row %d" % (name, bad[0])
+    assert len(steps) == int(hdr[1])
+    # the reference's per-step record: (step, kind, time)
+    S = g["S"]
+    assert np.array_equal(steps[:, 0], S[:, 0]) and np.array_equal(steps[:, 1], S[:, 1])
+    assert np.abs(steps[:, 2] - S[:, 2]).max() <= 1e-10 * np.abs(S[:, 2]).max()
+    # EpsAvg and Stress every 10 steps
+    S10 = g["S10"]
+    rows = {int(s): k for k, s in enumerate(steps[:, 0])}
+    for r10 in S10:
+        got = steps[rows[int(r10[0])]]
+        assert np.allclose(got[3:9], r10[3:9], rtol=1e-9, atol=1e-12)
+    # actQ.out: one record per thermal event, the chosen mode
+    thermal = X[X[:, 1] == 0]
+    assert len(actq) == len(thermal)
+    assert np.array_equal(actq[:, 0].astype(np.int64), thermal[:, 3])
