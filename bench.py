@@ -103,21 +103,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(seconds=15.0, grid=GRID):
+def cpu_baseline(seconds=15.0, grid=GRID, threads=None):
     """The CPU oracle (FP64, the reference's full re-solve per event) on all
-    host threads, on a bounded sample of the same workload."""
+    host threads (or `threads`), on a bounded sample of the same workload."""
     from metallic_glasses_gb300 import configs
     from oracle import pyoracle
     p = configs.plain128(n=grid)
     m = pyoracle.Model(p)
-    m.run(max_events=1)  # first event outside the sample (warm caches)
-    t0 = time.perf_counter()
-    n = 0
-    while time.perf_counter() - t0 < seconds and n < 2000:
-        m.run(max_events=1)
-        n += 1
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": UNIT, "cores": pyoracle.threads(), "kind": "port",
+    all_threads = pyoracle.threads()
+    if threads:
+        pyoracle.set_threads(threads)
+    try:
+        m.run(max_events=1)  # first event outside the sample (warm caches)
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < seconds and n < 2000:
+            m.run(max_events=1)
+            n += 1
+        dt = time.perf_counter() - t0
+        cores = pyoracle.threads()
+    finally:
+        pyoracle.set_threads(all_threads)
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": "%d thermal events of the %d^3 FP64 shear configuration (seed 0) after setup, %.1f s" %
                       (n, grid, dt)}
 
@@ -231,6 +238,8 @@ def main():
     k_ms, k_n = eng.kernel_time(steps=200)
     N = n ** 3
     alg_bytes = 44 * N  # read+write 5 FP32 deviatoric stress components, read the FP32 barrier
+    # the full re-solve method's figure (FFT fwd read + spectrum write + read +
+    # stress write of 6 components, FP32): 24 N s bytes per event
     peak, peak_kind = peaks()
     achieved = alg_bytes / (k_ms / 1e3) / 1e9 if k_ms > 0 else None
     tr = traffic_record("k_mixed", n)
@@ -238,7 +247,9 @@ def main():
             "frac": (achieved / peak) if achieved else None, "traffic": tr,
             "kernel": "k_mixed (incremental update + rates + FP64 partial sums + last-block select/commit)",
             "alg_bytes_per_launch": alg_bytes, "launch_ms": k_ms, "launches_timed": k_n,
-            "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
+            "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+            "alg_bytes_full_resolve_per_event": 24 * N * 4,
+            "effective_gbs_full_resolve": 24 * N * 4 * (value / world) / 1e9}
     scf = eng.scalars()
     stress_err = {"rel_l2_worst": scf["stress_err_rms_worst"], "rel_max_worst": scf["stress_err_max_worst"],
                   "resolves": scf["n_resolves"],
@@ -287,6 +298,7 @@ def main():
         line["batched"] = bt
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
+        line["cpu_baseline_1core"] = cpu_baseline(seconds=8.0, grid=n, threads=1)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -143,7 +143,12 @@ typedef struct stz_params {
   int32_t resolve_period;    /* mixed: FP64 full re-solve every this many events (0 = never) */
   int32_t device;            /* CUDA device ordinal */
   int32_t log_capacity;      /* device event-ring entries (0: 1 << 20) */
-  int32_t reserved[7];
+  int32_t mode_seed_set;     /* GLOBAL3D: 1 = the 20 modes come from their own MT19937
+                                stream seeded with mode_seed (replicas sharing one mode
+                                set, each with its own barrier field from seed); 0 = the
+                                modes are the first draws of the seed's stream */
+  int32_t mode_seed;
+  int32_t reserved[5];
 } stz_params;
 
 /* kinds of stz_event */

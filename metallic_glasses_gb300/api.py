@@ -43,7 +43,8 @@ class Params(C.Structure):
         ("xmro_frac", C.c_double), ("xq0amp", C.c_double), ("random_ratio", C.c_double),
         ("init_mro", C.c_int32), ("print_period", C.c_int32), ("seed", C.c_uint64),
         ("precision", C.c_int32), ("solver", C.c_int32), ("resolve_period", C.c_int32), ("device", C.c_int32),
-        ("log_capacity", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("log_capacity", C.c_int32), ("mode_seed_set", C.c_int32), ("mode_seed", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

@@ -118,8 +118,10 @@ def grf256(seed=0, n=256):
 
 def replicas(count=256, seed_base=0, mixed=True, sizes=(32, 48, 64, 96)):
     """Uneven replicas: grid uniform over `sizes`, T uniform in [325, 585] K,
-    engineering strain rate log-uniform in [1e-5, 1e-2] /s, seeds 0..count-1.
-    The draws come from numpy's PCG64 seeded with 2024 + seed_base."""
+    engineering strain rate log-uniform in [1e-5, 1e-2] /s, barrier seeds
+    0..count-1, and the 20 modes of the seed-0 configuration for every
+    replica. The size, T and rate draws come from numpy's PCG64 seeded with
+    2024 + seed_base."""
     rng = np.random.default_rng(2024 + seed_base)
     out = []
     for i in range(count):
@@ -127,6 +129,7 @@ def replicas(count=256, seed_base=0, mixed=True, sizes=(32, 48, 64, 96)):
         T = float(rng.uniform(325.0, 585.0))
         rate = float(10 ** rng.uniform(-5, -2))
         p = shear64(seed_base + i, n, eng_rate=rate)
+        p.mode_seed_set, p.mode_seed = 1, 0
         p.temperature = T
         p.t_temp = 1 / (p.trial_frequency * math.exp(-0.37 / (T * 1.380658e-23 / 1.60217733e-19)))
         if mixed:

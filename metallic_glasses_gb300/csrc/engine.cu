@@ -153,9 +153,12 @@ int init_global3d(stz_ctx* c, MT* rng) {
   const stz_params& p = c->p;
   KParams& kp = c->kp;
   const long long N = kp.N;
+  MT mrng;
+  if (p.mode_seed_set) mt_seed(&mrng, (unsigned long)(uint32_t)p.mode_seed);
+  MT* const modes_rng = p.mode_seed_set ? &mrng : rng;
   for (int m = 0; m < STZ_MODES; m++) {
     double R[3][3];
-    random_rotation(rng, R);
+    random_rotation(modes_rng, R);
     const double a[3] = {R[0][0], R[1][0], R[2][0]};
     const double b[3] = {R[0][1], R[1][1], R[2][1]};
     const double g = 0.5 * p.gamma0;
@@ -209,21 +212,19 @@ void mixed_constants(stz_ctx* c) {
   kp.a_scale = (float)(l2e / kp.kT);
   kp.inv_a_scale = 1.0 / (double)kp.a_scale;
   kp.rate_scale = kp.vt * std::exp(-(double)kp.q_ref / kp.kT);
-  double nmax = 0;
+  // temperature-free mode coordinates (shared by replicas of one mode set at
+  // different temperatures); the stress coordinates carry 1/kT
   for (int m = 0; m < STZ_MODES; m++) {
-    double d[5], n2 = 0;
+    double d[5];
     dev_coords(kp.modes[m], d);
     for (int k = 0; k < 5; k++) {
       kp.mdev_raw[m][k] = (float)d[k];
-      kp.mdev[m][k] = (float)(d[k] * cW * 0.5 * l2e / kp.kT);
-      n2 += (double)kp.mdev[m][k] * kp.mdev[m][k];
+      kp.mdev[m][k] = (float)(d[k] * cW * 0.5 * l2e);
     }
-    nmax = std::max(nmax, std::sqrt(n2));
   }
   for (int j = 0; j < STZ_MODES / 2; j++)
     for (int k = 0; k < 5; k++) kp.mdev2[j][k] = make_float2(kp.mdev[2 * j][k], kp.mdev[2 * j + 1][k]);
-  kp.inv_mdev_norm = (float)(1.0 / std::max(nmax, 1e-300));
-  kp.bound_slack = 1.001f;  // covers FP32 rounding of the bound itself
+  kp.inv_kt = (float)(1.0 / kp.kT);
 }
 
 // ------------------------------------------------------------- solves
@@ -1067,6 +1068,8 @@ struct stz_batch {
   int total_blocks = 0;
   int max_n0 = 1;  // largest plane count (grid x of the plane-sum kernel)
   int max_n2 = 4;  // longest line (shared memory of the batched main kernel)
+  int shared_modes = 0;  // every replica has the same modes (kernel-parameter path)
+  stz::ModeSet modes{};
   cudaGraphExec_t graph = nullptr;
   int graph_rounds = 0;
   int64_t launches = 0;
@@ -1101,8 +1104,8 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
     }
     if (p.log_capacity <= 0) p.log_capacity = 1 << 15;
     stz_ctx* c = nullptr;
-    // batches: four line units per block
-    const int st = stz::create_ctx(&p, &c, 4);
+    // batches: sixteen line units per block
+    const int st = stz::create_ctx(&p, &c, 16);
     if (st) {
       stz_batch_destroy(b);
       return st;
@@ -1122,6 +1125,13 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
     b->min_log_cap = i == 0 ? b->reps[i]->kp.log_cap : std::min<int64_t>(b->min_log_cap, b->reps[i]->kp.log_cap);
   }
   b->total_blocks = (int)blk_rep.size();
+  // one mode set for every replica: the batched kernel takes it as parameters
+  b->shared_modes = 1;
+  for (auto* c : b->reps)
+    b->shared_modes &= std::memcmp(c->kp.mdev2, b->reps[0]->kp.mdev2, sizeof(c->kp.mdev2)) == 0 &&
+                       std::memcmp(c->kp.mdev_raw, b->reps[0]->kp.mdev_raw, sizeof(c->kp.mdev_raw)) == 0;
+  std::memcpy(b->modes.mdev2, b->reps[0]->kp.mdev2, sizeof(b->modes.mdev2));
+  std::memcpy(b->modes.mdev_raw, b->reps[0]->kp.mdev_raw, sizeof(b->modes.mdev_raw));
   b->max_n0 = 1;
   b->max_n2 = 4;
   for (auto* c : b->reps) {
@@ -1157,7 +1167,8 @@ int batch_capture(stz_batch* b, int rounds) {
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < rounds; r++)
     launch_mixed_batched(b->d_desc, b->d_blk_rep, b->d_rep_first, b->total_blocks, b->d_status,
-                         (int)b->reps.size(), b->max_n0, b->max_n2, b->stream);
+                         (int)b->reps.size(), b->max_n0, b->max_n2, b->shared_modes ? &b->modes : nullptr,
+                         b->stream);
   CK(cudaStreamEndCapture(b->stream, &g));
   CK(cudaGraphInstantiate(&b->graph, g, 0));
   cudaGraphDestroy(g);

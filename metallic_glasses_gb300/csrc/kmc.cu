@@ -358,12 +358,13 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
-// Mixed: scaled log2-rate x = log2(e)/kT (q_ref - Q); identical code in the
-// main pass and in the rescan so both see the same bits.
+// Mixed: scaled log2-rate x = log2(e)/kT (q_ref - Q) = a + sum_k (s_k/kT) mdev[m][k]
+// with temperature-free mode coordinates; identical code in the main pass and
+// in the rescan so both see the same bits.
 __device__ __forceinline__ float mx_x(const KParams& kp, const float* sv, float a, int m) {
   float x = a;
 #pragma unroll
-  for (int k = 0; k < 5; k++) x = __fmaf_rn(sv[k], kp.mdev[m][k], x);
+  for (int k = 0; k < 5; k++) x = __fmaf_rn(__fmul_rn(sv[k], kp.inv_kt), kp.mdev[m][k], x);
   return x;
 }
 
@@ -1057,22 +1058,46 @@ __device__ __forceinline__ void mixed_update(const Fields& f, int N32, int s, in
   for (int k = 0; k < 5; k++) f.sdev[k * N32 + s] = sv[k];
 }
 
+// The 20 rates of one site (a lane whose pair partner is past the line).
+__device__ __forceinline__ void mixed_rates1(const float* sa, float aa, float ct, const float2* md, float2* acc2,
+                                             float* xma) {
+  float mx = -INFINITY;
+  float ta[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) ta[k] = __fmul_rn(sa[k], ct);
+#pragma unroll
+  for (int j = 0; j < STZ_MODES / 2; j++) {
+    float2 xa = make_float2(aa, aa);
+#pragma unroll
+    for (int k = 0; k < 5; k++) xa = __ffma2_rn(make_float2(ta[k], ta[k]), md[5 * j + k], xa);
+    acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
+    mx = fmaxf(mx, fmaxf(xa.x, xa.y));
+  }
+  *xma = mx;
+}
+
 // The 20 rates of two sites (b may be absent), packed two modes per FP32x2
-// FMA; each lane of a pair is the scalar chain of mx_x, so the search sees the
-// same bits. One load of each mode coefficient serves both sites. Returns the
+// FMA after scaling the stress coordinates by ct = 1/kT; each lane of a pair
+// is the scalar chain of mx_x, so the search sees the same bits. One load of each mode coefficient serves both sites. Returns the
 // largest argument of site a in *xma and of site b in *xmb (an argument above
 // q_ref a_scale is a negative barrier, the athermal trigger).
-__device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const float* sb, float ab, bool hb,
+__device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const float* sb, float ab, bool hb, float ct,
                                              const float2* md, float2* acc2, float* xma, float* xmb) {
   float2 mx = make_float2(-INFINITY, -INFINITY);
+  float ta[5], tb[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    ta[k] = __fmul_rn(sa[k], ct);
+    tb[k] = __fmul_rn(sb[k], ct);
+  }
 #pragma unroll
   for (int j = 0; j < STZ_MODES / 2; j++) {
     float2 xa = make_float2(aa, aa), xb = make_float2(ab, ab);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       const float2 c = md[5 * j + k];
-      xa = __ffma2_rn(make_float2(sa[k], sa[k]), c, xa);
-      xb = __ffma2_rn(make_float2(sb[k], sb[k]), c, xb);
+      xa = __ffma2_rn(make_float2(ta[k], ta[k]), c, xa);
+      xb = __ffma2_rn(make_float2(tb[k], tb[k]), c, xb);
     }
     acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
     if (hb) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xb.x), ex2_approx(xb.y)));
@@ -1194,8 +1219,13 @@ __device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, i
       const float dFa = stage[5 * n2 + i2];
       const float dFb = hb ? stage[5 * n2 + i2b] : dFa;
       const float aa = (kp.q_ref - dFa) * kp.a_scale, ab = (kp.q_ref - dFb) * kp.a_scale;
-      float xma, xmb;
-      mixed_rates2(sa, aa, sb, ab, hb, md, acc2, &xma, &xmb);
+      float xma, xmb = -INFINITY;
+      // lines of 32 and the last third of 96: no lane has a partner. The vote
+      // is among the lanes executing here (lines shorter than 32 leave some
+      // outside the loop); a lane takes the single-site path only when no
+      // lane of its group has a partner, so the result is the same either way.
+      if (__any_sync(__activemask(), hb)) mixed_rates2(sa, aa, sb, ab, hb, kp.inv_kt, md, acc2, &xma, &xmb);
+      else mixed_rates1(sa, aa, kp.inv_kt, md, acc2, &xma);
       neg |= (xma > thr_neg || (hb && xmb > thr_neg)) ? 1u : 0u;
     }
   }
@@ -1256,7 +1286,7 @@ __device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, do
 // takes units b, b + nblk, ... and its warps run through them independently.
 template <int UPDATE_ONLY>
 __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b, const float2* md,
-                                                float* mix_smem) {
+                                                const float (*mraw)[5], float* mix_smem) {
   __shared__ __align__(8) unsigned long long mbar[TH / 32][2];
   Ctl* ctl = f.ctl;
   // the header and the halt flag in independent loads
@@ -1274,7 +1304,7 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   float de[5] = {0, 0, 0, 0, 0};
   if (hp) {
 #pragma unroll
-    for (int k = 0; k < 5; k++) de[k] = kp.mdev_raw[pm][k];
+    for (int k = 0; k < 5; k++) de[k] = mraw[pm][k];
   }
   const float thr_neg = kp.q_ref * kp.a_scale;
   unsigned neg = 0;
@@ -1352,7 +1382,7 @@ template <int UPDATE_ONLY>
 __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   extern __shared__ __align__(128) float mix_smem[];
   pdl_wait();
-  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x, &kp.mdev2[0][0], mix_smem);
+  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x, &kp.mdev2[0][0], kp.mdev_raw, mix_smem);
 }
 
 
@@ -1910,16 +1940,24 @@ __device__ __forceinline__ void load_desc(const BatchDesc* d, int r, KParams* sk
   __syncthreads();
 }
 
+// SHARED: every replica has the same modes, passed as kernel parameters
+// (constant-bank operands) instead of being read from each block's copy of
+// its replica's constants in shared memory.
+template <int SHARED>
 __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __restrict__ d,
                                                           const int* __restrict__ blk_rep,
-                                                          const int* __restrict__ rep_first) {
+                                                          const int* __restrict__ rep_first, ModeSet ms) {
   __shared__ KParams skp;
   __shared__ Fields sf;
   pdl_wait();
   const int r = blk_rep[blockIdx.x];
+  if (d[r].f.ctl->halt) return;  // a halted replica's blocks skip the copy
   load_desc(d, r, &skp, &sf);
   extern __shared__ __align__(128) float mix_smem[];
-  mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], mix_smem);
+  if (SHARED)
+    mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &ms.mdev2[0][0], ms.mdev_raw, mix_smem);
+  else
+    mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
 }
 
 // Plane sums and selection of a batch: block (x, r) sums plane x of replica
@@ -2052,7 +2090,8 @@ static void mixed_smem_init() {
   };
   raise((const void*)k_mixed<0>);
   raise((const void*)k_mixed<1>);
-  raise((const void*)k_mixed_batched);
+  raise((const void*)k_mixed_batched<0>);
+  raise((const void*)k_mixed_batched<1>);
 }
 
 size_t mixed_smem(int n2) { return mix_smem_bytes(n2); }
@@ -2089,9 +2128,14 @@ void launch_pdl(void (*kern)(A...), dim3 grid, size_t smem, cudaStream_t st, A..
 }  // namespace
 
 void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st) {
+                          BatchStatus* status, int nrep, int max_n0, int max_n2, const ModeSet* shared,
+                          cudaStream_t st) {
   mixed_smem_init();
-  launch_pdl(k_mixed_batched, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first);
+  if (shared)
+    launch_pdl(k_mixed_batched<1>, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first, *shared);
+  else
+    launch_pdl(k_mixed_batched<0>, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first,
+               ModeSet{});
   launch_pdl(k_mixed_select_batched, dim3(max_n0, nrep), 0, st, d, status);
 }
 

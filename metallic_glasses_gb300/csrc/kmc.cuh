@@ -22,7 +22,8 @@ void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStrea
 // selection in their last block.
 constexpr int kMixedLaunches = 2;
 void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, int max_n0, int max_n2, cudaStream_t st);
+                          BatchStatus* status, int nrep, int max_n0, int max_n2, const ModeSet* shared,
+                          cudaStream_t st);
 // Resident blocks per SM of the mixed-form kernel (occupancy query).
 int mixed_blocks_per_sm(int n2);
 // Dynamic shared memory of one mixed-form main block for lines of n2 sites.

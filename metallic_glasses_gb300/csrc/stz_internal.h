@@ -139,10 +139,11 @@ struct KParams {
   double applied[6];
   double modes[STZ_MODES][6];      // GLOBAL3D mode table (Voigt, tensor shear)
   // mixed form
-  float mdev[STZ_MODES][5];        // mode deviatoric coords * (c/2) * log2(e)/kT
+  float mdev[STZ_MODES][5];        // mode deviatoric coords * (c/2) * log2(e) (c: eV per GPa
+                                   // and unit strain); the rate argument is
+                                   // a + sum_k (s_k * inv_kt) mdev[m][k]
   float2 mdev2[STZ_MODES / 2][5];  // the same, modes paired (2j, 2j+1) for packed FMA
-  float inv_mdev_norm;             // 1 / max_m |mdev[m]|
-  float bound_slack;               // > 1: margin of the |W| bound test
+  float inv_kt;                    // 1 / kT (eV): the replica's scale of the stress coordinates
   float a_scale;                   // log2(e)/kT
   float q_ref;                     // reference barrier of the scaled rates
   double rate_scale;               // vt * exp(-q_ref/kT): true rate per scaled unit
@@ -154,6 +155,12 @@ struct KParams {
 };
 
 // One replica of a batch as the batched kernels see it.
+// The mode matrices of the mixed form, for a batch whose replicas share them.
+struct ModeSet {
+  float2 mdev2[STZ_MODES / 2][5];
+  float mdev_raw[STZ_MODES][5];
+};
+
 struct BatchDesc {
   KParams kp;
   Fields f;

@@ -46,6 +46,8 @@ def lib():
         L.or_ran_gaussian.argtypes = [vp, C.c_double]
         L.or_ran_gaussian.restype = C.c_double
         L.or_threads.restype = C.c_int
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_set_threads.restype = None
         _lib = L
     return _lib
 
@@ -136,3 +138,8 @@ class Model:
 
 def threads():
     return lib().or_threads()
+
+
+def set_threads(n):
+    """Threads of the oracle's parallel loops from now on."""
+    lib().or_set_threads(int(n))

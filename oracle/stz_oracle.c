@@ -198,6 +198,14 @@ int or_fft3(int n0, int n1, int n2, double* data, int sign) {
   return STZ_OK;
 }
 
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 int or_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
@@ -344,10 +352,14 @@ static void random_rotation(or_rng* r, double R[3][3]) {
 static int gen_dF(or_model* m);
 
 static int init_global3d(or_model* m) {
-  /* 20 global modes: eps* = gamma0/2 (a b^T + b a^T), a = R e_x, b = R e_y. */
+  /* 20 global modes: eps* = gamma0/2 (a b^T + b a^T), a = R e_x, b = R e_y,
+   * from the main stream or from their own stream (mode_seed_set) */
+  or_rng mrng;
+  if (m->p.mode_seed_set) or_rng_seed(&mrng, (unsigned long)(uint32_t)m->p.mode_seed);
+  or_rng* const modes_rng = m->p.mode_seed_set ? &mrng : &m->rng;
   for (int mo = 0; mo < STZ_MODES; mo++) {
     double R[3][3];
-    random_rotation(&m->rng, R);
+    random_rotation(modes_rng, R);
     double a[3] = {R[0][0], R[1][0], R[2][0]};
     double b[3] = {R[0][1], R[1][1], R[2][1]};
     double g = 0.5 * m->p.gamma0;

@@ -59,6 +59,7 @@ int  or_set_field(or_model* m, int which, int comp, const double* in, int64_t co
 int  or_elastic_energy(or_model* m, double* out);
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int  or_threads(void);
+void or_set_threads(int n);
 
 #ifdef __cplusplus
 }
