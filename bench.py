@@ -290,11 +290,12 @@ def main():
     if not args.no_batch:
         # independent replicas of uneven sizes advanced together vs one at a time
         from metallic_glasses_gb300 import timing
-        bt = timing.batch(args.batch_replicas, events=128, alone=16)
+        bt = timing.batch(args.batch_replicas, events=128)
         bt["workload"] = ("%d replicas, grids uniform over 32^3/48^3/64^3/96^3, T uniform in [325, 585] K, "
-                          "strain rate log-uniform in [1e-5, 1e-2] /s, seeds 0..%d; 128 thermal events each; "
-                          "one at a time = the first 16 replicas, each alone through stz_run"
+                          "strain rate log-uniform in [1e-5, 1e-2] /s, barrier seeds 0..%d, the seed-0 mode set; "
+                          "128 thermal events each; one at a time = every replica alone through stz_run"
                           % (args.batch_replicas, args.batch_replicas - 1))
+        bt["ratio"] = bt["batched_events_per_s"] / bt["alone_events_per_s"]
         line["batched"] = bt
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)

@@ -518,6 +518,9 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
     const int kt0 = kp.n0 / 2 + 1, kt1 = kp.n1 / 2 + 1;
     kp.mx_c1 = (kt1 + 1) / 2;
     kp.mx_units = kt0 * kp.mx_c1;
+    // u / mx_c1 as a multiply-high: exact while u * mx_c1 < 2^32 (u < 2^22
+    // units for extents up to 512, mx_c1 <= 129)
+    kp.c1_magic = (unsigned)((((uint64_t)1 << 32) + (uint64_t)kp.mx_c1 - 1) / (uint64_t)kp.mx_c1);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device);
     const long long wave = (long long)std::max(sms, 1) * mixed_blocks_per_sm(kp.n2);

@@ -1010,10 +1010,25 @@ struct LineOf {
   int i0, i1, valid;
 };
 
+// The per-replica constants and field pointers of the main pass, copied to
+// registers at the block's start: read through the KParams / Fields in shared
+// memory of the batched kernel, every use would be a reload after each
+// shared-memory store of the loop.
+struct MixK {
+  int n0, n1, n2, kt1, kt2, mx_c1, mx_units, nblk;
+  unsigned c1_magic;  // ceil(2^32 / mx_c1): u / mx_c1 = umulhi(u, c1_magic) for u < 2^22
+  long long N;
+  float q_ref, a_scale, inv_kt;
+  float* sdev;
+  const float* dF32;
+  const float* ktab;
+  float* lsum;
+};
+
 __device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-__device__ __forceinline__ LineOf unit_line(const KParams& kp, int u, int w, int p0, int p1) {
-  const int d0 = u / kp.mx_c1, c = u - d0 * kp.mx_c1;
+__device__ __forceinline__ LineOf unit_line(const MixK& kp, int u, int w, int p0, int p1) {
+  const int d0 = (int)__umulhi((unsigned)u, kp.c1_magic), c = u - d0 * kp.mx_c1;
   const int s0 = w & 1, s1 = w >> 2;
   const int d1 = 2 * c + ((w >> 1) & 1);
   LineOf L;
@@ -1029,7 +1044,7 @@ __device__ __forceinline__ LineOf unit_line(const KParams& kp, int u, int w, int
 // coordinates and leaves them in sv. dl holds
 // de (5), then the sign of coordinate 2 (y z) and the z and y flips that,
 // times the site's x flip sx, give the signs of coordinates 3 (x z) and 4 (x y).
-__device__ __forceinline__ void mixed_update(const Fields& f, int N32, int s, int hp, const float4* rec, float sx,
+__device__ __forceinline__ void mixed_update(float* sdev, int N32, int s, int hp, const float4* rec, float sx,
                                              const float* dl, const float* Ud, float* sv) {
   if (hp) {
     const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2), q3 = __ldg(rec + 3);
@@ -1055,7 +1070,7 @@ __device__ __forceinline__ void mixed_update(const Fields& f, int N32, int s, in
     for (int k = 0; k < 5; k++) sv[k] += Ud[k];
   }
 #pragma unroll
-  for (int k = 0; k < 5; k++) f.sdev[k * N32 + s] = sv[k];
+  for (int k = 0; k < 5; k++) sdev[k * N32 + s] = sv[k];
 }
 
 // The 20 rates of one site (a lane whose pair partner is past the line).
@@ -1158,8 +1173,7 @@ __host__ __device__ __forceinline__ size_t mix_smem_bytes(int n2) {
 }
 
 template <int UPDATE_ONLY>
-__device__ __forceinline__ void issue_line(const KParams& kp, const Fields& f, int i0, int i1, float* stage,
-                                           unsigned long long* bar) {
+__device__ __forceinline__ void issue_line(const MixK& kp, int i0, int i1, float* stage, unsigned long long* bar) {
   const long long base = ((long long)i0 * kp.n1 + i1) * kp.n2;
   const unsigned bytes = (unsigned)kp.n2 * 4u;
   // the generic-proxy reads and writes of this stage are done (syncwarp by
@@ -1167,14 +1181,14 @@ __device__ __forceinline__ void issue_line(const KParams& kp, const Fields& f, i
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   mbar_expect_tx(bar, (UPDATE_ONLY ? 5u : 6u) * bytes);
 #pragma unroll
-  for (int k = 0; k < 5; k++) bulk_g2s(stage + k * kp.n2, f.sdev + (long long)k * kp.N + base, bytes, bar);
-  if (!UPDATE_ONLY) bulk_g2s(stage + 5 * kp.n2, f.dF32 + base, bytes, bar);
+  for (int k = 0; k < 5; k++) bulk_g2s(stage + k * kp.n2, kp.sdev + (long long)k * kp.N + base, bytes, bar);
+  if (!UPDATE_ONLY) bulk_g2s(stage + 5 * kp.n2, kp.dF32 + base, bytes, bar);
 }
 
 // One line (i0, i1) by one warp from its staged inputs: update every site,
 // and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2.
 template <int UPDATE_ONLY>
-__device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, int N32, int hp, int i0, int i1,
+__device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int i0, int i1,
                                            int p0, int p1, int p2, const float* de, const float* Ud,
                                            const float2* md, const float* stage, float2* acc2, unsigned& neg,
                                            float thr_neg) {
@@ -1183,7 +1197,7 @@ __device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, i
   int fz, fy;
   const int d0 = fold(i0 - p0, kp.n0, &fz);
   const int d1 = fold(i1 - p1, kp.n1, &fy);
-  const float4* row = reinterpret_cast<const float4*>(f.ktab) + 4LL * ((d0 * kp.kt1 + d1) * kp.kt2);
+  const float4* row = reinterpret_cast<const float4*>(kp.ktab) + 4LL * ((d0 * kp.kt1 + d1) * kp.kt2);
   // per-line signs: coordinate 2 takes y z, 3 takes x z, 4 takes x y; the x
   // flip varies along the line and is applied per site
   const float sy = fy ? -1.f : 1.f, sz = fz ? -1.f : 1.f;
@@ -1203,14 +1217,14 @@ __device__ __forceinline__ void mixed_line(const KParams& kp, const Fields& f, i
       const int d2 = fold(i2 - p2, n2, &fx);
 #pragma unroll
       for (int k = 0; k < 5; k++) sa[k] = stage[k * n2 + i2];
-      mixed_update(f, N32, base + i2, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sa);
+      mixed_update(kp.sdev, N32, base + i2, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sa);
     }
     if (hb) {
       int fx;
       const int d2 = fold(i2b - p2, n2, &fx);
 #pragma unroll
       for (int k = 0; k < 5; k++) sb[k] = stage[k * n2 + i2b];
-      mixed_update(f, N32, base + i2b, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sb);
+      mixed_update(kp.sdev, N32, base + i2b, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sb);
     } else {
 #pragma unroll
       for (int k = 0; k < 5; k++) sb[k] = sa[k];
@@ -1306,11 +1320,13 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
 #pragma unroll
     for (int k = 0; k < 5; k++) de[k] = mraw[pm][k];
   }
-  const float thr_neg = kp.q_ref * kp.a_scale;
+  const MixK k = {kp.n0, kp.n1,    kp.n2,      kp.kt1,    kp.kt2, kp.mx_c1, kp.mx_units, kp.nblk, kp.c1_magic,
+                  kp.N,  kp.q_ref, kp.a_scale, kp.inv_kt, f.sdev, f.dF32,   f.ktab,      f.lsum};
+  const float thr_neg = k.q_ref * k.a_scale;
   unsigned neg = 0;
-  const int N32 = (int)kp.N;
+  const int N32 = (int)k.N;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sf = mix_stage_floats(kp.n2);
+  const int sf = mix_stage_floats(k.n2);
   float* stages = mix_smem + (size_t)w * 2 * sf;
   unsigned long long* bar = &mbar[w][0];
   if (lane == 0) {
@@ -1323,22 +1339,22 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   // warp idles); line j lives in stage j & 1
   int u = b;
   LineOf L{0, 0, 0};
-  for (; u < kp.mx_units; u += kp.nblk)
-    if ((L = unit_line(kp, u, w, p0, p1)).valid) break;
-  if (u < kp.mx_units && lane == 0) issue_line<UPDATE_ONLY>(kp, f, L.i0, L.i1, stages, &bar[0]);
-  unsigned pending = u < kp.mx_units ? 1u : 0u;  // stages with a copy in flight
+  for (; u < k.mx_units; u += k.nblk)
+    if ((L = unit_line(k, u, w, p0, p1)).valid) break;
+  if (u < k.mx_units && lane == 0) issue_line<UPDATE_ONLY>(k, L.i0, L.i1, stages, &bar[0]);
+  unsigned pending = u < k.mx_units ? 1u : 0u;  // stages with a copy in flight
   unsigned ppar = 0;                                // bit k: parity the copy of stage k completes
   bool timed_out = false;
-  for (int j = 0; u < kp.mx_units; j++) {
-    int un = u + kp.nblk;
+  for (int j = 0; u < k.mx_units; j++) {
+    int un = u + k.nblk;
     LineOf Ln{0, 0, 0};
-    for (; un < kp.mx_units; un += kp.nblk)
-      if ((Ln = unit_line(kp, un, w, p0, p1)).valid) break;
+    for (; un < k.mx_units; un += k.nblk)
+      if ((Ln = unit_line(k, un, w, p0, p1)).valid) break;
     float* cur = stages + (j & 1) * sf;
     float* nxt = stages + ((j + 1) & 1) * sf;
     __syncwarp();
-    if (un < kp.mx_units) {
-      if (lane == 0) issue_line<UPDATE_ONLY>(kp, f, Ln.i0, Ln.i1, nxt, &bar[(j + 1) & 1]);
+    if (un < k.mx_units) {
+      if (lane == 0) issue_line<UPDATE_ONLY>(k, Ln.i0, Ln.i1, nxt, &bar[(j + 1) & 1]);
       pending |= 1u << ((j + 1) & 1);
       ppar = (ppar & ~(1u << ((j + 1) & 1))) | ((((unsigned)(j + 1) >> 1) & 1u) << ((j + 1) & 1));
     }
@@ -1351,12 +1367,12 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
     float2 acc2[STZ_MODES / 2];
 #pragma unroll
     for (int q = 0; q < STZ_MODES / 2; q++) acc2[q] = make_float2(0.f, 0.f);
-    mixed_line<UPDATE_ONLY>(kp, f, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
+    mixed_line<UPDATE_ONLY>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
     if (!UPDATE_ONLY) {
       // the consumed stage holds the transpose
       __syncwarp();
       line_sums(acc2, reinterpret_cast<float(*)[STZ_MODES]>(cur),
-                f.lsum + ((long long)L.i0 * kp.n1 + L.i1) * STZ_MODES);
+                k.lsum + ((long long)L.i0 * k.n1 + L.i1) * STZ_MODES);
     }
     u = un;
     L = Ln;

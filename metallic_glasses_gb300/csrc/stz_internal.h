@@ -128,6 +128,7 @@ struct KParams {
   int nblk, bsites;          // rate kernel: blocks and sites per block
   int ngroups;               // groups of kGroup blocks
   int mx_c1, mx_units;       // mixed form: d1 chunks per d0, units (kt0 * mx_c1)
+  unsigned c1_magic;         // ceil(2^32 / mx_c1), for the division of unit indices
   int adv_q2, adv_r2;        // kRateThreads sites = adv_q2 rows of n2 plus adv_r2 sites
   int fast_inv;              // mixed form: precomputed compliance coefficients
   double inv_2mu, inv_lam_coef, invN, inv_a_scale;

@@ -7,8 +7,8 @@
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
 only, 2: a whole event including selection). `batch` advances independent
 replicas (grid sizes 32^3..96^3, temperatures and strain rates drawn from the
-seed) together in one batch, then the first few of them one at a time, and
-prints both aggregate rates (one at a time = each replica in its own
+seed) together in one batch, then the same replicas one at a time, and prints
+both aggregate rates (one at a time = each replica in its own
 context through stz_run, the single-run path). Both are the commands the ncu summaries are
 taken on.
 """
@@ -26,7 +26,7 @@ def kernel(grid, which, steps, resolve_period=0):
     return {"grid": grid, "which": which, "launch_ms": ms, "launches": n}
 
 
-def batch(replicas, events, alone=16, seed0=0):
+def batch(replicas, events, alone=None, seed0=0):
     """Aggregate replica-events/s batched vs the same replicas one at a time.
 
     Every replica advances `events` thermal events in both arms (the warm-up
@@ -44,7 +44,9 @@ def batch(replicas, events, alone=16, seed0=0):
     done = sum(r.scalars()["kstep"] for r in b.replicas) - k0
     sites = sum(p.n[0] * p.n[1] * p.n[2] for p in ps)
     b.close()
-    n1 = min(alone, replicas)
+    # one at a time: every replica of the batch (alone=None) or the first
+    # `alone` of them
+    n1 = replicas if alone is None else min(alone, replicas)
     t1 = 0.0
     done1 = 0
     for p in ps[:n1]:
@@ -73,7 +75,7 @@ def main(argv=None):
     b = sub.add_parser("batch")
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
-    b.add_argument("--alone", type=int, default=16)
+    b.add_argument("--alone", type=int, default=None)
     a = ap.parse_args(argv)
     if a.cmd == "kernel":
         out = kernel(a.grid, a.which, a.steps)
