@@ -129,14 +129,27 @@ def cpu_baseline(seconds=15.0, grid=GRID, threads=None):
                       (n, grid, dt)}
 
 
+def reduce_ranks(ms, events, dist=None):
+    """Whole-job figures of a weak-scaling run: the slowest rank's time and the
+    events of all ranks (host tensors, so gloo serves as well as NCCL)."""
+    if dist is None:
+        return ms, events
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e = torch.tensor([events], dtype=torch.float64)
+    dist.all_reduce(e)
+    return float(t.item()), int(e.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    cb = cpu_baseline(seconds=max(5.0, 30.0 / max(args.steps + args.warmup, 1)))
+    cb = cpu_baseline(seconds=max(5.0, 30.0 / max(args.steps + args.warmup, 1)), grid=args.grid)
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "dtype": "f64",
             "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-            "config": {"workload": "FP64 STZ KMC at %d^3, shear strain rate, seed 0" % GRID,
+            "config": {"workload": "FP64 STZ KMC at %d^3, shear strain rate, seed 0" % args.grid,
                        "implementation": "CPU restatement of the reference method (oracle/stz_oracle.c, "
                                          "OpenMP); the reference's own FFTW2+MPI+GSL build is not buildable "
                                          "on this box"},
@@ -205,16 +218,7 @@ def main():
     sc = eng.scalars()
     events = sc["kstep"] - k0
     launches = eng.launches() - l0
-    ms_max = ms
-    ev_total = events
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-        e = torch.tensor([events], dtype=torch.float64)
-        dist.all_reduce(e)
-        ev_total = int(e.item())
+    ms_max, ev_total = reduce_ranks(ms, events, dist)
     value = ev_total / (ms_max / 1e3)
 
     # e2e through the C ABI: run + copy this step's events and scalars to host

@@ -266,6 +266,13 @@ int stz_get_scalars(stz_ctx* ctx, stz_scalars* out);
 int stz_get_events(stz_ctx* ctx, int64_t first, stz_event* out, int64_t cap, int64_t* n);
 int stz_get_field(stz_ctx* ctx, int32_t which, int32_t comp, double* host, int64_t count);
 int stz_set_field(stz_ctx* ctx, int32_t which, int32_t comp, const double* host, int64_t count);
+/* The FFT schedule the context runs (FFT_MPI_Init's plans, init.c:77-110, are
+ * replaced by passes whose tiles and radix order are timed per grid shape):
+ * tiles[4] = lines per block of the x, y and outer-axis passes and the number
+ * of candidate schedules rejected for differing from the default's result;
+ * radices[36] = the radix order of the half-length x transform, of axis 1 and
+ * of axis 0, 12 entries each, zero-terminated. Either pointer may be null. */
+int stz_fft_schedule(stz_ctx* ctx, int32_t* tiles, int32_t* radices);
 /* Sets the mean strain EpsAvg (Voigt order, tensor shear; the first 3 in 2D)
  * that the next solve applies: the host assignment of EpsAvg before the first
  * solve of bmg.c:114, passed to the device. */

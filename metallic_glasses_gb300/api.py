@@ -92,6 +92,7 @@ def load_library(path=None):
     lib.stz_get_field.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64]
     lib.stz_set_field.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64]
     lib.stz_set_mean_strain.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.stz_fft_schedule.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     lib.stz_elastic_energy.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_sync.argtypes = [vp]
     lib.stz_timer_start.argtypes = [vp]
@@ -205,6 +206,14 @@ class Engine:
         v = np.ascontiguousarray(values, dtype=np.float64)
         _check(self.lib.stz_set_field(self.h, which, comp, v.ctypes.data, self.N))
 
+
+    def fft_schedule(self):
+        """(tiles, rejected, radix orders) of the tuned FFT plan."""
+        t = (C.c_int32 * 4)()
+        r = (C.c_int32 * 36)()
+        _check(self.lib.stz_fft_schedule(self.h, t, r))
+        orders = [[v for v in list(r)[12 * a:12 * a + 12] if v] for a in range(3)]
+        return {"tiles": list(t)[:3], "rejected": t[3], "radices": orders}
 
     def set_mean_strain(self, eps_avg):
         """EpsAvg (Voigt, tensor shear) applied by the next solve."""

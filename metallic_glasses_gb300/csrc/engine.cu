@@ -608,6 +608,11 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
     set_error("FFT plan for %dx%dx%d failed", kp.n0, kp.n1, kp.n2);
     return fail(st);
   }
+  // tiles and radix order timed for this grid (once per process and shape)
+  if ((st = fft_autotune(plan, c->stream, c->fft_tuned))) {
+    set_error("FFT schedule tuning failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(st);
+  }
   kp.c2r_blocks = fft_c2r_blocks(*plan);
   if (!mixed && (st = dalloc(&f.msum, (size_t)nc * kp.c2r_blocks))) return fail(st);
   MT rng;
@@ -875,6 +880,19 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
   if (which == STZ_FIELD_SIGMA) {
     sync_ctl(c);
     for (long long s = 0; s < N; s++) host[s] += c->host_ctl.u[comp];
+  }
+  return STZ_OK;
+}
+
+extern "C" int stz_fft_schedule(stz_ctx* c, int32_t* tiles, int32_t* radices) {
+  if (!c || !c->fft) return STZ_ERR_INVALID;
+  const FFTPlan& p = *plan_of(c);
+  if (tiles)
+    for (int k = 0; k < 4; k++) tiles[k] = c->fft_tuned[k];
+  if (radices) {
+    const Sched* sc[3] = {&p.sh, &p.s1, &p.s0};
+    for (int a = 0; a < 3; a++)
+      for (int k = 0; k < 12; k++) radices[a * 12 + k] = k < sc[a]->nst ? sc[a]->r[k] : 0;
   }
   return STZ_OK;
 }

@@ -28,8 +28,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <vector>
 #include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
+#include <vector>
 
 #include "fft.cuh"
 
@@ -540,6 +543,24 @@ Sched make_sched(int n) {
   return s;
 }
 
+// Alternative orders of the same factors: radix 4 first (more, simpler
+// stages), and the default's stages reversed (small radices first).
+Sched make_sched_r4(int n) {
+  Sched s;
+  s.n = n;
+  int m = n;
+  while (m % 4 == 0) { s.r[s.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { s.r[s.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { s.r[s.nst++] = 3; m /= 3; }
+  if (m != 1) s.nst = -1;
+  return s;
+}
+Sched make_sched_rev(int n) {
+  Sched d = make_sched(n), s = d;
+  for (int i = 0; i < d.nst; i++) s.r[i] = d.r[d.nst - 1 - i];
+  return s;
+}
+
 int upload_twiddles(int n, int count, double2** d64, float2** d32) {
   std::vector<double2> h(count > 0 ? count : 1);
   std::vector<float2> hf(h.size());
@@ -705,6 +726,154 @@ int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
   set_smem_attrs<double>(p->smem_x, p->smem_y, p->smem_g, sc_max);
   set_smem_attrs<float>(p->smem_x, p->smem_y, p->smem_g, sc_max);
   return STZ_OK;
+}
+
+// Tiles (lines per block) of the three kinds of pass and their shared memory;
+// false if a pass would not fit.
+static bool plan_set_tiles(FFTPlan* p, int Lx, int Ly, int Lg) {
+  const size_t cz = sizeof(double2);
+  const int ng = p->n0 > 1 ? p->n0 : p->n1;
+  const size_t sx = 2 * (size_t)Lx * (p->h + 1) * cz, sc = 2 * (size_t)Lx * (p->h + 2) * cz;
+  const size_t sy = 2 * (size_t)Ly * (p->n1 + 1) * cz, sg = 2 * (size_t)p->nc * Lg * (ng + 1) * cz;
+  if (Lx < 1 || Ly < 1 || Lg < 1) return false;
+  if (sc + sizeof(double) * p->nc * Lx * p->n2 > 200 * 1024 || sy > 200 * 1024 || sg > 200 * 1024) return false;
+  p->L_x = Lx;
+  p->L_y = Ly;
+  p->L_g = Lg;
+  p->smem_x = sx;
+  p->smem_c2r = sc;
+  p->smem_y = sy;
+  p->smem_g = sg;
+  return true;
+}
+
+namespace {
+struct Tuned {
+  int Lx, Ly, Lg;
+  Sched sh, s1, s0;
+  int rejected;  // candidates whose result differed from the default schedule's
+};
+std::mutex g_tune_mu;
+std::map<std::array<int, 5>, Tuned> g_tuned;
+
+float time_solve(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1) {
+  float best = 1e30f;
+  for (int rep = 0; rep < 2; rep++) {
+    cudaEventRecord(e0, st);
+    for (int i = 0; i < 3; i++) fft_solve(p, a, st, nullptr);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  return best;
+}
+}  // namespace
+
+int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const std::array<int, 5> key = {dev, p->n0, p->n1, p->n2, p->nc};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      plan_set_tiles(p, it->second.Lx, it->second.Ly, it->second.Lg);
+      p->sh = it->second.sh;
+      p->s1 = it->second.s1;
+      p->s0 = it->second.s0;
+      if (chosen) { chosen[0] = p->L_x; chosen[1] = p->L_y; chosen[2] = p->L_g; chosen[3] = it->second.rejected; }
+      return STZ_OK;
+    }
+  }
+  const size_t n = (size_t)p->nc * p->N, nk = (size_t)p->nc * p->Nk;
+  double *eps = nullptr, *ref = nullptr, *out = nullptr;
+  double2* spec = nullptr;
+  if (cudaMalloc(&eps, n * 8) != cudaSuccess || cudaMalloc(&ref, n * 8) != cudaSuccess ||
+      cudaMalloc(&out, n * 8) != cudaSuccess || cudaMalloc(&spec, nk * sizeof(double2)) != cudaSuccess) {
+    cudaFree(eps); cudaFree(ref); cudaFree(out); cudaFree(spec);
+    (void)cudaGetLastError();
+    return STZ_OK;  // no room to tune: keep the default schedule
+  }
+  // a deterministic eigenstrain with content on every wave vector
+  std::vector<double> h(n);
+  uint64_t x = 0x9E3779B97F4A7C15ull;
+  for (size_t i = 0; i < n; i++) {
+    x = x * 6364136223846793005ull + 1442695040888963407ull;
+    h[i] = (double)(x >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+  cudaMemcpyAsync(eps, h.data(), n * 8, cudaMemcpyHostToDevice, st);
+  SolveArgs a{};
+  a.eps = eps;
+  a.lambda = 2.0;
+  a.mu = 1.0;
+  a.out = kOutSig64;
+  a.sig64 = ref;
+  a.spec = spec;
+  a.ortho_mean = 1;
+  fft_solve(*p, a, st, nullptr);
+  cudaStreamSynchronize(st);
+  std::vector<double> r(n), o(n);
+  cudaMemcpy(r.data(), ref, n * 8, cudaMemcpyDeviceToHost);
+  double refmax = 0;
+  for (double v : r) refmax = std::max(refmax, std::fabs(v));
+  a.sig64 = out;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rejected = 0;
+  // a candidate is timed only if its result equals the default schedule's
+  auto valid = [&](const FFTPlan& q) {
+    fft_solve(q, a, st, nullptr);
+    cudaMemcpyAsync(o.data(), out, n * 8, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    double err = 0;
+    for (size_t i = 0; i < n; i++) err = std::max(err, std::fabs(o[i] - r[i]));
+    const bool ok = cudaGetLastError() == cudaSuccess && err <= 1e-10 * std::max(refmax, 1e-300);
+    if (!ok) rejected++;
+    return ok;
+  };
+  FFTPlan best = *p;
+  float tbest = time_solve(best, a, st, e0, e1);
+  auto consider = [&](FFTPlan q) {
+    if (!valid(q)) return;
+    const float t = time_solve(q, a, st, e0, e1);
+    if (t < tbest) { tbest = t; best = q; }
+  };
+  // coordinate descent over the tiles of each pass, then the radix orders
+  for (int Lx : {p->L_x * 2, p->L_x / 2, p->L_x / 4}) {
+    FFTPlan q = best;
+    if (Lx >= 1 && plan_set_tiles(&q, Lx, q.L_y, q.L_g)) consider(q);
+  }
+  for (int Ly : {2, 4, 16}) {
+    FFTPlan q = best;
+    if (Ly != best.L_y && plan_set_tiles(&q, q.L_x, Ly, q.L_g)) consider(q);
+  }
+  for (int Lg : {2, 4, 16}) {
+    FFTPlan q = best;
+    if (Lg != best.L_g && plan_set_tiles(&q, q.L_x, q.L_y, Lg)) consider(q);
+  }
+  for (int v = 0; v < 2; v++) {
+    FFTPlan q = best;
+    q.sh = v ? make_sched_rev(p->h) : make_sched_r4(p->h);
+    q.s1 = v ? make_sched_rev(p->n1) : make_sched_r4(p->n1);
+    q.s0 = v ? make_sched_rev(p->n0) : make_sched_r4(p->n0);
+    if (q.sh.nst > 0 && q.s1.nst > 0 && q.s0.nst > 0) consider(q);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(eps); cudaFree(ref); cudaFree(out); cudaFree(spec);
+  plan_set_tiles(p, best.L_x, best.L_y, best.L_g);
+  p->sh = best.sh;
+  p->s1 = best.s1;
+  p->s0 = best.s0;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = Tuned{p->L_x, p->L_y, p->L_g, p->sh, p->s1, p->s0, rejected};
+  }
+  if (chosen) { chosen[0] = p->L_x; chosen[1] = p->L_y; chosen[2] = p->L_g; chosen[3] = rejected; }
+  return cudaGetLastError() == cudaSuccess ? STZ_OK : STZ_ERR_CUDA;
 }
 
 // Plan whose twiddle tables live in caller-provided device storage (for the

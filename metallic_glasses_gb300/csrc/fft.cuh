@@ -37,6 +37,12 @@ struct FFTPlan {
 };
 
 int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc);
+// Chooses the tiles (lines per block of each pass) and the radix order of the
+// plan by timing FP64 solves of a fixed eigenstrain, once per device and grid
+// shape per process (cached); a candidate is admitted only if its result
+// equals the default schedule's within 1e-10. chosen (optional, 4 ints): the
+// tiles L_x, L_y, L_g and the number of candidates rejected.
+int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen);
 // A plan whose twiddle tables are written into caller-provided device storage
 // of at least fft_twiddle_count() elements (FP64 transforms only).
 size_t fft_twiddle_count(int n0, int n1, int n2);

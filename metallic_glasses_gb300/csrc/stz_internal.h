@@ -198,6 +198,7 @@ struct stz_ctx {
   void* l2buf = nullptr;
   size_t l2flush_bytes = 0;
   double* qbuf = nullptr;            // [N] activation energies of one mode (stz_get_field)
+  int fft_tuned[4] = {0, 0, 0, 0};   // FFT tiles chosen (L_x, L_y, L_g) and candidates rejected
   double* err_dev = nullptr;         // [4] error sums of the periodic re-solve
   double err_max = 0, err_rms = 0;   // last periodic re-solve
   double err_max_worst = 0, err_rms_worst = 0;
