@@ -1,11 +1,13 @@
 """Kernel and throughput timing of the STZ step on one GPU.
 
   python -m metallic_glasses_gb300.timing kernel --grid 128 --which 0 --steps 8
+  python -m metallic_glasses_gb300.timing solve --grid 256
   python -m metallic_glasses_gb300.timing batch --replicas 256 --events 32
 
 `kernel` times one per-event kernel of the mixed form launch by launch with
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
-only, 2: a whole event including selection). `batch` advances independent
+only, 2: a whole event including selection). `solve` times the FP64 re-solve
+of the full field (the FFT passes) with the tuned schedule. `batch` advances independent
 replicas (grid sizes 32^3..96^3, temperatures and strain rates drawn from the
 seed) together in one batch, then the same replicas one at a time, and prints
 both aggregate rates (one at a time = each replica in its own
@@ -24,6 +26,28 @@ def kernel(grid, which, steps, resolve_period=0):
     ms, n = eng.kernel_time(steps=steps, which=which)
     eng.close()
     return {"grid": grid, "which": which, "launch_ms": ms, "launches": n}
+
+
+def solve(grid, reps=5, mixed=True):
+    """FP64 Green's-function re-solves of the full field at grid^3 (the FFT
+    passes), timed with CUDA events. alg_bytes: what one solve must move
+    through HBM at least, the full re-solve figure 24 N s with s = 8: the
+    eigenstrain read and the field written (8 B per component and site) and
+    the half spectrum written and read once (16 B per component and wave
+    vector)."""
+    p = configs.mixed128(n=grid) if mixed else configs.plain128(n=grid)
+    eng = api.Engine(p)
+    eng.solve()
+    eng.sync()
+    eng.timer_start()
+    for _ in range(reps):
+        eng.solve()
+    ms = eng.timer_stop() / reps
+    sch = eng.fft_schedule()
+    eng.close()
+    n = grid ** 3
+    alg = 6 * n * (8 + 8) + 6 * (grid * grid * (grid // 2 + 1)) * 16 * 2
+    return {"grid": grid, "solve_ms": ms, "alg_bytes": alg, "alg_gbs": alg / (ms / 1e3) / 1e9, "schedule": sch}
 
 
 def batch(replicas, events, alone=None, seed0=0):
@@ -72,6 +96,9 @@ def main(argv=None):
     k.add_argument("--grid", type=int, default=128)
     k.add_argument("--which", type=int, default=0)
     k.add_argument("--steps", type=int, default=8)
+    sv = sub.add_parser("solve")
+    sv.add_argument("--grid", type=int, default=256)
+    sv.add_argument("--reps", type=int, default=5)
     b = sub.add_parser("batch")
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
@@ -79,6 +106,8 @@ def main(argv=None):
     a = ap.parse_args(argv)
     if a.cmd == "kernel":
         out = kernel(a.grid, a.which, a.steps)
+    elif a.cmd == "solve":
+        out = solve(a.grid, a.reps)
     else:
         out = batch(a.replicas, a.events, a.alone)
     print(json.dumps(out), flush=True)
