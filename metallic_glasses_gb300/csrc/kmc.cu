@@ -1040,14 +1040,15 @@ __device__ __forceinline__ LineOf unit_line(const MixK& kp, int u, int w, int p0
 
 // Stress update of one site (sv holds its coordinates): the pending
 // transformation's response S K(|x - p|) S de (S the reflection signs, K the
-// folded table record at rec) plus the uniform change Ud; stores the new
+// folded table record whose chunks are rec[0], rec[kt2], rec[2 kt2],
+// rec[3 kt2]) plus the uniform change Ud; stores the new
 // coordinates and leaves them in sv. dl holds
 // de (5), then the sign of coordinate 2 (y z) and the z and y flips that,
 // times the site's x flip sx, give the signs of coordinates 3 (x z) and 4 (x y).
-__device__ __forceinline__ void mixed_update(float* sdev, int N32, int s, int hp, const float4* rec, float sx,
-                                             const float* dl, const float* Ud, float* sv) {
+__device__ __forceinline__ void mixed_update(float* sdev, int N32, int s, int hp, const float4* rec, int kt2,
+                                             float sx, const float* dl, const float* Ud, float* sv) {
   if (hp) {
-    const float4 q0 = __ldg(rec), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2), q3 = __ldg(rec + 3);
+    const float4 q0 = __ldg(rec), q1 = __ldg(rec + kt2), q2 = __ldg(rec + 2 * kt2), q3 = __ldg(rec + 3 * kt2);
     const float K[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
                          q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
     const float g2 = dl[5], g3 = dl[6] * sx, g4 = dl[7] * sx;
@@ -1074,6 +1075,8 @@ __device__ __forceinline__ void mixed_update(float* sdev, int N32, int s, int hp
 }
 
 // The 20 rates of one site (a lane whose pair partner is past the line).
+// TRACK: also the largest argument in *xma.
+template <int TRACK>
 __device__ __forceinline__ void mixed_rates1(const float* sa, float aa, float ct, const float2* md, float2* acc2,
                                              float* xma) {
   float mx = -INFINITY;
@@ -1086,16 +1089,18 @@ __device__ __forceinline__ void mixed_rates1(const float* sa, float aa, float ct
 #pragma unroll
     for (int k = 0; k < 5; k++) xa = __ffma2_rn(make_float2(ta[k], ta[k]), md[5 * j + k], xa);
     acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
-    mx = fmaxf(mx, fmaxf(xa.x, xa.y));
+    if (TRACK) mx = fmaxf(mx, fmaxf(xa.x, xa.y));
   }
-  *xma = mx;
+  if (TRACK) *xma = mx;
 }
 
 // The 20 rates of two sites (b may be absent), packed two modes per FP32x2
 // FMA after scaling the stress coordinates by ct = 1/kT; each lane of a pair
-// is the scalar chain of mx_x, so the search sees the same bits. One load of each mode coefficient serves both sites. Returns the
-// largest argument of site a in *xma and of site b in *xmb (an argument above
-// q_ref a_scale is a negative barrier, the athermal trigger).
+// is the scalar chain of mx_x, so the search sees the same bits. One load of
+// each mode coefficient serves both sites. TRACK: also the largest argument
+// of site a in *xma and of site b in *xmb (an argument above q_ref a_scale is
+// a negative barrier, the athermal trigger).
+template <int TRACK>
 __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const float* sb, float ab, bool hb, float ct,
                                              const float2* md, float2* acc2, float* xma, float* xmb) {
   float2 mx = make_float2(-INFINITY, -INFINITY);
@@ -1116,11 +1121,44 @@ __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const fl
     }
     acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xa.x), ex2_approx(xa.y)));
     if (hb) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(xb.x), ex2_approx(xb.y)));
-    mx.x = fmaxf(mx.x, fmaxf(xa.x, xa.y));
-    mx.y = fmaxf(mx.y, fmaxf(xb.x, xb.y));
+    if (TRACK) {
+      mx.x = fmaxf(mx.x, fmaxf(xa.x, xa.y));
+      mx.y = fmaxf(mx.y, fmaxf(xb.x, xb.y));
+    }
   }
-  *xma = mx.x;
-  *xmb = mx.y;
+  if (TRACK) {
+    *xma = mx.x;
+    *xmb = mx.y;
+  }
+}
+
+// Exact athermal test of one line by its warp, for the lines whose mode sums
+// reach half of 2^thr (see line_sums): every site's 20 arguments recomputed
+// with the chain of mixed_rates1/2 from the stored (updated) stress; true in
+// a lane when one of its sites has an argument above thr. Rare: only lines
+// holding a barrier within a few kT of zero get here.
+__device__ __forceinline__ bool line_negative(const float* sdev, const float* dF32, int N32, int base, int n2,
+                                              float q_ref, float a_scale, float ct, const float2* md, float thr) {
+  bool neg = false;
+#pragma unroll 1
+  for (int i2 = threadIdx.x & 31; i2 < n2; i2 += 32) {
+    float t[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) t[k] = __fmul_rn(sdev[k * N32 + base + i2], ct);
+    const float a = (q_ref - dF32[base + i2]) * a_scale;
+#pragma unroll 1
+    for (int j = 0; j < STZ_MODES / 2; j++) {
+      float x0 = a, x1 = a;
+#pragma unroll
+      for (int k = 0; k < 5; k++) {
+        const float2 c = md[5 * j + k];
+        x0 = __fmaf_rn(t[k], c.x, x0);
+        x1 = __fmaf_rn(t[k], c.y, x1);
+      }
+      neg |= x0 > thr || x1 > thr;
+    }
+  }
+  return neg;
 }
 
 // ------------------------------------------ bulk-copy staging of a line
@@ -1186,8 +1224,10 @@ __device__ __forceinline__ void issue_line(const MixK& kp, int i0, int i1, float
 }
 
 // One line (i0, i1) by one warp from its staged inputs: update every site,
-// and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2.
-template <int UPDATE_ONLY>
+// and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2. Unless
+// LINEVOTE (the athermal test is then made per line from the mode sums), set
+// neg when a site's largest argument exceeds thr_neg.
+template <int UPDATE_ONLY, int LINEVOTE>
 __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int i0, int i1,
                                            int p0, int p1, int p2, const float* de, const float* Ud,
                                            const float2* md, const float* stage, float2* acc2, unsigned& neg,
@@ -1217,14 +1257,14 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
       const int d2 = fold(i2 - p2, n2, &fx);
 #pragma unroll
       for (int k = 0; k < 5; k++) sa[k] = stage[k * n2 + i2];
-      mixed_update(kp.sdev, N32, base + i2, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sa);
+      mixed_update(kp.sdev, N32, base + i2, hp, row + d2, kp.kt2, fx ? -1.f : 1.f, dl, Ud, sa);
     }
     if (hb) {
       int fx;
       const int d2 = fold(i2b - p2, n2, &fx);
 #pragma unroll
       for (int k = 0; k < 5; k++) sb[k] = stage[k * n2 + i2b];
-      mixed_update(kp.sdev, N32, base + i2b, hp, row + 4 * d2, fx ? -1.f : 1.f, dl, Ud, sb);
+      mixed_update(kp.sdev, N32, base + i2b, hp, row + d2, kp.kt2, fx ? -1.f : 1.f, dl, Ud, sb);
     } else {
 #pragma unroll
       for (int k = 0; k < 5; k++) sb[k] = sa[k];
@@ -1233,14 +1273,14 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
       const float dFa = stage[5 * n2 + i2];
       const float dFb = hb ? stage[5 * n2 + i2b] : dFa;
       const float aa = (kp.q_ref - dFa) * kp.a_scale, ab = (kp.q_ref - dFb) * kp.a_scale;
-      float xma, xmb = -INFINITY;
+      float xma = -INFINITY, xmb = -INFINITY;
       // lines of 32 and the last third of 96: no lane has a partner. The vote
       // is among the lanes executing here (lines shorter than 32 leave some
       // outside the loop); a lane takes the single-site path only when no
       // lane of its group has a partner, so the result is the same either way.
-      if (__any_sync(__activemask(), hb)) mixed_rates2(sa, aa, sb, ab, hb, kp.inv_kt, md, acc2, &xma, &xmb);
-      else mixed_rates1(sa, aa, kp.inv_kt, md, acc2, &xma);
-      neg |= (xma > thr_neg || (hb && xmb > thr_neg)) ? 1u : 0u;
+      if (__any_sync(__activemask(), hb)) mixed_rates2<!LINEVOTE>(sa, aa, sb, ab, hb, kp.inv_kt, md, acc2, &xma, &xmb);
+      else mixed_rates1<!LINEVOTE>(sa, aa, kp.inv_kt, md, acc2, &xma);
+      if (!LINEVOTE) neg |= (xma > thr_neg || (hb && xmb > thr_neg)) ? 1u : 0u;
     }
   }
 }
@@ -1248,20 +1288,32 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
 // Per-line sums: each lane parks its 20 sums in shared memory and lanes
 // 0..19 add one mode each over the 32 lanes (a fixed order), written to
 // lsum[line][m].
-__device__ __forceinline__ void line_sums(const float2* acc2, float (*red)[STZ_MODES], float* lsum_line) {
+//
+// With LINEVOTE, also the line's athermal vote: a site argument above thr
+// gives a term of at least 2^thr (1 - 2^-22) in its mode's line sum, and FP32
+// sums of non-negative terms never fall below their largest term, so a line
+// whose 20 sums all stay below 2^(thr - 1) holds no trigger; true when one
+// does not (or is NaN), for an exact test of the line.
+template <int LINEVOTE>
+__device__ __forceinline__ bool line_sums(const float2* acc2, float (*red)[STZ_MODES], float* lsum_line,
+                                          float thr) {
   const int lane = threadIdx.x & 31;
   float4* my = reinterpret_cast<float4*>(red[lane]);
 #pragma unroll
   for (int j = 0; j < STZ_MODES / 4; j++)
     my[j] = make_float4(acc2[2 * j].x, acc2[2 * j].y, acc2[2 * j + 1].x, acc2[2 * j + 1].y);
   __syncwarp();
+  bool hot = false;
   if (lane < STZ_MODES) {
     float t = 0.f;
 #pragma unroll 8
     for (int r = 0; r < 32; r++) t += red[r][lane];
     lsum_line[lane] = t;
+    if (LINEVOTE) hot = !(t < exp2f(thr - 1.0f));
   }
+  if (LINEVOTE) return __any_sync(FULL, hot);
   __syncwarp();
+  return false;
 }
 
 // Plane sums psum[m][i0] = sum over i1 of lsum[i0 n1 + i1][m] in FP64 for
@@ -1298,7 +1350,7 @@ __device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, do
 // Body of the grid-wide mixed-form kernel for block b of one replica (kp may
 // live in kernel parameters or, for batches, in shared memory); the block
 // takes units b, b + nblk, ... and its warps run through them independently.
-template <int UPDATE_ONLY>
+template <int UPDATE_ONLY, int LINEVOTE>
 __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b, const float2* md,
                                                 const float (*mraw)[5], float* mix_smem) {
   __shared__ __align__(8) unsigned long long mbar[TH / 32][2];
@@ -1367,12 +1419,14 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
     float2 acc2[STZ_MODES / 2];
 #pragma unroll
     for (int q = 0; q < STZ_MODES / 2; q++) acc2[q] = make_float2(0.f, 0.f);
-    mixed_line<UPDATE_ONLY>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
+    mixed_line<UPDATE_ONLY, LINEVOTE>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
     if (!UPDATE_ONLY) {
       // the consumed stage holds the transpose
       __syncwarp();
-      line_sums(acc2, reinterpret_cast<float(*)[STZ_MODES]>(cur),
-                k.lsum + ((long long)L.i0 * k.n1 + L.i1) * STZ_MODES);
+      const int base = (L.i0 * k.n1 + L.i1) * k.n2;
+      if (line_sums<LINEVOTE>(acc2, reinterpret_cast<float(*)[STZ_MODES]>(cur),
+                              k.lsum + ((long long)L.i0 * k.n1 + L.i1) * STZ_MODES, thr_neg))
+        neg |= line_negative(k.sdev, k.dF32, N32, base, k.n2, k.q_ref, k.a_scale, k.inv_kt, md, thr_neg) ? 1u : 0u;
     }
     u = un;
     L = Ln;
@@ -1398,7 +1452,7 @@ template <int UPDATE_ONLY>
 __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   extern __shared__ __align__(128) float mix_smem[];
   pdl_wait();
-  mixed_main_body<UPDATE_ONLY>(kp, f, blockIdx.x, &kp.mdev2[0][0], kp.mdev_raw, mix_smem);
+  mixed_main_body<UPDATE_ONLY, 1>(kp, f, blockIdx.x, &kp.mdev2[0][0], kp.mdev_raw, mix_smem);
 }
 
 
@@ -1971,9 +2025,9 @@ __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __rest
   load_desc(d, r, &skp, &sf);
   extern __shared__ __align__(128) float mix_smem[];
   if (SHARED)
-    mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &ms.mdev2[0][0], ms.mdev_raw, mix_smem);
+    mixed_main_body<0, 0>(skp, sf, blockIdx.x - rep_first[r], &ms.mdev2[0][0], ms.mdev_raw, mix_smem);
   else
-    mixed_main_body<0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
+    mixed_main_body<0, 0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
 }
 
 // Plane sums and selection of a batch: block (x, r) sums plane x of replica
@@ -2050,7 +2104,10 @@ __global__ void k_dev_from_sig(KParams kp, const double* sig, float* sdev) {
 }
 
 // Column b of the response table: K[a][b](d) = e_a : sigma^(b)(d) for d in
-// the octant 0 <= d_i <= n_i/2, stored in the packed upper triangle.
+// the octant 0 <= d_i <= n_i/2, stored in the packed upper triangle (15 of a
+// record's 16 floats). A row (d0, d1) holds its kt2 records chunk-major: the
+// 16-byte chunk q of record d2 at float4 index (row * 4 + q) * kt2 + d2, so
+// the lanes of a warp reading consecutive records read contiguous bytes.
 __global__ void k_ktab_column(KParams kp, const double* sig, float* ktab, int b) {
   const long long ts = (long long)kp.kt1 * kp.kt2, tn = (long long)kp.kt0 * ts;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tn; t += (long long)gridDim.x * blockDim.x) {
@@ -2064,7 +2121,7 @@ __global__ void k_ktab_column(KParams kp, const double* sig, float* ktab, int b)
     for (int a = 0; a <= b; a++) {
       // packed index of (a, b), a <= b, row-major upper triangle
       const int idx = a * 5 - a * (a - 1) / 2 + (b - a);
-      ktab[16 * t + idx] = (float)d[a];
+      ktab[((t / kp.kt2 * 4 + (idx >> 2)) * kp.kt2 + d2) * 4 + (idx & 3)] = (float)d[a];
     }
   }
 }

@@ -47,3 +47,30 @@ def test_batch_replicas_advance_and_stay_accurate(engine_lib):
         if sc["n_resolves"]:
             assert sc["stress_err_rms_worst"] < 1e-5
     batch.close()
+
+
+def test_athermal_trigger_forms_agree(engine_lib):
+    """The single-grid main pass decides the athermal trigger per line from
+    its 20 FP32 mode sums (an exact re-test of the lines whose sums reach half
+    of the trigger's rate); the batched pass tests every site's largest
+    argument. On a 32^3 grid under 4 GPa of shear stress, where avalanches
+    start within the first 60 steps, both take the same steps."""
+    p = configs.stress32(n=32)
+    p.applied_stress[api.XY] = 4.0
+    p.precision = api.PREC_MIXED
+    p.solver = api.SOLVER_KERNEL
+    p.resolve_period = 1000
+    eng = api.Engine(p)
+    eng.run(max_events=57)
+    batch = api.Batch([p])
+    batch.run(57)
+    a, b = eng.events(), batch.replicas[0].events()
+    sa, sb = eng.scalars(), batch.replicas[0].scalars()
+    assert sa["astep"] > 0
+    assert (sa["kstep"], sa["astep"]) == (sb["kstep"], sb["astep"])
+    assert len(a) == len(b) > 0
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(a["time"], b["time"])
+    eng.close()
+    batch.close()
