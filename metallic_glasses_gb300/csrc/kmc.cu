@@ -1316,35 +1316,66 @@ __device__ __forceinline__ bool line_sums(const float2* acc2, float (*red)[STZ_M
   return false;
 }
 
-// Plane sums psum[m][i0] = sum over i1 of lsum[i0 n1 + i1][m] in FP64 for
-// plane i0, by one block: warp w adds modes w, w + 8, w + 16 with its lanes
-// striding the lines, then a fixed shuffle tree.
-__device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, double* psum, int i0) {
-  constexpr int kModesPerWarp = (STZ_MODES + TH / 32 - 1) / (TH / 32);  // 3
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const float* ls = lsum + (long long)i0 * n1 * STZ_MODES;
-  double v[kModesPerWarp];
+// Error-free FP32 addition (Knuth's TwoSum, six operations, no branch):
+// a + b = s + e exactly, s = fl(a + b).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  const float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+// (hi, lo) += (h2, l2) for unevaluated sums hi + lo of FP32 pairs.
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
+  float s, e;
+  two_sum(hi, h2, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, l2));
+  hi = __fadd_rn(s, e);  // renormalise: |e| is below half an ulp of s or s = 0
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+// Plane sums psum[m][i0] = sum over i1 of lsum[i0 n1 + i1][m] for plane i0,
+// by one block: 8 threads per mode (thread m 8 + g takes lines g, g + 8, ...)
+// add the FP32 line sums as unevaluated pairs hi + lo with error-free
+// additions (about 48 bits; GB300 issues FP64 at 1/64 of the FP32 rate, and
+// a chain of FP64 additions per mode was most of this step), combine the 8
+// pairs by shuffles in a fixed tree, and store hi + lo in FP64. The plane's
+// largest biased exponent goes to *emax (an integer maximum, independent of
+// the order of the blocks).
+__device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, double* psum, int i0,
+                                           unsigned* emax) {
+  constexpr int kG = 8;     // threads per mode
+  constexpr int kBatch = 16;  // loads in flight per thread
+  const int m = threadIdx.x / kG, g = threadIdx.x % kG;
+  const float* ls = lsum + (long long)i0 * n1 * STZ_MODES + m;
+  float hi = 0.f, lo = 0.f;
+  if (m < STZ_MODES) {
+    for (int i1 = g; i1 < n1; i1 += kG * kBatch) {
+      float x[kBatch];
 #pragma unroll
-  for (int j = 0; j < kModesPerWarp; j++) v[j] = 0.0;
-  // all loads of a line before the adds: one memory round trip per 32 lines
-  for (int i1 = lane; i1 < n1; i1 += 32) {
-    float x[kModesPerWarp];
+      for (int q = 0; q < kBatch; q++) x[q] = i1 + q * kG < n1 ? ls[(i1 + q * kG) * STZ_MODES] : 0.f;
 #pragma unroll
-    for (int j = 0; j < kModesPerWarp; j++) {
-      const int m = w + j * (TH / 32);
-      x[j] = m < STZ_MODES ? ls[i1 * STZ_MODES + m] : 0.f;
+      for (int q = 0; q < kBatch; q++) {
+        float s, e;
+        two_sum(hi, x[q], s, e);
+        hi = s;
+        lo = __fadd_rn(lo, e);
+      }
     }
-#pragma unroll
-    for (int j = 0; j < kModesPerWarp; j++) v[j] += (double)x[j];
   }
+  // the 8 threads of a mode are consecutive lanes of one warp
 #pragma unroll
-  for (int j = 0; j < kModesPerWarp; j++) {
-    double t = v[j];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(FULL, t, off);
-    const int m = w + j * (TH / 32);
-    if (lane == 0 && m < STZ_MODES) psum[(long long)m * n0 + i0] = t;
+  for (int off = 1; off < kG; off <<= 1) {
+    const float h2 = __shfl_xor_sync(FULL, hi, off), l2 = __shfl_xor_sync(FULL, lo, off);
+    pair_add(hi, lo, h2, l2);
   }
+  unsigned ex = 0;
+  if (m < STZ_MODES && g == 0) {
+    const double v = (double)hi + (double)lo;
+    psum[(long long)m * n0 + i0] = v;
+    ex = (unsigned)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffu;
+  }
+  ex = __reduce_max_sync(FULL, ex);
+  if ((threadIdx.x & 31) == 0 && ex) atomicMax(emax, ex);
 }
 
 // Body of the grid-wide mixed-form kernel for block b of one replica (kp may
@@ -1652,11 +1683,12 @@ __device__ __forceinline__ int chunk_find(const long long* v, long long E, long 
 // plane i0 for mode m from their FP32 sums, then the sites of the chosen line
 // with their rates recomputed exactly as the main pass computed them, both in
 // the fixed point of scale e. T is the target left within (m, i0). Returns
-// the site (or -1) in every lane and the distance of the target from the
-// nearer edge of the chosen site's interval in *margin.
+// the site (or -1) in every lane, the distance of the target from the nearer
+// edge of the chosen site's interval in *margin and the chosen (site, mode)'s
+// scaled log2-rate argument (the chain of mx_x) in *x_sel.
 constexpr int kLaneChunk = 16;  // lines or sites per lane: n1, n2 <= 512
 __device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
-                                      long long* margin, unsigned long long* t_lines) {
+                                      long long* margin, unsigned long long* t_lines, float* x_sel) {
   const int lane = threadIdx.x & 31;
   // level 2: lines
   const int n1 = kp.n1;
@@ -1688,28 +1720,42 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   // level 3: sites of line (i0, i1), rates recomputed with the main pass's chain
   const int n2 = kp.n2;
   const long long base = ((long long)i0 * n1 + i1) * n2;
-  const double zero[6] = {0, 0, 0, 0, 0, 0};
   const int c3 = (n2 + 31) / 32;
   const int a2 = lane * c3;
   long long rv[kLaneChunk];
+  float xv[kLaneChunk];
   long long S2 = 0;
 #pragma unroll
   for (int q = 0; q < kLaneChunk; q++) {
-    rv[q] = (q < c3 && a2 + q < n2) ? fix_f((float)site_rate<2>(kp, f, zero, 0.0, base + a2 + q, m), e) : 0;
+    xv[q] = 0.f;
+    rv[q] = 0;
+    if (q < c3 && a2 + q < n2) {
+      const long long s = base + a2 + q;
+      float sv[5];
+#pragma unroll
+      for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+      xv[q] = mx_x(kp, sv, (kp.q_ref - f.dF32[s]) * kp.a_scale, m);
+      rv[q] = fix_f(ex2_approx(xv[q]), e);
+    }
     S2 += rv[q];
   }
   long long E2, T2;
   const int L2 = warp_find_i64(S2, rem2, &E2, &T2);
   if (L2 < 0) return -1;
   long long site = -1, mg = 0;
+  float xs = 0.f;
   if (lane == L2) {
     long long hb, ha;
     const int h = chunk_find<kLaneChunk>(rv, E2, T2, &hb, &ha);
     site = h < 0 ? -1 : base + a2 + h;
     mg = min(T2 - hb, ha - T2);
+#pragma unroll
+    for (int q = 0; q < kLaneChunk; q++)
+      if (q == h) xs = xv[q];
   }
   site = (long long)__shfl_sync(FULL, (unsigned long long)site, L2);
   *margin = (long long)__shfl_sync(FULL, (unsigned long long)mg, L2);
+  *x_sel = __shfl_sync(FULL, xs, L2);
   return site;
 }
 
@@ -1736,9 +1782,9 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   __shared__ long long sh_site;
   __shared__ int sh_mode;
   __shared__ double sh_margin;
+  __shared__ float sh_x;
   __shared__ long long sh_p1, sh_rem1, sh_Tint, sh_Rint;
   __shared__ long long sh_inc_i[TH];
-  __shared__ int sh_emax;
   __shared__ unsigned long long sh_tl[2];  // search clock: level 1 done, level 2 done
   // total rate: the FP64 plane sums q = m n0 + i0 in per-thread contiguous
   // chunks (loaded before the control-block copy so that the two overlap),
@@ -1761,20 +1807,14 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
     for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
   }
-  // largest biased exponent (the bit patterns of non-negative doubles order
-  // like the values; 0x7ff marks a non-finite sum)
-  int emax = 0;
-#pragma unroll
-  for (int k = 0; k < kLaneChunk; k++) emax = max(emax, (int)((unsigned long long)__double_as_longlong(pv[k]) >> 52) & 0x7ff);
-  for (long long q = q0 + kLaneChunk; q < q1; q++)
-    emax = max(emax, (int)((unsigned long long)__double_as_longlong(f.psum[q]) >> 52) & 0x7ff);
-  emax = __reduce_max_sync(FULL, (unsigned)emax);
-  if (threadIdx.x == 0) { sh_emax = 0; sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; }
+  if (threadIdx.x == 0) { sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; }
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) atomicMax(&sh_emax, emax);
-  __syncthreads();
-  // every value < 2^(emax - 1022): P of them sum below 2^62
-  const int e = 1084 - clog2(P) - sh_emax;
+  // largest biased exponent of the plane sums, gathered by the plane blocks
+  // (the bit patterns of non-negative doubles order like the values; 0x7ff
+  // marks a non-finite sum); every value < 2^(emax - 1022), so P of them sum
+  // below 2^62
+  const int emax = (int)sc.plane_emax;
+  const int e = 1084 - clog2(P) - emax;
   long long iv[kLaneChunk];
   long long S = 0;
 #pragma unroll
@@ -1789,6 +1829,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   Ctl* c = &sc;
   if (threadIdx.x == 0) {
     c->step++;
+    c->plane_emax = 0;  // read by every thread before the scan's barriers
     c->has_pend = 0;
     for (int k = 0; k < 6; k++) c->U[k] = 0;
     const long long Rint = sh_inc_i[TH - 1];
@@ -1802,7 +1843,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       kind = kAthermal;
       c->halt = 1;
       c->halt_reason = kHaltAthermal;
-    } else if (sh_emax == 0x7ff || Rint <= 0) {
+    } else if (emax == 0x7ff || Rint <= 0) {
       kind = kNone;
       c->status = STZ_ERR_NAN;
       c->halt = 1;
@@ -1867,17 +1908,19 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       // levels 2 and 3: warp 0
       const long long pg = sh_p1;
       long long site = -1, mg = 0;
+      float xs = 0.f;
       int m = -1;
       if (threadIdx.x == 0) sh_tl[0] = gtimer();
       if (pg >= 0) {
         m = (int)(pg / kp.n0);
         const int i0 = (int)(pg - (long long)m * kp.n0);
-        site = search_line_site(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1]);
+        site = search_line_site(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
       }
       if (threadIdx.x == 0) {
         sh_site = site;
         sh_mode = m;
         sh_margin = (double)mg;
+        sh_x = xs;
       }
     } else if (threadIdx.x == 32) {
       // the clock advance, while warp 0 searches
@@ -1900,10 +1943,8 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
           c->step_kind = kNone;
         } else {
           if (sh_margin < (double)(sh_Rint >> 40)) c->near_ties++;  // within 2^-40 R of an edge
-          float sv[5];
-          for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
-          const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
-          const double q = (double)kp.q_ref - (double)mx_x(kp, sv, a, m) * kp.inv_a_scale;
+          // Q of the chosen (site, mode) from the argument the search computed
+          const double q = (double)kp.q_ref - (double)sh_x * kp.inv_a_scale;
           c->sel_site = s;
           c->sel_mode = m;
           c->sel_q = q;
@@ -1991,7 +2032,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select(KParams kp, Fields f) {
   pdl_wait();
   pdl_release();
   if (f.ctl->halt) return;
-  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x);
+  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x, &f.ctl->plane_emax);
   if (!last_of(&f.ctl->ticket, gridDim.x)) return;
   mixed_tail_body(kp, f, 0);
 }
@@ -2043,7 +2084,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __
   const int n0 = e.kp.n0;
   Ctl* ctl = e.f.ctl;
   if ((int)blockIdx.x >= n0 || ctl->halt) return;
-  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x);
+  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x, &ctl->plane_emax);
   if (!last_of(&ctl->ticket, (unsigned)n0)) return;
   load_desc(d, r, &skp, &sf);
   mixed_tail_body(skp, sf, 0);

@@ -86,6 +86,7 @@ struct Ctl {
   int sel_mode;
   long long sel_site;
   int ath_count;
+  unsigned int plane_emax;   // mixed: largest biased exponent of this event's plane sums
   // device-clock phase times of the mixed-form kernel (globaltimer, ns)
   unsigned long long prof_t0, prof_main_ns, prof_tail_ns, prof_n;
   unsigned long long prof_part_ns[8];  // tail: copy-in+sums, twist+decision, search, commit,
