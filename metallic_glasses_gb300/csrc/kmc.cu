@@ -1132,6 +1132,26 @@ __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const fl
   }
 }
 
+// The 20 rates of four sites of a lane (all inside the line), one
+// coefficient pair load per four FP32x2 FMAs; each site's lane of a pair is
+// the scalar chain of mx_x, and the sums take sites 0, 1, 2, 3 in order.
+__device__ __forceinline__ void mixed_rates4(const float (*t)[5], const float* a, const float2* md, float2* acc2) {
+#pragma unroll
+  for (int j = 0; j < STZ_MODES / 2; j++) {
+    float2 x[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) x[q] = make_float2(a[q], a[q]);
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const float2 c = md[5 * j + k];
+#pragma unroll
+      for (int q = 0; q < 4; q++) x[q] = __ffma2_rn(make_float2(t[q][k], t[q][k]), c, x[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(x[q].x), ex2_approx(x[q].y)));
+  }
+}
+
 // Exact athermal test of one line by its warp, for the lines whose mode sums
 // reach half of 2^thr (see line_sums): every site's 20 arguments recomputed
 // with the chain of mixed_rates1/2 from the stored (updated) stress; true in
@@ -1227,13 +1247,13 @@ __device__ __forceinline__ void issue_line(const MixK& kp, int i0, int i1, float
 // and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2. Unless
 // LINEVOTE (the athermal test is then made per line from the mode sums), set
 // neg when a site's largest argument exceeds thr_neg.
-template <int UPDATE_ONLY, int LINEVOTE>
+template <int UPDATE_ONLY, int LINEVOTE, int N2>
 __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int i0, int i1,
                                            int p0, int p1, int p2, const float* de, const float* Ud,
                                            const float2* md, const float* stage, float2* acc2, unsigned& neg,
                                            float thr_neg) {
   const int lane = threadIdx.x & 31;
-  const int n2 = kp.n2;
+  const int n2 = N2 > 0 ? N2 : kp.n2;
   int fz, fy;
   const int d0 = fold(i0 - p0, kp.n0, &fz);
   const int d1 = fold(i1 - p1, kp.n1, &fy);
@@ -1248,6 +1268,26 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
   dl[6] = sz;
   dl[7] = sy;
   const int base = (i0 * kp.n1 + i1) * n2;
+  if (N2 == 128 && LINEVOTE && !UPDATE_ONLY) {
+    // each lane's four sites lane + 32 q in one pass; offsets are immediates
+    constexpr int kKt2 = N2 / 2 + 1;
+    float t[4][5], a[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i2 = lane + 32 * q;
+      int fx;
+      const int d2 = fold(i2 - p2, N2, &fx);
+      float sv[5];
+#pragma unroll
+      for (int k = 0; k < 5; k++) sv[k] = stage[k * N2 + i2];
+      mixed_update(kp.sdev, N32, base + i2, hp, row + d2, kKt2, fx ? -1.f : 1.f, dl, Ud, sv);
+#pragma unroll
+      for (int k = 0; k < 5; k++) t[q][k] = __fmul_rn(sv[k], kp.inv_kt);
+      a[q] = (kp.q_ref - stage[5 * N2 + i2]) * kp.a_scale;
+    }
+    mixed_rates4(t, a, md, acc2);
+    return;
+  }
   for (int i2 = lane; i2 < n2; i2 += 64) {
     const int i2b = i2 + 32;
     const bool hb = i2b < n2;
@@ -1381,7 +1421,7 @@ __device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, do
 // Body of the grid-wide mixed-form kernel for block b of one replica (kp may
 // live in kernel parameters or, for batches, in shared memory); the block
 // takes units b, b + nblk, ... and its warps run through them independently.
-template <int UPDATE_ONLY, int LINEVOTE>
+template <int UPDATE_ONLY, int LINEVOTE, int N2 = 0>
 __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields& f, int b, const float2* md,
                                                 const float (*mraw)[5], float* mix_smem) {
   __shared__ __align__(8) unsigned long long mbar[TH / 32][2];
@@ -1450,7 +1490,7 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
     float2 acc2[STZ_MODES / 2];
 #pragma unroll
     for (int q = 0; q < STZ_MODES / 2; q++) acc2[q] = make_float2(0.f, 0.f);
-    mixed_line<UPDATE_ONLY, LINEVOTE>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
+    mixed_line<UPDATE_ONLY, LINEVOTE, N2>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
     if (!UPDATE_ONLY) {
       // the consumed stage holds the transpose
       __syncwarp();
@@ -1479,11 +1519,11 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
 }
 
-template <int UPDATE_ONLY>
+template <int UPDATE_ONLY, int N2 = 0>
 __global__ void __launch_bounds__(TH, 3) k_mixed(KParams kp, Fields f) {
   extern __shared__ __align__(128) float mix_smem[];
   pdl_wait();
-  mixed_main_body<UPDATE_ONLY, 1>(kp, f, blockIdx.x, &kp.mdev2[0][0], kp.mdev_raw, mix_smem);
+  mixed_main_body<UPDATE_ONLY, 1, N2>(kp, f, blockIdx.x, &kp.mdev2[0][0], kp.mdev_raw, mix_smem);
 }
 
 
@@ -2203,6 +2243,7 @@ static void mixed_smem_init() {
       (void)cudaGetLastError();
   };
   raise((const void*)k_mixed<0>);
+  raise((const void*)k_mixed<0, 128>);
   raise((const void*)k_mixed<1>);
   raise((const void*)k_mixed_batched<0>);
   raise((const void*)k_mixed_batched<1>);
@@ -2256,6 +2297,7 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   mixed_smem_init();
   if (update_only) k_mixed<1><<<kp.nblk, TH, mix_smem_bytes(kp.n2), st>>>(kp, f);
+  else if (kp.n2 == 128) launch_pdl(k_mixed<0, 128>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else launch_pdl(k_mixed<0>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
 }
 
