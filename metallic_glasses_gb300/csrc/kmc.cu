@@ -1552,16 +1552,27 @@ __device__ __forceinline__ double lane_Cinv(const KParams& kp, double s, int k) 
 // Thermal event of the mixed form: eigenstrain update, the incremental
 // "solve" (pending response + uniform change U) and the loading of
 // evolution.c:262-317, lane-parallel over the six components.
-__device__ void mixed_commit_lanes(const KParams& kp, const Fields& f, Ctl* c, long long s, int m) {
+// The site's part of the commit (lanes 0..5 of a warp): its eigenstrain and
+// last strain increment in global memory.
+__device__ void mixed_commit_site_lanes(const KParams& kp, const Fields& f, long long s, int m) {
   const int k = threadIdx.x & 31;
-  const bool own = k < 6;
-  const long long N = kp.N;
-  const double mk = own ? kp.modes[m][k] : 0.0;
-  if (own) {
+  if (k < 6) {
+    const long long N = kp.N;
+    const double mk = kp.modes[m][k];
     f.prev_deps[k * N + s] = mk;
     f.eps0[k * N + s] += mk;
-    c->eps0_sum[k] += mk;
   }
+}
+
+// The rest of the commit, which needs only the mode and the clock advance
+// c->t_kmc (so it runs while another warp searches the site): the sum of the
+// eigenstrain, the uniform stress change U of the loading, the mean strains
+// and the stress.
+__device__ void mixed_commit_lanes(const KParams& kp, Ctl* c, int m) {
+  const int k = threadIdx.x & 31;
+  const bool own = k < 6;
+  const double mk = own ? kp.modes[m][k] : 0.0;
+  if (own) c->eps0_sum[k] += mk;
   __syncwarp();
   const double ebar = own ? c->eps_avg[k] : 0.0;
   const double dA = own ? ebar - c->eps_avg_applied[k] : 0.0;
@@ -1727,6 +1738,8 @@ __device__ __forceinline__ int chunk_find(const long long* v, long long E, long 
 // edge of the chosen site's interval in *margin and the chosen (site, mode)'s
 // scaled log2-rate argument (the chain of mx_x) in *x_sel.
 constexpr int kLaneChunk = 16;  // lines or sites per lane: n1, n2 <= 512
+// KL: the lines or sites a lane holds (n1, n2 <= 32 KL)
+template <int KL>
 __device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
                                       long long* margin, unsigned long long* t_lines, float* x_sel) {
   const int lane = threadIdx.x & 31;
@@ -1735,10 +1748,10 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   const int c2 = (n1 + 31) / 32;
   const int a1 = lane * c2;
   const float* lp = f.lsum + (long long)i0 * n1 * STZ_MODES + m;
-  long long lv[kLaneChunk];
+  long long lv[KL];
   long long S1 = 0;
 #pragma unroll
-  for (int q = 0; q < kLaneChunk; q++) {
+  for (int q = 0; q < KL; q++) {
     lv[q] = (q < c2 && a1 + q < n1) ? fix_f(lp[(a1 + q) * STZ_MODES], e) : 0;
     S1 += lv[q];
   }
@@ -1750,7 +1763,7 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   long long rem2 = 0;
   if (lane == L1) {
     long long hb, ha;
-    const int h = chunk_find<kLaneChunk>(lv, E1, T1, &hb, &ha);
+    const int h = chunk_find<KL>(lv, E1, T1, &hb, &ha);
     i1 = h < 0 ? -1 : a1 + h;
     rem2 = T1 - hb;
   }
@@ -1762,11 +1775,11 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   const long long base = ((long long)i0 * n1 + i1) * n2;
   const int c3 = (n2 + 31) / 32;
   const int a2 = lane * c3;
-  long long rv[kLaneChunk];
-  float xv[kLaneChunk];
+  long long rv[KL];
+  float xv[KL];
   long long S2 = 0;
 #pragma unroll
-  for (int q = 0; q < kLaneChunk; q++) {
+  for (int q = 0; q < KL; q++) {
     xv[q] = 0.f;
     rv[q] = 0;
     if (q < c3 && a2 + q < n2) {
@@ -1786,11 +1799,11 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   float xs = 0.f;
   if (lane == L2) {
     long long hb, ha;
-    const int h = chunk_find<kLaneChunk>(rv, E2, T2, &hb, &ha);
+    const int h = chunk_find<KL>(rv, E2, T2, &hb, &ha);
     site = h < 0 ? -1 : base + a2 + h;
     mg = min(T2 - hb, ha - T2);
 #pragma unroll
-    for (int q = 0; q < kLaneChunk; q++)
+    for (int q = 0; q < KL; q++)
       if (q == h) xs = xv[q];
   }
   site = (long long)__shfl_sync(FULL, (unsigned long long)site, L2);
@@ -1954,7 +1967,10 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       if (pg >= 0) {
         m = (int)(pg / kp.n0);
         const int i0 = (int)(pg - (long long)m * kp.n0);
-        site = search_line_site(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+        const int nl = max(kp.n1, kp.n2);
+        if (nl <= 128) site = search_line_site<4>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+        else if (nl <= 256) site = search_line_site<8>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+        else site = search_line_site<16>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
       }
       if (threadIdx.x == 0) {
         sh_site = site;
@@ -1962,17 +1978,26 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
         sh_margin = (double)mg;
         sh_x = xs;
       }
-    } else if (threadIdx.x == 32) {
-      // the clock advance, while warp 0 searches
-      c->t_kmc = 1.0 / c->total_rate;
+    } else if (threadIdx.x < 64) {
+      // warp 1, while warp 0 searches: the clock advance and the parts of the
+      // commit that need only the mode (level 1 chose it). If the search then
+      // finds no site the step ends in an error and this state is not used.
+      const long long pg = sh_p1;
+      if (pg >= 0) {
+        if (threadIdx.x == 32) c->t_kmc = 1.0 / c->total_rate;
+        __syncwarp();
+        mixed_commit_lanes(kp, c, (int)(pg / kp.n0));
+      }
     }
     __syncthreads();
   }
   const unsigned long long t_search = gtimer();
-  if (threadIdx.x < 32) {
+  if (threadIdx.x >= 64 && threadIdx.x < 96) {
+    // warp 2: the site's eigenstrain, while thread 0 logs the event
+    if (kind == kThermal && sh_site >= 0) mixed_commit_site_lanes(kp, f, sh_site, sh_mode);
+  } else if (threadIdx.x < 32) {
     const long long s = sh_site;
     const int m = sh_mode;
-    if (kind == kThermal && s >= 0) mixed_commit_lanes(kp, f, c, s, m);
     if (threadIdx.x == 0) {
       const double Rtrue = sh_R * kp.rate_scale;
       if (kind == kThermal) {
