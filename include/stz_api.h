@@ -148,7 +148,10 @@ typedef struct stz_params {
                                 set, each with its own barrier field from seed); 0 = the
                                 modes are the first draws of the seed's stream */
   int32_t mode_seed;
-  int32_t reserved[5];
+  int32_t resolve_fp64;      /* mixed: 1 = the field solves (start, periodic re-solves, prints,
+                                avalanches) in FP64; 0 = in FP32 pairs (unevaluated sums of two
+                                floats, about 48 bits, at the FP32 issue rate) */
+  int32_t reserved[4];
 } stz_params;
 
 /* kinds of stz_event */

@@ -44,7 +44,7 @@ class Params(C.Structure):
         ("init_mro", C.c_int32), ("print_period", C.c_int32), ("seed", C.c_uint64),
         ("precision", C.c_int32), ("solver", C.c_int32), ("resolve_period", C.c_int32), ("device", C.c_int32),
         ("log_capacity", C.c_int32), ("mode_seed_set", C.c_int32), ("mode_seed", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("resolve_fp64", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 

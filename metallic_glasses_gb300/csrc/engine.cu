@@ -243,9 +243,11 @@ int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
   return fft_solve(*plan_of(c), a, c->stream, &c->launches);
 }
 
-// FP64 re-solve into the FP32 deviatoric field (mixed form).
+// Full re-solve into the FP32 deviatoric field (mixed form), in FP32 pairs
+// unless the parameters ask for FP64.
 int solve_dev(stz_ctx* c, const double* ebar, const double* uadd, double* err) {
   SolveArgs a{};
+  a.pair = c->p.resolve_fp64 ? 0 : 1;
   a.eps = c->f.eps0;
   a.ebar = ebar;
   a.uadd = uadd;
@@ -609,7 +611,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
     return fail(st);
   }
   // tiles and radix order timed for this grid (once per process and shape)
-  if ((st = fft_autotune(plan, c->stream, c->fft_tuned))) {
+  if ((st = fft_autotune(plan, c->stream, c->fft_tuned, mixed && !c->p.resolve_fp64 ? 1 : 0))) {
     set_error("FFT schedule tuning failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail(st);
   }

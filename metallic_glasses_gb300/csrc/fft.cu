@@ -39,9 +39,49 @@
 namespace stz {
 namespace {
 
+// FP32 pair: the unevaluated sum hi + lo of two floats (|lo| <= half an ulp of
+// hi), about 48 significant bits, with error-free FP32 transformations
+// (Knuth's TwoSum, Dekker's product through an FMA). GB300 issues FP64 at 1/64
+// of its FP32 rate, and an FFT pass in FP64 is bound by that rate; in pairs the
+// same pass runs on the FP32 pipes. A pair and a complex pair take 8 and 16
+// bytes, as a double and a double2 do, so every layout is shared.
+struct dfl {
+  float hi, lo;
+  dfl() = default;
+  __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ dfl(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ dfl df_norm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return dfl(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bp = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+  return df_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return df_norm(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ dfl operator/(dfl a, dfl b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const dfl r = a - dfl(q1, 0.f) * b;
+  return df_norm(q1, __fdiv_rn(r.hi, b.hi));
+}
+struct __align__(16) df2 {
+  dfl x, y;
+};
+
 template <typename T> struct VT;
 template <> struct VT<double> { using V = double2; };
 template <> struct VT<float> { using V = float2; };
+template <> struct VT<dfl> { using V = df2; };
 
 template <typename V> __device__ __forceinline__ V vadd(V a, V b) { return V{a.x + b.x, a.y + b.y}; }
 template <typename V> __device__ __forceinline__ V vsub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
@@ -561,18 +601,23 @@ Sched make_sched_rev(int n) {
   return s;
 }
 
-int upload_twiddles(int n, int count, double2** d64, float2** d32) {
+int upload_twiddles(int n, int count, double2** d64, float2** d32, float4** dpair) {
   std::vector<double2> h(count > 0 ? count : 1);
   std::vector<float2> hf(h.size());
+  std::vector<float4> hp(h.size());
   for (int k = 0; k < count; k++) {
     double ang = -2.0 * M_PI * (double)k / (double)n;
     h[k] = make_double2(std::cos(ang), std::sin(ang));
     hf[k] = make_float2((float)h[k].x, (float)h[k].y);
+    const dfl x(h[k].x), y(h[k].y);
+    hp[k] = make_float4(x.hi, x.lo, y.hi, y.lo);
   }
   if (cudaMalloc(d64, sizeof(double2) * h.size()) != cudaSuccess) return STZ_ERR_NOMEM;
   if (cudaMalloc(d32, sizeof(float2) * h.size()) != cudaSuccess) return STZ_ERR_NOMEM;
+  if (cudaMalloc(dpair, sizeof(float4) * h.size()) != cudaSuccess) return STZ_ERR_NOMEM;
   cudaMemcpy(*d64, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(*d32, hf.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(*dpair, hp.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice);
   return STZ_OK;
 }
 
@@ -626,6 +671,13 @@ struct Tw<float> {
   static const float2* a1(const FFTPlan& p) { return p.tw_1f; }
   static const float2* a0(const FFTPlan& p) { return p.tw_0f; }
   static const float2* post(const FFTPlan& p) { return p.tw_pf; }
+};
+template <>
+struct Tw<dfl> {
+  static const df2* h(const FFTPlan& p) { return reinterpret_cast<const df2*>(p.tw_hd); }
+  static const df2* a1(const FFTPlan& p) { return reinterpret_cast<const df2*>(p.tw_1d); }
+  static const df2* a0(const FFTPlan& p) { return reinterpret_cast<const df2*>(p.tw_0d); }
+  static const df2* post(const FFTPlan& p) { return reinterpret_cast<const df2*>(p.tw_pd); }
 };
 
 template <typename T>
@@ -704,10 +756,10 @@ int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
   if (p->sh.nst < 0 || p->s1.nst < 0 || p->s0.nst < 0) return STZ_ERR_INVALID;
   if (p->h > 4096 || n1 > 1024 || n0 > 1024) return STZ_ERR_INVALID;
   int st;
-  if ((st = upload_twiddles(p->h, p->h, &p->tw_h, &p->tw_hf))) return st;
-  if ((st = upload_twiddles(n1, n1, &p->tw_1, &p->tw_1f))) return st;
-  if ((st = upload_twiddles(n0, n0, &p->tw_0, &p->tw_0f))) return st;
-  if ((st = upload_twiddles(n2, p->nh, &p->tw_p, &p->tw_pf))) return st;
+  if ((st = upload_twiddles(p->h, p->h, &p->tw_h, &p->tw_hf, &p->tw_hd))) return st;
+  if ((st = upload_twiddles(n1, n1, &p->tw_1, &p->tw_1f, &p->tw_1d))) return st;
+  if ((st = upload_twiddles(n0, n0, &p->tw_0, &p->tw_0f, &p->tw_0d))) return st;
+  if ((st = upload_twiddles(n2, p->nh, &p->tw_p, &p->tw_pf, &p->tw_pd))) return st;
   // tiles (FP64 sizes; the FP32 transform uses the same tiles)
   const size_t cz = sizeof(double2);
   p->L_x = std::max(1, 1024 / p->h);
@@ -725,6 +777,7 @@ int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc) {
   size_t sc_max = p->smem_c2r + sizeof(double) * nc * p->L_x * n2;
   set_smem_attrs<double>(p->smem_x, p->smem_y, p->smem_g, sc_max);
   set_smem_attrs<float>(p->smem_x, p->smem_y, p->smem_g, sc_max);
+  set_smem_attrs<dfl>(p->smem_x, p->smem_y, p->smem_g, sc_max);
   return STZ_OK;
 }
 
@@ -754,7 +807,7 @@ struct Tuned {
   int rejected;  // candidates whose result differed from the default schedule's
 };
 std::mutex g_tune_mu;
-std::map<std::array<int, 5>, Tuned> g_tuned;
+std::map<std::array<int, 6>, Tuned> g_tuned;
 
 float time_solve(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1) {
   float best = 1e30f;
@@ -771,10 +824,10 @@ float time_solve(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, cudaEven
 }
 }  // namespace
 
-int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen) {
+int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen, int pair) {
   int dev = 0;
   cudaGetDevice(&dev);
-  const std::array<int, 5> key = {dev, p->n0, p->n1, p->n2, p->nc};
+  const std::array<int, 6> key = {dev, p->n0, p->n1, p->n2, p->nc, pair};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
@@ -812,6 +865,7 @@ int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen) {
   a.sig64 = ref;
   a.spec = spec;
   a.ortho_mean = 1;
+  a.pair = pair;
   fft_solve(*p, a, st, nullptr);
   cudaStreamSynchronize(st);
   std::vector<double> r(n), o(n);
@@ -933,10 +987,12 @@ int fft_c2r_blocks(const FFTPlan& p) { return (int)(((long long)p.n0 * p.n1 + p.
 void fft_plan_destroy(FFTPlan* p) {
   cudaFree(p->tw_h); cudaFree(p->tw_1); cudaFree(p->tw_0); cudaFree(p->tw_p);
   cudaFree(p->tw_hf); cudaFree(p->tw_1f); cudaFree(p->tw_0f); cudaFree(p->tw_pf);
+  cudaFree(p->tw_hd); cudaFree(p->tw_1d); cudaFree(p->tw_0d); cudaFree(p->tw_pd);
   std::memset((void*)p, 0, sizeof(*p));
 }
 
 int fft_solve(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* launches) {
+  if (a.pair) return solve_t<dfl>(p, a, st, launches);
   return a.fp32 ? solve_t<float>(p, a, st, launches) : solve_t<double>(p, a, st, launches);
 }
 

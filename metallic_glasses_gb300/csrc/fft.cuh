@@ -31,6 +31,7 @@ struct FFTPlan {
   // and the real-FFT post twiddle of length n2 (k = 0..h)
   double2 *tw_h = nullptr, *tw_1 = nullptr, *tw_0 = nullptr, *tw_p = nullptr;
   float2 *tw_hf = nullptr, *tw_1f = nullptr, *tw_0f = nullptr, *tw_pf = nullptr;
+  float4 *tw_hd = nullptr, *tw_1d = nullptr, *tw_0d = nullptr, *tw_pd = nullptr;  // FP32 pairs (hi, lo) x 2
   // tiles (lines per block) of each pass
   int L_x = 0, L_y = 0, L_g = 0;
   size_t smem_x = 0, smem_y = 0, smem_g = 0, smem_c2r = 0;
@@ -38,11 +39,12 @@ struct FFTPlan {
 
 int fft_plan_create(FFTPlan* p, int n0, int n1, int n2, int nc);
 // Chooses the tiles (lines per block of each pass) and the radix order of the
-// plan by timing FP64 solves of a fixed eigenstrain, once per device and grid
-// shape per process (cached); a candidate is admitted only if its result
-// equals the default schedule's within 1e-10. chosen (optional, 4 ints): the
-// tiles L_x, L_y, L_g and the number of candidates rejected.
-int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen);
+// plan by timing solves of a fixed eigenstrain in FP64 (pair = 0) or in FP32
+// pairs (pair = 1), once per device, grid shape and precision per process
+// (cached); a candidate is admitted only if its result equals the default
+// schedule's within 1e-10. chosen (optional, 4 ints): the tiles L_x, L_y, L_g
+// and the number of candidates rejected.
+int fft_autotune(FFTPlan* p, cudaStream_t st, int* chosen, int pair);
 // A plan whose twiddle tables are written into caller-provided device storage
 // of at least fft_twiddle_count() elements (FP64 transforms only).
 size_t fft_twiddle_count(int n0, int n1, int n2);
@@ -66,6 +68,7 @@ struct SolveArgs {
   double* msum;          // kOutSig64, optional: per-(component, block) sums of the
                          // solved field, [nc][fft_c2r_blocks] (for the mean stress)
   int fp32;              // run the transform in FP32 (eps converted on load)
+  int pair;              // run the transform in FP32 pairs (about 48 bits; eps split on load)
   void* spec;            // [nc][Nk] complex scratch (double2, or float2 when fp32)
   int ortho_mean;        // 1: the k = 0 term is C:(N ebar - eps_hat(0)) (always 1 here)
 };

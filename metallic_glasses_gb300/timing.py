@@ -28,14 +28,16 @@ def kernel(grid, which, steps, resolve_period=0):
     return {"grid": grid, "which": which, "launch_ms": ms, "launches": n}
 
 
-def solve(grid, reps=5, mixed=True):
-    """FP64 Green's-function re-solves of the full field at grid^3 (the FFT
-    passes), timed with CUDA events. alg_bytes: what one solve must move
+def solve(grid, reps=5, mixed=True, fp64=False):
+    """Green's-function re-solves of the mixed form's full field at grid^3
+    (the FFT passes), in FP32 pairs or (fp64) in FP64, timed with CUDA events.
+    alg_bytes: what one solve must move
     through HBM at least, the full re-solve figure 24 N s with s = 8: the
     eigenstrain read and the field written (8 B per component and site) and
     the half spectrum written and read once (16 B per component and wave
     vector)."""
     p = configs.mixed128(n=grid) if mixed else configs.plain128(n=grid)
+    p.resolve_fp64 = 1 if fp64 else 0
     eng = api.Engine(p)
     eng.solve()
     eng.sync()
@@ -47,7 +49,7 @@ def solve(grid, reps=5, mixed=True):
     eng.close()
     n = grid ** 3
     alg = 6 * n * (8 + 8) + 6 * (grid * grid * (grid // 2 + 1)) * 16 * 2
-    return {"grid": grid, "solve_ms": ms, "alg_bytes": alg, "alg_gbs": alg / (ms / 1e3) / 1e9, "schedule": sch}
+    return {"grid": grid, "precision": "fp64" if fp64 else "fp32 pairs", "solve_ms": ms, "alg_bytes": alg, "alg_gbs": alg / (ms / 1e3) / 1e9, "schedule": sch}
 
 
 def batch(replicas, events, alone=None, seed0=0):
@@ -99,6 +101,7 @@ def main(argv=None):
     sv = sub.add_parser("solve")
     sv.add_argument("--grid", type=int, default=256)
     sv.add_argument("--reps", type=int, default=5)
+    sv.add_argument("--fp64", action="store_true")
     b = sub.add_parser("batch")
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
@@ -107,7 +110,7 @@ def main(argv=None):
     if a.cmd == "kernel":
         out = kernel(a.grid, a.which, a.steps)
     elif a.cmd == "solve":
-        out = solve(a.grid, a.reps)
+        out = solve(a.grid, a.reps, fp64=a.fp64)
     else:
         out = batch(a.replicas, a.events, a.alone)
     print(json.dumps(out), flush=True)

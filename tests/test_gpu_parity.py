@@ -189,3 +189,29 @@ def test_mixed_first_resolve_error_small(engine_lib):
     assert sc["kstep"] == 3 and sc["n_resolves"] == 3
     assert 0 < sc["stress_err_rms_worst"] < 1e-6
     assert sc["stress_err_max_worst"] < 1e-6
+
+
+def test_mixed_pair_resolve_matches_fp64(engine_lib):
+    """The mixed form's field solves in FP32 pairs (the default) against the
+    same solves in FP64 (resolve_fp64 = 1): after the start solve and three
+    periodic re-solves of a 32^3 run the stored FP32 field agrees to within one
+    FP32 rounding, the events are the same, and the measured stress errors of
+    the incremental field agree to 1e-6 of their size (the pair transform
+    carries about 48 bits)."""
+    out = {}
+    for fp64 in (0, 1):
+        p = configs.mixed128(n=32, resolve_period=100)
+        p.resolve_fp64 = fp64
+        e = api.Engine(p)
+        e.run(max_events=300)
+        sc = e.scalars()
+        assert sc["kstep"] == 300 and sc["n_resolves"] == 3
+        out[fp64] = (e.events(), sc, np.stack([e.field(api.FIELD_SDEV, k) for k in range(5)]))
+        e.close()
+    (ea, sa, fa), (eb, sb, fb) = out[0], out[1]
+    for k in ("site", "mode"):
+        assert np.array_equal(ea[k], eb[k]), k
+    scale = np.abs(fb).max()
+    assert np.abs(fa - fb).max() <= 2 ** -23 * scale
+    for k in ("stress_err_rms_worst", "stress_err_max_worst"):
+        assert abs(sa[k] - sb[k]) <= 1e-6 * sb[k] + 1e-13, k
