@@ -268,6 +268,12 @@ int stz_get_scalars(stz_ctx* ctx, stz_scalars* out);
 /* Copy out log entries [first, first+cap) ; *n receives the number copied. */
 int stz_get_events(stz_ctx* ctx, int64_t first, stz_event* out, int64_t cap, int64_t* n);
 int stz_get_field(stz_ctx* ctx, int32_t which, int32_t comp, double* host, int64_t count);
+/* The displacement field u of the current eigenstrain's elastic solution (periodic, zero
+ * mean): dim x N doubles component-major (dim = 2 in REF2D, axis order (j, i) of g in Grad,
+ * init.c:112-140; dim = 3 in GLOBAL3D). Replaces the displacement part of
+ * HomogeneousStressSolver(..., uflag 2) (elastic.c:873-900) and DispField (io.c:137-240); the
+ * supercell position (i (1 + EpsAvg[0]) LX + j EpsAvg[2] LY, ...) is the caller's, as there. */
+int stz_get_displacement(stz_ctx* ctx, double* host, int64_t count);
 int stz_set_field(stz_ctx* ctx, int32_t which, int32_t comp, const double* host, int64_t count);
 /* The FFT schedule the context runs (FFT_MPI_Init's plans, init.c:77-110, are
  * replaced by passes whose tiles and radix order are timed per grid shape):

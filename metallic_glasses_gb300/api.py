@@ -93,6 +93,7 @@ def load_library(path=None):
     lib.stz_set_field.argtypes = [vp, C.c_int32, C.c_int32, vp, C.c_int64]
     lib.stz_set_mean_strain.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_fft_schedule.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.stz_get_displacement.argtypes = [vp, C.c_void_p, C.c_int64]
     lib.stz_elastic_energy.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_sync.argtypes = [vp]
     lib.stz_timer_start.argtypes = [vp]
@@ -196,6 +197,14 @@ class Engine:
         n = C.c_int64()
         _check(self.lib.stz_get_events(self.h, first, out.ctypes.data, count, C.byref(n)))
         return out[:n.value]
+
+    def displacement(self):
+        """The displacement field of the current eigenstrain, [dim][N] (dim = 2
+        in 2D, axis order (j, i); 3 in 3D, axis order (2, 1, 0)), zero mean."""
+        dim = 3 if self.params.n[0] > 1 else 2
+        out = np.empty((dim, self.N), dtype=np.float64)
+        _check(self.lib.stz_get_displacement(self.h, out.ctypes.data, dim * self.N))
+        return out
 
     def field(self, which, comp=0):
         out = np.empty(self.N, dtype=np.float64)

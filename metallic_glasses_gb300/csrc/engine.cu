@@ -843,12 +843,9 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
   if (which == STZ_FIELD_SDEV) {
     if (!c->f.sdev || comp < 0 || comp >= 5) return STZ_ERR_INVALID;
     launch_mixed(c->kp, c->f, 1, c->stream);  // apply the pending update
-    float* tmp = nullptr;
-    if (dalloc(&tmp, (size_t)N)) return STZ_ERR_NOMEM;
     std::vector<float> hf((size_t)N);
     CK(cudaMemcpyAsync(hf.data(), c->f.sdev + (size_t)comp * N, sizeof(float) * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    cudaFree(tmp);
     for (long long s = 0; s < N; s++) host[s] = hf[(size_t)s];
     return STZ_OK;
   }
@@ -883,6 +880,38 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
     sync_ctl(c);
     for (long long s = 0; s < N; s++) host[s] += c->host_ctl.u[comp];
   }
+  return STZ_OK;
+}
+
+// Displacement field of the current eigenstrain (HomogeneousStressSolver with
+// uflag 2, elastic.c:873-900; DispField, io.c:137-240, without the supercell
+// position the caller adds): one FP64 solve whose Green's pass writes
+// u_hat = -i (F - alpha G g)/(mu |k|), into a temporary buffer (print-time only).
+extern "C" int stz_get_displacement(stz_ctx* c, double* host, int64_t count) {
+  if (!c || !host) return STZ_ERR_INVALID;
+  const long long N = c->kp.N;
+  const int dim = c->kp.n0 > 1 ? 3 : 2;
+  if (count != (int64_t)dim * N) return STZ_ERR_INVALID;
+  cudaSetDevice(c->p.device);
+  double* tmp = nullptr;
+  if (dalloc(&tmp, (size_t)dim * N)) return STZ_ERR_NOMEM;
+  SolveArgs a{};
+  a.eps = c->f.eps0;
+  a.lambda = c->kp.lambda;
+  a.mu = c->kp.mu;
+  a.out = kOutSig64;
+  a.sig64 = tmp;
+  a.spec = c->f.spec;
+  a.disp = 1;
+  fft_solve(*plan_of(c), a, c->stream, &c->launches);
+  cudaMemcpyAsync(host, tmp, sizeof(double) * dim * N, cudaMemcpyDeviceToHost, c->stream);
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) {
+    set_error("displacement solve: %s", cudaGetErrorString(e));
+    return STZ_ERR_CUDA;
+  }
+  c->d2h_bytes += (int64_t)sizeof(double) * dim * N;
   return STZ_OK;
 }
 

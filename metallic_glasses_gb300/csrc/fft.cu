@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(256) k_c2c_axis(typename VT<T>::V* __restrict_
 // ------------------------------------------------------------- Green's pass
 struct GreenArgs {
   int nc, is3d, n0, n1, n2, nh;
+  int disp;  // write the displacement spectrum (components 0 .. dim-1) instead of the stress
   double lambda, mu;
   double Ntot;
 };
@@ -320,6 +321,38 @@ __device__ __forceinline__ void green_op(int nc, T lam, T mu, T alpha, const T* 
   apply_C<T, V>(nc, lam, mu, d, sig);
 }
 
+// Displacement of the same solution, u_hat = -i (F - alpha G g) / (mu |k|) for
+// each axis a < dim (HomogeneousStressSolver with uflag 2, elastic.c:873-900:
+// HadamardSumnSProd then HadamardSiDivd with g2 = |k|; DispField, io.c:187-205,
+// is the same formula); F and G as in green_op, inv_k = 1/|k|.
+template <typename T, typename V>
+__device__ __forceinline__ void disp_op(int nc, T lam, T mu, T alpha, const T* g, T inv_k, const V* e, V* u) {
+  V tau[6];
+  apply_C<T, V>(nc, lam, mu, e, tau);
+  V t[3][3];
+  if (nc == 3) {
+    t[0][0] = tau[0]; t[1][1] = tau[1]; t[0][1] = t[1][0] = tau[2];
+    t[2][2] = t[0][2] = t[2][0] = t[1][2] = t[2][1] = V{0, 0};
+  } else {
+    t[0][0] = tau[0]; t[1][1] = tau[1]; t[2][2] = tau[2];
+    t[1][2] = t[2][1] = tau[3];
+    t[0][2] = t[2][0] = tau[4];
+    t[0][1] = t[1][0] = tau[5];
+  }
+  V F[3];
+  for (int a = 0; a < 3; a++) {
+    F[a] = V{t[a][0].x * g[0] + t[a][1].x * g[1] + t[a][2].x * g[2],
+             t[a][0].y * g[0] + t[a][1].y * g[1] + t[a][2].y * g[2]};
+  }
+  V G = V{g[0] * F[0].x + g[1] * F[1].x + g[2] * F[2].x, g[0] * F[0].y + g[1] * F[1].y + g[2] * F[2].y};
+  const T s = inv_k / mu;
+  const int dim = nc == 3 ? 2 : 3;
+  for (int a = 0; a < dim; a++) {
+    const V w = V{F[a].x - alpha * G.x * g[a], F[a].y - alpha * G.y * g[a]};
+    u[a] = V{s * w.y, -s * w.x};
+  }
+}
+
 __device__ __forceinline__ double wrapf(int k, int n) {
   double s = (double)k * (1.0 / n);
   return s - round(s);
@@ -365,7 +398,33 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
     }
     V e[6], sig[6];
     for (int c = 0; c < nc; c++) e[c] = res[(c * L + l) * ld + p];
-    if (k0 == 0 && k1 == 0 && k2 == 0) {
+    if (ga.disp) {
+      // displacement components 0 .. dim-1; zero at k = 0
+      for (int c = 0; c < nc; c++) sig[c] = V{0, 0};
+      if (k0 != 0 || k1 != 0 || k2 != 0) {
+        const double f2 = wrapf(k2, ga.n2), f1 = wrapf(k1, ga.n1), f0 = ga.is3d ? wrapf(k0, ga.n0) : 0.0;
+        const double gn = sqrt(f2 * f2 + f1 * f1 + f0 * f0);
+        T g[3] = {(T)(f2 / gn), (T)(f1 / gn), (T)(f0 / gn)};
+        const T inv_k = (T)(1.0 / (6.28318530717958647692 * gn));
+        const bool ny2 = (ga.n2 % 2 == 0) && (2 * k2 == ga.n2);
+        const bool ny1 = (ga.n1 % 2 == 0) && (2 * k1 == ga.n1);
+        const bool ny0 = ga.is3d && (ga.n0 % 2 == 0) && (2 * k0 == ga.n0);
+        // the Hermitian part of the reference's operator: the average over
+        // the sign choices of the Nyquist components, as for the stress
+        int nv = 0;
+        for (int sg = 0; sg < 8; sg++) {
+          if (((sg & 1) && !ny2) || ((sg & 2) && !ny1) || ((sg & 4) && !ny0)) continue;
+          if (nc == 3 && sg != 0 && sg != ((ny2 ? 1 : 0) | (ny1 ? 2 : 0))) continue;  // 2D: all flipped together
+          T gm[3] = {(sg & 1) ? -g[0] : g[0], (sg & 2) ? -g[1] : g[1], (sg & 4) ? -g[2] : g[2]};
+          V u2[3];
+          disp_op<T, V>(nc, lam, mu, alpha, gm, inv_k, e, u2);
+          for (int c = 0; c < (nc == 3 ? 2 : 3); c++) sig[c] = vadd(sig[c], u2[c]);
+          nv++;
+        }
+        const T inv = (T)1 / (T)nv;
+        for (int c = 0; c < nc; c++) sig[c] = V{sig[c].x * inv, sig[c].y * inv};
+      }
+    } else if (k0 == 0 && k1 == 0 && k2 == 0) {
       V d[6];
       for (int c = 0; c < nc; c++) {
         const T eb = ebar ? (T)(ga.Ntot * ebar[c]) : (T)0;
@@ -697,6 +756,9 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   ga.n0 = p.n0; ga.n1 = p.n1; ga.n2 = p.n2; ga.nh = p.nh;
   ga.lambda = a.lambda; ga.mu = a.mu;
   ga.Ntot = (double)p.N;
+  ga.disp = a.disp;
+  // components left for the inverse passes: the displacement has one per axis
+  const int nco = a.disp ? (p.n0 > 1 ? 3 : 2) : p.nc;
   if (p.n0 > 1) {
     // axis 1, forward
     const long long inner = p.nh;
@@ -710,8 +772,9 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
     k_green<T><<<gg, TH, p.smem_g, st>>>(spec, p.n0, inner0, inner0, p.Nk, p.L_g, p.s0, Tw<T>::a0(p), ga, a.ebar,
                                           a.gate);
     // axis 1, inverse
-    k_c2c_axis<T, +1><<<gy, TH, p.smem_y, st>>>(spec, p.n1, p.nh, inner, (long long)p.n1 * p.nh, ntile, p.Nk,
-                                                  p.L_y, p.s1, Tw<T>::a1(p), a.gate);
+    k_c2c_axis<T, +1><<<dim3(gy.x, (unsigned)nco), TH, p.smem_y, st>>>(spec, p.n1, p.nh, inner,
+                                                                         (long long)p.n1 * p.nh, ntile, p.Nk, p.L_y,
+                                                                         p.s1, Tw<T>::a1(p), a.gate);
     nl += 3;
   } else {
     const long long inner = p.nh;
@@ -724,7 +787,7 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   size_t sc = p.smem_c2r;
   if (a.out == kOutDev32) sc += sizeof(double) * (size_t)p.nc * p.L_x * p.n2;
   if (a.out == kOutSig64)
-    k_c2r_x<T, kOutSig64><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
+    k_c2r_x<T, kOutSig64><<<gx.x, TH, sc, st>>>(spec, nco, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, a.sig64, nullptr, nullptr,
                                                nullptr, nullptr, a.msum, a.gate);
   else if (a.out == kOutSig32)

@@ -69,6 +69,8 @@ struct SolveArgs {
                          // solved field, [nc][fft_c2r_blocks] (for the mean stress)
   int fp32;              // run the transform in FP32 (eps converted on load)
   int pair;              // run the transform in FP32 pairs (about 48 bits; eps split on load)
+  int disp;              // kOutSig64 only: write the displacement field ([dim][N], dim = 2 in 2D,
+                         // 3 in 3D; zero mean) instead of the stress
   void* spec;            // [nc][Nk] complex scratch (double2, or float2 when fp32)
   int ortho_mean;        // 1: the k = 0 term is C:(N ebar - eps_hat(0)) (always 1 here)
 };

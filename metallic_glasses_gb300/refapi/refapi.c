@@ -25,10 +25,13 @@
  * as in the reference: the engine's internal print test is switched off, so
  * the globals after KMC() hold the state before that re-solve.
  *
- * Not provided: the displacement field of the uflag-2 solve (XR is left at
- * zero), SOC counters (UpdateSOC leaves main's arrays as they are), spatially
- * varying Lambda/Mu (the solve is homogeneous; a non-uniform field is
- * reported), MRO maps, residual-stress generation.
+ * The uflag-1/2 solves and DispField fill the positions XR: the engine's
+ * displacement field of the eigenstrain plus the supercell position, as
+ * elastic.c:866-900 and io.c:137-240 write them.
+ *
+ * Not provided: SOC counters (UpdateSOC leaves main's arrays as they are),
+ * spatially varying Lambda/Mu (the solve is homogeneous; a non-uniform field
+ * is reported), MRO maps, residual-stress generation.
  */
 #include <math.h>
 #include <stdio.h>
@@ -283,6 +286,23 @@ static void solve_into(real** epso, real** sigmao, real* stress, real* epsavg) {
   }
 }
 
+/* Positions of the print step (elastic.c:866-870, io.c:151-155 and 204):
+ * the supercell position with the mean strain epsavg plus the displacement
+ * field of the current eigenstrain from the engine. */
+static void positions(real** xr, const real* epsavg) {
+  real* u = (real*)malloc(sizeof(real) * 2 * NXY);
+  if (!u) fail("malloc", STZ_ERR_NOMEM);
+  int st = stz_get_displacement(g_ctx, u, (int64_t)2 * NXY);
+  if (st) fail("stz_get_displacement", st);
+  for (int i = 0; i < lnx; i++)
+    for (int j = 0; j < NY; j++) {
+      const int idx = i * NY + j;
+      xr[0][idx] = (i + lxs) * (1 + epsavg[0]) * LX + j * epsavg[2] * LY + u[idx];
+      xr[1][idx] = (i + lxs) * epsavg[2] * LX + j * (1 + epsavg[1]) * LY + u[NXY + idx];
+    }
+  free(u);
+}
+
 #ifdef INHOM_ELAST
 /* elastic.c:977-1066 with uniform moduli: one homogeneous solve */
 void InhomogeneousStressSolver(real* Lambdao, real* Muo, real** eps0o, real* epsavg, real lambda_, real mu_,
@@ -298,8 +318,7 @@ void InhomogeneousStressSolver(real* Lambdao, real* Muo, real** eps0o, real* eps
       }
   }
   solve_into(epso, sigmao, stress, epsavg);
-  if (uflag == 2 && uo)
-    for (int s = 0; s < NXY; s++) uo[0][s] = uo[1][s] = 0.0;
+  if (uflag != 0 && uo) positions(uo, epsavg);
 }
 
 /* elastic.c:779-900 */
@@ -309,19 +328,15 @@ void HomogeneousStressSolver(real lambda_, real mu_, real** eps0o, real* epsavg,
   (void)mu_;
   (void)eps0o;
   solve_into(epso, sigmao, stress, epsavg);
-  if (uflag == 2 && uo)
-    for (int s = 0; s < NXY; s++) uo[0][s] = uo[1][s] = 0.0;
+  if (uflag != 0 && uo) positions(uo, epsavg);
 }
 #endif
 
 /* elastic.c: the solve on the global fields */
 void HomStressSolver(void) { solve_into(TotEps, Sigma, Stress, EpsAvg); }
 
-/* io.c: displacement field of the print step (not computed: zero) */
-void DispField(real* xr[2]) {
-  solve_into(TotEps, Sigma, Stress, EpsAvg);
-  for (int s = 0; s < NXY; s++) xr[0][s] = xr[1][s] = 0.0;
-}
+/* io.c:137-240: positions of the print step from Eps0 and EpsAvg */
+void DispField(real* xr[2]) { positions(xr, EpsAvg); }
 
 /* ------------------------------------------------------------- the step */
 

@@ -12,6 +12,10 @@ directory and stores, per case:
                sigma, eps0  float64 [3, N]  final stress and eigenstrain
                tlast, perm_soft, temp_soft  float64 [N]
                deps_sum   float64 [3] sum over modes and sites of DEps0[m][c]
+               xr         float64 [P, 2, N] the positions the reference's main
+                                   wrote at P = 4 of its prints spread over the
+                                   run (X1R/X2R files, "%lf" text: 6 decimals)
+               xr_k       int64 [P]  their print numbers (the files' %03d)
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz).
 
 Only this script reads the reference tree; tests read the .npz files.
@@ -75,12 +79,21 @@ def run_case(name, nx, ny, loading, overrides, events):
     tlast = take(N)
     perm = take(N)
     temp = take(N)
+    # the reference main's print files X1R%03d_P00.out / X2R%03d_P00.out:
+    # four prints spread over the run
+    n_prints = 0
+    while os.path.exists(os.path.join(d, "X1R%03d_P00.out" % (n_prints + 1))):
+        n_prints += 1
+    xr_k = sorted({max(1, n_prints // 8), max(1, n_prints // 3), max(1, 2 * n_prints // 3), n_prints})
+    xr = [[np.loadtxt(os.path.join(d, "X%dR%03d_P00.out" % (a, k))).reshape(-1) for a in (1, 2)] for k in xr_k]
+    xr = np.array(xr, np.float64).reshape(len(xr_k), 2, N)
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
     np.savez_compressed(out, X=np.array(X, np.int64), S=S[:, :3], S10=S[::10], hdr=hdr, sc=sc, sigma=sigma,
                         eps0=eps0, tlast=tlast, perm_soft=perm, temp_soft=temp, deps_sum=deps.sum(axis=(0, 2)),
-                        nx=nx, ny=ny, loading=loading, overrides=repr(overrides), events=events)
+                        nx=nx, ny=ny, loading=loading, overrides=repr(overrides), events=events, xr=xr,
+                        xr_k=np.array(xr_k, np.int64))
     print(name, "transforms", len(X), "steps", len(S), "hdr", hdr, "->", out)
 
 

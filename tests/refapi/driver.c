@@ -4,6 +4,10 @@
  *   steps.txt   per driver step: step kind time EpsAvg[3] Stress[3]
  *               (kind 0 thermal, 1 athermal, 2 elastic)
  *   events.txt  per transformation: step kind site mode (from the engine log)
+ *   X1R%03d_P00.out, X2R%03d_P00.out  the positions XR of the prints listed in
+ *               REFAPI_XR_PRINTS (comma-separated print numbers; all prints when
+ *               unset), named and formatted as the reference's main writes them
+ *               (bmg.c:300-330)
  * in the working directory, which holds the reference's "input" file. */
 #define BMG_GLOBALS_ONCE
 #include "bmg.h"
@@ -36,6 +40,8 @@ int main(int argc, char** argv) {
   InhomogeneousStressSolver(Lambda, Mu, Eps0, EpsAvg, lambda, mu, XR, TotEps, Sigma, Stress, 0);
   FILE* fs = fopen("steps.txt", "w");
   real last_print = 0.0;
+  int n_print = 1;
+  const char* xr_list = getenv("REFAPI_XR_PRINTS");
 #ifdef TENSION
   const int lc = 0;
 #else
@@ -70,6 +76,27 @@ int main(int argc, char** argv) {
           for (j = 0; j < NY; j++) Q0[m][i * NY + j] = Q1[m][i * NY + j];
       RecordFree();
       InhomogeneousStressSolver(Lambda, Mu, Eps0, EpsAvg, lambda, mu, XR, TotEps, Sigma, Stress, 2);
+      n_print++;
+      int want = !xr_list;
+      if (xr_list) {
+        const char* q = xr_list;
+        while (*q && !want) {
+          if (atoi(q) == n_print - 1) want = 1;
+          while (*q && *q != ',') q++;
+          if (*q == ',') q++;
+        }
+      }
+      for (int a = 0; a < 2 && want; a++) {
+        char fname[64];
+        sprintf(fname, "X%dR%03d_P%02d.out", a + 1, n_print - 1, rank);
+        FILE* fx = fopen(fname, "w");
+        if (!fx) { perror(fname); return 2; }
+        for (i = 0; i < lnx; i++) {
+          for (j = 0; j < NY; j++) fprintf(fx, "%lf ", XR[a][i * NY + j]);
+          fprintf(fx, "\n");
+        }
+        fclose(fx);
+      }
     }
     if (kstep >= max_events) break;
 #ifdef TENSION

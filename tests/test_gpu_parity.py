@@ -215,3 +215,36 @@ def test_mixed_pair_resolve_matches_fp64(engine_lib):
     assert np.abs(fa - fb).max() <= 2 ** -23 * scale
     for k in ("stress_err_rms_worst", "stress_err_max_worst"):
         assert abs(sa[k] - sb[k]) <= 1e-6 * sb[k] + 1e-13, k
+
+
+def test_displacement_gradient_is_the_solved_strain_3d(engine_lib):
+    """3D displacement field (no reference code exists in 3D): its spectral
+    symmetric gradient equals the fluctuation of the total strain of the stress
+    solve, C^-1:sigma + eps*, on every wave vector off the Nyquist planes (where
+    the operator is the average of the sign choices)."""
+    p = configs.plain128(n=16)
+    e = api.Engine(p)
+    e.run(max_events=40)
+    u = e.displacement()
+    sig = np.stack([e.field(api.FIELD_SIGMA, c) for c in range(6)])
+    eps0 = np.stack([e.field(api.FIELD_EPS0, c) for c in range(6)])
+    e.close()
+    lam, mu, n = p.lambda_, p.mu, 16
+    assert np.abs(u.mean(axis=1)).max() <= 1e-12 * np.abs(u).max()
+    tr = sig[0] + sig[1] + sig[2]
+    eps = np.empty_like(sig)
+    eps[:3] = (sig[:3] - lam / (3 * lam + 2 * mu) * tr) / (2 * mu)
+    eps[3:] = sig[3:] / (2 * mu)  # tensor shear components
+    eps += eps0
+    f = np.fft.fftfreq(n)
+    f0, f1, f2 = np.meshgrid(f, f, f, indexing="ij")
+    k = [2 * np.pi * f2, 2 * np.pi * f1, 2 * np.pi * f0]  # x = axis 2, y = axis 1, z = axis 0
+    mask = (np.abs(f0) < 0.5) & (np.abs(f1) < 0.5) & (np.abs(f2) < 0.5)
+    mask[0, 0, 0] = False  # the mean strain is not a gradient
+    U = [np.fft.fftn(u[a].reshape(n, n, n)) for a in range(3)]
+    pairs = [(0, 0), (1, 1), (2, 2), (1, 2), (0, 2), (0, 1)]  # xx yy zz yz xz xy
+    scale = np.abs(eps - eps.mean(axis=1, keepdims=True)).max()
+    for c, (a, b) in enumerate(pairs):
+        grad = np.real(np.fft.ifftn(0.5j * (k[a] * U[b] + k[b] * U[a]) * mask))
+        want = np.real(np.fft.ifftn(np.fft.fftn(eps[c].reshape(n, n, n)) * mask))
+        assert np.abs(grad - want).max() <= 1e-9 * scale, c

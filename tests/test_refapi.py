@@ -8,7 +8,8 @@ GPU: the test driver, which follows the reference main's call sequence
 (ReadInput ... Alloc, Energy_Init, DStrain, solve, then per step ActEnergy,
 the Q < 0 scan, athermal_plasticity or KMC, ElasticEnergy, the print-time
 RecordPrep / Q0 reset / uflag-2 solve), reproduces the reference's own
-(step, kind, site, mode) sequence of the 32x32 tension fixture and its clock.
+(step, kind, site, mode) sequence of the 32x32 tension fixture, its clock and
+the positions XR (supercell position plus displacement field) its prints write.
 """
 import os
 import subprocess
@@ -71,12 +72,15 @@ def test_driver_reproduces_reference_events(engine_lib):
     with tempfile.TemporaryDirectory() as d:
         exe = build_driver(os.path.join(d, "driver"))
         configs.write_input(os.path.join(d, "input"), end="0.5", seed="5", soft="0")
-        env = dict(os.environ, REFAPI_MAX_EVENTS=str(int(hdr[2])))
+        env = dict(os.environ, REFAPI_MAX_EVENTS=str(int(hdr[2])),
+                   REFAPI_XR_PRINTS=",".join(str(int(k)) for k in g["xr_k"]))
         r = subprocess.run([exe], cwd=d, env=env, capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
         ev = np.loadtxt(os.path.join(d, "events.txt"), dtype=np.int64, ndmin=2)
         steps = np.loadtxt(os.path.join(d, "steps.txt"), ndmin=2)
         actq = np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2)
+        xr = np.array([[np.loadtxt(os.path.join(d, "X%dR%03d_P00.out" % (a, int(k)))).reshape(-1) for a in (1, 2)]
+                       for k in g["xr_k"]])
     X = g["X"]
     assert ev.shape == X.shape
     for col, name in enumerate(("step", "kind", "site", "mode")):
@@ -97,3 +101,8 @@ def test_driver_reproduces_reference_events(engine_lib):
     thermal = X[X[:, 1] == 0]
     assert len(actq) == len(thermal)
     assert np.array_equal(actq[:, 0].astype(np.int64), thermal[:, 3])
+    # the print files' positions: supercell position plus the displacement
+    # field (up to ~1 nm here), both written with 6 decimals
+    ref_xr = g["xr"]
+    assert xr.shape == ref_xr.shape
+    assert np.abs(xr - ref_xr).max() <= 2e-6
