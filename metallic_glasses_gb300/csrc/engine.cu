@@ -1119,7 +1119,7 @@ struct stz_batch {
   std::vector<stz::BatchStatus> h_status;
   int total_blocks = 0;
   int max_n0 = 1;  // largest plane count (grid x of the plane-sum kernel)
-  int max_n2 = 4;  // longest line (shared memory of the batched main kernel)
+  stz::BatchLaunch bl;  // per line-length class: block range, longest line, stream
   int shared_modes = 0;  // every replica has the same modes (kernel-parameter path)
   stz::ModeSet modes{};
   cudaGraphExec_t graph = nullptr;
@@ -1134,6 +1134,11 @@ extern "C" void stz_batch_destroy(stz_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   for (stz_ctx* c : b->reps) stz_destroy(c);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (int c = 0; c < stz::kBatchClasses; c++) {
+    if (b->bl.side[c]) cudaStreamDestroy(b->bl.side[c]);
+    if (b->bl.join[c]) cudaEventDestroy(b->bl.join[c]);
+  }
+  if (b->bl.fork) cudaEventDestroy(b->bl.fork);
   cudaFree(b->d_desc);
   cudaFree(b->d_blk_rep);
   cudaFree(b->d_rep_first);
@@ -1169,14 +1174,29 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
   cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   std::vector<stz::BatchDesc> desc(count);
   std::vector<int> blk_rep, first(count);
+  // blocks grouped by line-length class, replicas in order within a class
+  for (int c = 0; c < stz::kBatchClasses; c++) {
+    b->bl.start[c] = (int)blk_rep.size();
+    for (int i = 0; i < count; i++) {
+      const stz::KParams& kp = b->reps[i]->kp;
+      if (stz::batch_class(kp.n2) != c) continue;
+      first[i] = (int)blk_rep.size();
+      for (int k = 0; k < kp.nblk; k++) blk_rep.push_back(i);
+      b->bl.max_n2[c] = std::max(b->bl.max_n2[c], kp.n2);
+    }
+    b->bl.count[c] = (int)blk_rep.size() - b->bl.start[c];
+  }
   for (int i = 0; i < count; i++) {
     desc[i].kp = b->reps[i]->kp;
     desc[i].f = b->reps[i]->f;
-    first[i] = (int)blk_rep.size();
-    for (int k = 0; k < b->reps[i]->kp.nblk; k++) blk_rep.push_back(i);
     b->min_log_cap = i == 0 ? b->reps[i]->kp.log_cap : std::min<int64_t>(b->min_log_cap, b->reps[i]->kp.log_cap);
   }
   b->total_blocks = (int)blk_rep.size();
+  cudaEventCreateWithFlags(&b->bl.fork, cudaEventDisableTiming);
+  for (int c = 0; c < stz::kBatchClasses; c++) {
+    cudaStreamCreateWithFlags(&b->bl.side[c], cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&b->bl.join[c], cudaEventDisableTiming);
+  }
   // one mode set for every replica: the batched kernel takes it as parameters
   b->shared_modes = 1;
   for (auto* c : b->reps)
@@ -1185,11 +1205,7 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
   std::memcpy(b->modes.mdev2, b->reps[0]->kp.mdev2, sizeof(b->modes.mdev2));
   std::memcpy(b->modes.mdev_raw, b->reps[0]->kp.mdev_raw, sizeof(b->modes.mdev_raw));
   b->max_n0 = 1;
-  b->max_n2 = 4;
-  for (auto* c : b->reps) {
-    b->max_n0 = std::max(b->max_n0, c->kp.n0);
-    b->max_n2 = std::max(b->max_n2, c->kp.n2);
-  }
+  for (auto* c : b->reps) b->max_n0 = std::max(b->max_n0, c->kp.n0);
   int st = STZ_OK;
   if ((st = dalloc(&b->d_desc, (size_t)count)) || (st = dalloc(&b->d_blk_rep, blk_rep.size())) ||
       (st = dalloc(&b->d_rep_first, (size_t)count)) || (st = dalloc(&b->d_status, (size_t)count))) {
@@ -1218,9 +1234,8 @@ int batch_capture(stz_batch* b, int rounds) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int r = 0; r < rounds; r++)
-    launch_mixed_batched(b->d_desc, b->d_blk_rep, b->d_rep_first, b->total_blocks, b->d_status,
-                         (int)b->reps.size(), b->max_n0, b->max_n2, b->shared_modes ? &b->modes : nullptr,
-                         b->stream);
+    launch_mixed_batched(b->d_desc, b->d_blk_rep, b->d_rep_first, b->bl, b->d_status, (int)b->reps.size(),
+                         b->max_n0, b->shared_modes ? &b->modes : nullptr, b->stream);
   CK(cudaStreamEndCapture(b->stream, &g));
   CK(cudaGraphInstantiate(&b->graph, g, 0));
   cudaGraphDestroy(g);

@@ -1132,23 +1132,24 @@ __device__ __forceinline__ void mixed_rates2(const float* sa, float aa, const fl
   }
 }
 
-// The 20 rates of four sites of a lane (all inside the line), one
-// coefficient pair load per four FP32x2 FMAs; each site's lane of a pair is
-// the scalar chain of mx_x, and the sums take sites 0, 1, 2, 3 in order.
-__device__ __forceinline__ void mixed_rates4(const float (*t)[5], const float* a, const float2* md, float2* acc2) {
+// The 20 rates of Q sites of a lane (all inside the line), one coefficient
+// pair load per Q FP32x2 FMAs; each site's lane of a pair is the scalar chain
+// of mx_x, and the sums take sites 0 .. Q-1 in order.
+template <int Q>
+__device__ __forceinline__ void mixed_rates_q(const float (*t)[5], const float* a, const float2* md, float2* acc2) {
 #pragma unroll
   for (int j = 0; j < STZ_MODES / 2; j++) {
-    float2 x[4];
+    float2 x[Q];
 #pragma unroll
-    for (int q = 0; q < 4; q++) x[q] = make_float2(a[q], a[q]);
+    for (int q = 0; q < Q; q++) x[q] = make_float2(a[q], a[q]);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       const float2 c = md[5 * j + k];
 #pragma unroll
-      for (int q = 0; q < 4; q++) x[q] = __ffma2_rn(make_float2(t[q][k], t[q][k]), c, x[q]);
+      for (int q = 0; q < Q; q++) x[q] = __ffma2_rn(make_float2(t[q][k], t[q][k]), c, x[q]);
     }
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(x[q].x), ex2_approx(x[q].y)));
+    for (int q = 0; q < Q; q++) acc2[j] = __fadd2_rn(acc2[j], make_float2(ex2_approx(x[q].x), ex2_approx(x[q].y)));
   }
 }
 
@@ -1268,12 +1269,12 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
   dl[6] = sz;
   dl[7] = sy;
   const int base = (i0 * kp.n1 + i1) * n2;
-  if (N2 == 128 && LINEVOTE && !UPDATE_ONLY) {
-    // each lane's four sites lane + 32 q in one pass; offsets are immediates
-    constexpr int kKt2 = N2 / 2 + 1;
-    float t[4][5], a[4];
+  if constexpr (N2 > 0 && LINEVOTE && !UPDATE_ONLY) {
+    // each lane's N2 / 32 sites lane + 32 q in one pass; offsets are immediates
+    constexpr int kKt2 = N2 / 2 + 1, kQ = N2 / 32;
+    float t[kQ][5], a[kQ];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < kQ; q++) {
       const int i2 = lane + 32 * q;
       int fx;
       const int d2 = fold(i2 - p2, N2, &fx);
@@ -1285,7 +1286,7 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
       for (int k = 0; k < 5; k++) t[q][k] = __fmul_rn(sv[k], kp.inv_kt);
       a[q] = (kp.q_ref - stage[5 * N2 + i2]) * kp.a_scale;
     }
-    mixed_rates4(t, a, md, acc2);
+    mixed_rates_q<kQ>(t, a, md, acc2);
     return;
   }
   for (int i2 = lane; i2 < n2; i2 += 64) {
@@ -2119,21 +2120,28 @@ __device__ __forceinline__ void load_desc(const BatchDesc* d, int r, KParams* sk
 // SHARED: every replica has the same modes, passed as kernel parameters
 // (constant-bank operands) instead of being read from each block's copy of
 // its replica's constants in shared memory.
-template <int SHARED>
+// N2: the line length of every replica of this launch (0: any); blk_off:
+// the first block of this launch in blk_rep.
+template <int SHARED, int N2>
 __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __restrict__ d,
                                                           const int* __restrict__ blk_rep,
-                                                          const int* __restrict__ rep_first, ModeSet ms) {
+                                                          const int* __restrict__ rep_first, int blk_off,
+                                                          ModeSet ms) {
   __shared__ KParams skp;
   __shared__ Fields sf;
   pdl_wait();
-  const int r = blk_rep[blockIdx.x];
+  const int blk = blockIdx.x + blk_off;
+  const int r = blk_rep[blk];
   if (d[r].f.ctl->halt) return;  // a halted replica's blocks skip the copy
   load_desc(d, r, &skp, &sf);
   extern __shared__ __align__(128) float mix_smem[];
+  // lines of a known length: the pass specialised to it, with the athermal
+  // test per line; otherwise the general pass with the per-site maximum
+  constexpr int LV = N2 > 0 ? 1 : 0;
   if (SHARED)
-    mixed_main_body<0, 0>(skp, sf, blockIdx.x - rep_first[r], &ms.mdev2[0][0], ms.mdev_raw, mix_smem);
+    mixed_main_body<0, LV, N2>(skp, sf, blk - rep_first[r], &ms.mdev2[0][0], ms.mdev_raw, mix_smem);
   else
-    mixed_main_body<0, 0>(skp, sf, blockIdx.x - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
+    mixed_main_body<0, LV, N2>(skp, sf, blk - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
 }
 
 // Plane sums and selection of a batch: block (x, r) sums plane x of replica
@@ -2270,8 +2278,16 @@ static void mixed_smem_init() {
   raise((const void*)k_mixed<0>);
   raise((const void*)k_mixed<0, 128>);
   raise((const void*)k_mixed<1>);
-  raise((const void*)k_mixed_batched<0>);
-  raise((const void*)k_mixed_batched<1>);
+  raise((const void*)k_mixed<0, 64>);
+  raise((const void*)k_mixed<0, 96>);
+  raise((const void*)k_mixed_batched<0, 0>);
+  raise((const void*)k_mixed_batched<1, 0>);
+  raise((const void*)k_mixed_batched<0, 64>);
+  raise((const void*)k_mixed_batched<1, 64>);
+  raise((const void*)k_mixed_batched<0, 96>);
+  raise((const void*)k_mixed_batched<1, 96>);
+  raise((const void*)k_mixed_batched<0, 128>);
+  raise((const void*)k_mixed_batched<1, 128>);
 }
 
 size_t mixed_smem(int n2) { return mix_smem_bytes(n2); }
@@ -2307,22 +2323,60 @@ void launch_pdl(void (*kern)(A...), dim3 grid, size_t smem, cudaStream_t st, A..
 }
 }  // namespace
 
-void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, int max_n0, int max_n2, const ModeSet* shared,
-                          cudaStream_t st) {
+int batch_class(int n2) {
+  for (int c = 0; c < kBatchClasses - 1; c++)
+    if (kBatchClassN2[c] == n2) return c;
+  return kBatchClasses - 1;
+}
+
+namespace {
+template <int N2>
+void launch_batched_class(const BatchDesc* d, const int* blk_rep, const int* rep_first, int start, int count,
+                          int max_n2, const ModeSet* shared, cudaStream_t s) {
+  const size_t smem = mix_smem_bytes(max_n2);
+  if (shared) k_mixed_batched<1, N2><<<count, TH, smem, s>>>(d, blk_rep, rep_first, start, *shared);
+  else k_mixed_batched<0, N2><<<count, TH, smem, s>>>(d, blk_rep, rep_first, start, ModeSet{});
+}
+}  // namespace
+
+void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, const BatchLaunch& bl,
+                          BatchStatus* status, int nrep, int max_n0, const ModeSet* shared, cudaStream_t st) {
   mixed_smem_init();
-  if (shared)
-    launch_pdl(k_mixed_batched<1>, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first, *shared);
-  else
-    launch_pdl(k_mixed_batched<0>, dim3(total_blocks), mix_smem_bytes(max_n2), st, d, blk_rep, rep_first,
-               ModeSet{});
-  launch_pdl(k_mixed_select_batched, dim3(max_n0, nrep), 0, st, d, status);
+  // the classes run side by side: the first on st, the others on side
+  // streams that fork from st and join it before the selection
+  int first = -1;
+  cudaEventRecord(bl.fork, st);
+  for (int c = 0; c < kBatchClasses; c++) {
+    if (bl.count[c] <= 0) continue;
+    cudaStream_t s = st;
+    if (first < 0) {
+      first = c;
+    } else {
+      s = bl.side[c];
+      cudaStreamWaitEvent(s, bl.fork, 0);
+    }
+    switch (kBatchClassN2[c]) {
+      case 64: launch_batched_class<64>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s); break;
+      case 96: launch_batched_class<96>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s); break;
+      case 128:
+        launch_batched_class<128>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s);
+        break;
+      default: launch_batched_class<0>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s);
+    }
+    if (s != st) {
+      cudaEventRecord(bl.join[c], s);
+      cudaStreamWaitEvent(st, bl.join[c], 0);
+    }
+  }
+  k_mixed_select_batched<<<dim3(max_n0, nrep), TH, 0, st>>>(d, status);
 }
 
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   mixed_smem_init();
   if (update_only) k_mixed<1><<<kp.nblk, TH, mix_smem_bytes(kp.n2), st>>>(kp, f);
   else if (kp.n2 == 128) launch_pdl(k_mixed<0, 128>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
+  else if (kp.n2 == 96) launch_pdl(k_mixed<0, 96>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
+  else if (kp.n2 == 64) launch_pdl(k_mixed<0, 64>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else launch_pdl(k_mixed<0>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
 }
 

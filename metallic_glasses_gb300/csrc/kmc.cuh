@@ -21,9 +21,22 @@ void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStrea
 // Kernels per thermal event of the mixed form: main pass, plane sums with the
 // selection in their last block.
 constexpr int kMixedLaunches = 2;
-void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, int total_blocks,
-                          BatchStatus* status, int nrep, int max_n0, int max_n2, const ModeSet* shared,
-                          cudaStream_t st);
+// Line-length classes of a batch: replicas with lines of 64, 96 or 128 sites
+// run the main pass specialised to that length, the rest the general pass.
+// Their blocks occupy contiguous ranges of blk_rep, one launch per class,
+// side by side on forked streams.
+constexpr int kBatchClasses = 4;
+constexpr int kBatchClassN2[kBatchClasses] = {64, 96, 128, 0};
+int batch_class(int n2);
+struct BatchLaunch {
+  int start[kBatchClasses] = {};   // first block of the class in blk_rep
+  int count[kBatchClasses] = {};   // its blocks
+  int max_n2[kBatchClasses] = {};  // its longest line (shared memory)
+  cudaStream_t side[kBatchClasses] = {};
+  cudaEvent_t fork = nullptr, join[kBatchClasses] = {};
+};
+void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep_first, const BatchLaunch& bl,
+                          BatchStatus* status, int nrep, int max_n0, const ModeSet* shared, cudaStream_t st);
 // Resident blocks per SM of the mixed-form kernel (occupancy query).
 int mixed_blocks_per_sm(int n2);
 // Dynamic shared memory of one mixed-form main block for lines of n2 sites.
