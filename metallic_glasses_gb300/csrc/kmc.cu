@@ -68,12 +68,29 @@ __device__ void iso_inv(const KParams& kp, const double* s, double* e) {
 
 // AvgStress (elastic.c:733-752): mean of the solved field, from the per-block
 // sums the C2R pass left in msum (fixed summation order)
+// Mean stress of the solved field from the C2R pass's block sums, by the
+// whole block: strided partial sums per thread, then a fixed shuffle tree and
+// the warps in order (a dependent chain of FP64 additions in one thread took
+// about 1 ms at 128^3: GB300 runs FP64 at 1/64 of the FP32 rate). Thread 0
+// writes out; every thread of the block must call it.
 __device__ void field_mean_stress(const KParams& kp, const Fields& f, double* out) {
+  __shared__ double red[TH / 32][6];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < kp.nc; c++)
+    for (int b = threadIdx.x; b < kp.c2r_blocks; b += blockDim.x) s[c] += f.msum[(long long)c * kp.c2r_blocks + b];
   for (int c = 0; c < kp.nc; c++) {
-    double s = 0;
-    for (int b = 0; b < kp.c2r_blocks; b++) s += f.msum[(long long)c * kp.c2r_blocks + b];
-    out[c] = s / (double)kp.N;
+    for (int off = 16; off > 0; off >>= 1) s[c] += __shfl_xor_sync(FULL, s[c], off);
+    if (lane == 0) red[w][c] = s[c];
   }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int c = 0; c < kp.nc; c++) {
+      double t = 0;
+      for (int k = 0; k < nw; k++) t += red[k][c];
+      out[c] = t / (double)kp.N;
+    }
+  __syncthreads();
 }
 
 __device__ void solved_mean_stress(const KParams& kp, const Ctl* ctl, const double* ebar, double* out) {
@@ -933,20 +950,21 @@ __global__ void k_ath_commit(KParams kp, Fields f, int mixed) {
 }
 
 // ------------------------------------------------------------ post steps
+// One block of TH threads: the field mean by the block, the rest by thread 0.
 __global__ void k_post_a(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->halt && ctl->step_kind == kNone) return;
   const int kind = ctl->step_kind;
   const bool fieldmean = f.msum != nullptr;
+  if ((kind == kThermal || kind == kAthermal) && fieldmean) field_mean_stress(kp, f, ctl->stress);
+  if (threadIdx.x != 0) return;
   if (kind == kThermal) {
-    if (fieldmean) field_mean_stress(kp, f, ctl->stress);
-    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (!fieldmean) solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
     load_after_event(kp, ctl, ctl->t_kmc);
     ctl->totime += ctl->t_kmc;
   } else if (kind == kAthermal) {
-    if (fieldmean) field_mean_stress(kp, f, ctl->stress);
-    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (!fieldmean) solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
     if (kp.loading == STZ_LOAD_STRESS) {
       hold_stress(kp, ctl);
@@ -971,12 +989,14 @@ __global__ void k_post_print(KParams kp, Fields f) {
   ctl->solve_req = ctl->print_done;
 }
 
+// One block of TH threads, as k_post_a.
 __global__ void k_post_b(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->step_kind == kNone) return;
+  if (ctl->print_done && f.msum) field_mean_stress(kp, f, ctl->stress);
+  if (threadIdx.x != 0) return;
   if (ctl->print_done) {
-    if (f.msum) field_mean_stress(kp, f, ctl->stress);
-    else solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
+    if (!f.msum) solved_mean_stress(kp, ctl, ctl->eps_avg, ctl->stress);
     for (int c = 0; c < 6; c++) ctl->u[c] = 0;
   }
   ctl->print_done = 0;
@@ -2397,11 +2417,11 @@ void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t
 }
 
 void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st) {
-  k_post_a<<<1, 1, 0, st>>>(kp, f);
+  k_post_a<<<1, TH, 0, st>>>(kp, f);
   k_post_print<<<1, 1, 0, st>>>(kp, f);
 }
 
-void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st) { k_post_b<<<1, 1, 0, st>>>(kp, f); }
+void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st) { k_post_b<<<1, TH, 0, st>>>(kp, f); }
 
 void launch_mixed_after_resolve(const KParams& kp, const Fields& f, int kind, cudaStream_t st) {
   k_mixed_after_resolve<<<1, 1, 0, st>>>(kp, f, kind);
