@@ -481,15 +481,31 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
 
 // ---------------------------------------------------------------- C2R, axis 2
 // Deviatoric coordinates of a Voigt stress (tensor shear) in the orthonormal
-// basis (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2*yz, sqrt2*xz, sqrt2*xy.
-__device__ __forceinline__ void dev_coords(const double* s, double* d) {
-  const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637, s2 = 1.41421356237309504880;
+// basis (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2*yz, sqrt2*xz, sqrt2*xy, in the
+// transform's arithmetic.
+template <typename T>
+__device__ __forceinline__ void dev_coords(const T* s, T* d) {
+  const T r2 = (T)0.70710678118654752440, r6 = (T)0.40824829046386301637, s2 = (T)1.41421356237309504880;
   d[0] = (s[0] - s[1]) * r2;
-  d[1] = (2.0 * s[2] - s[0] - s[1]) * r6;
+  d[1] = ((T)2.0 * s[2] - s[0] - s[1]) * r6;
   d[2] = s2 * s[3];
   d[3] = s2 * s[4];
   d[4] = s2 * s[5];
 }
+// The nearest float of a value, a float as a value, and the accumulator of the
+// error norms of the deviatoric epilogue: FP64 for FP64 transforms; FP32 per
+// thread for pairs (norms of a difference of order 1e-6 of the field; the
+// block totals are added in FP64).
+__device__ __forceinline__ float to_f32(double x) { return (float)x; }
+__device__ __forceinline__ float to_f32(float x) { return x; }
+__device__ __forceinline__ float to_f32(dfl x) { return __fadd_rn(x.hi, x.lo); }
+template <typename T> __device__ __forceinline__ T from_f32(float v) { return (T)v; }
+template <> __device__ __forceinline__ dfl from_f32<dfl>(float v) { return dfl(v, 0.f); }
+template <typename T> struct ErrAcc { using A = float; };
+template <> struct ErrAcc<double> { using A = double; };
+__device__ __forceinline__ double acc_of(double x) { return x; }
+__device__ __forceinline__ float acc_of(float x) { return x; }
+__device__ __forceinline__ float acc_of(dfl x) { return to_f32(x); }
 
 template <typename T, int OUT>
 __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restrict__ in, int nc, int n2, int h,
@@ -506,8 +522,9 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
   const int ld = h + 2;
   V* a = reinterpret_cast<V*>(smraw);
   V* b = a + L * ld;
-  double* o = reinterpret_cast<double*>(b + L * ld);  // [nc][L][n2] for the deviatoric epilogue
+  T* o = reinterpret_cast<T*>(b + L * ld);  // [nc][L][n2] for the deviatoric epilogue
   const long long r0 = (long long)blockIdx.x * L;
+  const T invNT = OUT == kOutDev32 ? (T)invN : (T)0;
   __shared__ double msred[8];
   for (int c = 0; c < nc; c++) {
     double part = 0;
@@ -544,8 +561,8 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
       } else if (OUT == kOutSig32) {
         reinterpret_cast<float2*>(sig32 + (long long)c * N)[(r * n2) / 2 + j] = make_float2((float)x0, (float)x1);
       } else {
-        o[(c * L + l) * n2 + 2 * j] = x0;
-        o[(c * L + l) * n2 + 2 * j + 1] = x1;
+        o[(c * L + l) * n2 + 2 * j] = z.x * invNT;
+        o[(c * L + l) * n2 + 2 * j + 1] = z.y * invNT;
       }
     }
     if (OUT == kOutSig64 && msum) {
@@ -562,28 +579,33 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
     __syncthreads();
   }
   if (OUT == kOutDev32) {
-    double mx = 0, ss = 0, sr = 0, mr = 0;
+    using A = typename ErrAcc<T>::A;
+    T ua[6];
+    for (int c = 0; c < 6; c++) ua[c] = uadd ? (T)uadd[c] : (T)0.0;
+    A mxa = 0, ssa = 0, sra = 0, mra = 0;
     for (int idx = threadIdx.x; idx < L * n2; idx += blockDim.x) {
       const int l = idx / n2, i = idx - l * n2;
       const long long r = r0 + l;
       if (r >= rows) continue;
       const long long s = r * n2 + i;
-      double sv[6], d[5];
-      for (int c = 0; c < 6; c++) sv[c] = o[(c * L + l) * n2 + i] + (uadd ? uadd[c] : 0.0);
-      dev_coords(sv, d);
-      double e2 = 0, n2s = 0;
+      T sv[6], d[5];
+      for (int c = 0; c < 6; c++) sv[c] = o[(c * L + l) * n2 + i] + ua[c];
+      dev_coords<T>(sv, d);
+      A e2 = 0, n2s = 0;
       for (int k = 0; k < 5; k++) {
-        const double old = (double)sdev[k * N + s];
-        const double dd = old - d[k];
+        const float old = sdev[k * N + s];
+        const A dd = acc_of(from_f32<T>(old) - d[k]);
+        const A dk = acc_of(d[k]);
         e2 += dd * dd;
-        n2s += d[k] * d[k];
-        sdev[k * N + s] = (float)d[k];
+        n2s += dk * dk;
+        sdev[k * N + s] = to_f32(d[k]);
       }
-      mx = fmax(mx, e2);
-      mr = fmax(mr, n2s);
-      ss += e2;
-      sr += n2s;
+      mxa = mxa > e2 ? mxa : e2;
+      mra = mra > n2s ? mra : n2s;
+      ssa += e2;
+      sra += n2s;
     }
+    double mx = (double)mxa, ss = (double)ssa, sr = (double)sra, mr = (double)mra;
     // block reduction
     for (int off = 16; off > 0; off >>= 1) {
       mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
@@ -785,7 +807,15 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   }
   const double invN = 1.0 / (double)p.N;
   size_t sc = p.smem_c2r;
-  if (a.out == kOutDev32) sc += sizeof(double) * (size_t)p.nc * p.L_x * p.n2;
+  // the deviatoric epilogue stages the block's six real rows: a row tile of
+  // its own, kept within 72 KB of shared memory so that several blocks share
+  // an SM (the tuned tile is timed without this staging)
+  int Ld = p.L_x;
+  auto dev_smem = [&](int L) {
+    return 2 * (size_t)L * (p.h + 2) * sizeof(V) + sizeof(double) * (size_t)p.nc * L * p.n2;
+  };
+  while (a.out == kOutDev32 && Ld > 1 && dev_smem(Ld) > 72 * 1024) Ld /= 2;
+  if (a.out == kOutDev32) sc = dev_smem(Ld);
   if (a.out == kOutSig64)
     k_c2r_x<T, kOutSig64><<<gx.x, TH, sc, st>>>(spec, nco, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, a.sig64, nullptr, nullptr,
@@ -795,9 +825,9 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
                                                Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, a.sig32, nullptr,
                                                nullptr, nullptr, nullptr, a.gate);
   else
-    k_c2r_x<T, kOutDev32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
-                                               Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, nullptr, a.sdev, a.uadd,
-                                               a.err, nullptr, a.gate);
+    k_c2r_x<T, kOutDev32><<<(unsigned)((rows + Ld - 1) / Ld), TH, sc, st>>>(
+        spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, Ld, p.sh, Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, nullptr,
+        a.sdev, a.uadd, a.err, nullptr, a.gate);
   nl += 1;
   if (launches) *launches += nl;
   return STZ_OK;
