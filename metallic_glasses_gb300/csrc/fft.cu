@@ -633,6 +633,102 @@ __global__ void __launch_bounds__(256) k_c2r_x(const typename VT<T>::V* __restri
   }
 }
 
+// C2R of all six components of L rows in one batch of 6 L lines (the block's
+// threads busy in every stage), then the deviatoric epilogue read straight
+// from the transform's buffer (its complex entry j of a row holds the reals
+// 2j and 2j + 1): the stored FP32 coordinates are replaced and the error
+// norms of the old ones accumulated (kOutDev32 of k_c2r_x).
+template <typename T>
+__global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __restrict__ in, int n2, int h, int nh,
+                                                 long long rows, long long N, long long Nk, int L, Sched sh,
+                                                 const typename VT<T>::V* __restrict__ tw_h,
+                                                 const typename VT<T>::V* __restrict__ tw_p, double invN,
+                                                 float* __restrict__ sdev, const double* __restrict__ uadd,
+                                                 double* __restrict__ err, const int* gate) {
+  using V = typename VT<T>::V;
+  if (gate && *gate == 0) return;
+  constexpr int NC = 6;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ld = h + 2;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + NC * L * ld;
+  const long long r0 = (long long)blockIdx.x * L;
+  for (int idx = threadIdx.x; idx < NC * L * nh; idx += blockDim.x) {
+    const int c = idx / (L * nh), rem = idx - c * L * nh;
+    const int l = rem / nh, k = rem - l * nh;
+    const long long r = r0 + l;
+    a[(c * L + l) * ld + k] = r < rows ? in[(long long)c * Nk + r * nh + k] : V{0, 0};
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < NC * L * h; idx += blockDim.x) {
+    const int line = idx / h, k = idx - line * h;
+    V xk = a[line * ld + k];
+    V xc = a[line * ld + (h - k)];
+    xc.y = -xc.y;
+    V e = vadd(xk, xc), d = vsub(xk, xc);
+    V w = tw_p[k];
+    w.y = -w.y;
+    V od = vmul(w, d);
+    b[line * ld + k] = V{e.x - od.y, e.y + od.x};  // Z = E + i O
+  }
+  __syncthreads();
+  const V* res = fft_lines<V, +1>(b, a, NC * L, ld, sh, tw_h);
+  const T invNT = (T)invN;
+  using A = typename ErrAcc<T>::A;
+  T ua[NC];
+  for (int c = 0; c < NC; c++) ua[c] = uadd ? (T)uadd[c] : (T)0.0;
+  A mxa = 0, ssa = 0, sra = 0, mra = 0;
+  for (int idx = threadIdx.x; idx < L * n2; idx += blockDim.x) {
+    const int l = idx / n2, i = idx - l * n2;
+    const long long r = r0 + l;
+    if (r >= rows) continue;
+    const long long s = r * n2 + i;
+    T sv[NC], d[5];
+    for (int c = 0; c < NC; c++) {
+      const V z = res[(c * L + l) * ld + (i >> 1)];
+      sv[c] = ((i & 1) ? z.y : z.x) * invNT + ua[c];
+    }
+    dev_coords<T>(sv, d);
+    A e2 = 0, n2s = 0;
+    for (int k = 0; k < 5; k++) {
+      const float old = sdev[k * N + s];
+      const A dd = acc_of(from_f32<T>(old) - d[k]);
+      const A dk = acc_of(d[k]);
+      e2 += dd * dd;
+      n2s += dk * dk;
+      sdev[k * N + s] = to_f32(d[k]);
+    }
+    mxa = mxa > e2 ? mxa : e2;
+    mra = mra > n2s ? mra : n2s;
+    ssa += e2;
+    sra += n2s;
+  }
+  double mx = (double)mxa, ss = (double)ssa, sr = (double)sra, mr = (double)mra;
+  for (int off = 16; off > 0; off >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, off));
+    ss += __shfl_xor_sync(0xffffffffu, ss, off);
+    sr += __shfl_xor_sync(0xffffffffu, sr, off);
+  }
+  __shared__ double red[4][8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = mx; red[1][w] = ss; red[2][w] = sr; red[3][w] = mr; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+      mx = fmax(mx, red[0][k]);
+      ss += red[1][k];
+      sr += red[2][k];
+      mr = fmax(mr, red[3][k]);
+    }
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long*>(&err[0]), (unsigned long long)__double_as_longlong(mx));
+    atomicAdd(&err[1], ss);
+    atomicAdd(&err[2], sr);
+    atomicMax(reinterpret_cast<unsigned long long*>(&err[3]), (unsigned long long)__double_as_longlong(mr));
+  }
+}
+
 // ------------------------------------------------------------ filter (GRF)
 template <typename T>
 __global__ void k_gauss_filter(typename VT<T>::V* spec, int n0, int n1, int n2, int nh, double corr, long long Nk) {
@@ -725,6 +821,7 @@ void set_smem_attrs_max(int optin) {
   raise_smem_limit(k_c2r_x<T, kOutSig64>, optin);
   raise_smem_limit(k_c2r_x<T, kOutSig32>, optin);
   raise_smem_limit(k_c2r_x<T, kOutDev32>, optin);
+  raise_smem_limit(k_c2r_dev<T>, optin);
 }
 
 template <typename T>
@@ -811,9 +908,7 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   // its own, kept within 72 KB of shared memory so that several blocks share
   // an SM (the tuned tile is timed without this staging)
   int Ld = p.L_x;
-  auto dev_smem = [&](int L) {
-    return 2 * (size_t)L * (p.h + 2) * sizeof(V) + sizeof(double) * (size_t)p.nc * L * p.n2;
-  };
+  auto dev_smem = [&](int L) { return 2 * (size_t)p.nc * L * (p.h + 2) * sizeof(V); };
   while (a.out == kOutDev32 && Ld > 1 && dev_smem(Ld) > 72 * 1024) Ld /= 2;
   if (a.out == kOutDev32) sc = dev_smem(Ld);
   if (a.out == kOutSig64)
@@ -824,10 +919,14 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
     k_c2r_x<T, kOutSig32><<<gx.x, TH, sc, st>>>(spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh,
                                                Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, a.sig32, nullptr,
                                                nullptr, nullptr, nullptr, a.gate);
+  else if (p.nc == 6)
+    k_c2r_dev<T><<<(unsigned)((rows + Ld - 1) / Ld), TH, sc, st>>>(spec, p.n2, p.h, p.nh, rows, p.N, p.Nk, Ld, p.sh,
+                                                                     Tw<T>::h(p), Tw<T>::post(p), invN, a.sdev,
+                                                                     a.uadd, a.err, a.gate);
   else
-    k_c2r_x<T, kOutDev32><<<(unsigned)((rows + Ld - 1) / Ld), TH, sc, st>>>(
-        spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, Ld, p.sh, Tw<T>::h(p), Tw<T>::post(p), invN, nullptr, nullptr,
-        a.sdev, a.uadd, a.err, nullptr, a.gate);
+    k_c2r_x<T, kOutDev32><<<gx.x, TH, p.smem_c2r + sizeof(double) * (size_t)p.nc * p.L_x * p.n2, st>>>(
+        spec, p.nc, p.n2, p.h, p.nh, rows, p.N, p.Nk, p.L_x, p.sh, Tw<T>::h(p), Tw<T>::post(p), invN, nullptr,
+        nullptr, a.sdev, a.uadd, a.err, nullptr, a.gate);
   nl += 1;
   if (launches) *launches += nl;
   return STZ_OK;
