@@ -201,10 +201,15 @@ enum {
   STZ_FIELD_TEMP_SOFT = 6,
   STZ_FIELD_PREV_DEPS = 7,   /* eigenstrain increment of the site's last transformation */
   STZ_FIELD_Q = 8,           /* activation energy Q[mode] for the current stress */
-  STZ_FIELD_SDEV = 9         /* mixed form: the stored FP32 deviatoric stress,
+  STZ_FIELD_SDEV = 9,        /* mixed form: the stored FP32 deviatoric stress,
                                 coordinate comp 0..4 of the orthonormal basis
                                 (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2 yz,
                                 sqrt2 xz, sqrt2 xy (pending update applied first) */
+  STZ_FIELD_LAMBDA = 10,     /* plain forms: the Lame moduli of each site (Lambda, Mu of   */
+  STZ_FIELD_MU = 11          /* init.c:456-465; the params' lambda, mu until set). Once either
+                                varies, every stress solve is the reference's polarisation
+                                fixed point (InhomogeneousStressSolver, elastic.c:977-1066)
+                                with the params' moduli as the reference medium */
 };
 
 typedef struct stz_ctx stz_ctx;

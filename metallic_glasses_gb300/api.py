@@ -24,7 +24,7 @@ DF_TRUNC_NORMAL, DF_CORRELATED = 0, 1
 XX, YY, ZZ, YZ, XZ, XY = range(6)
 EV_THERMAL, EV_ATHERMAL, EV_ELASTIC = 0, 1, 2
 FIELD_SIGMA, FIELD_EPS0, FIELD_DF, FIELD_DEPS, FIELD_TLAST, FIELD_PERM_SOFT, FIELD_TEMP_SOFT, \
-    FIELD_PREV_DEPS, FIELD_Q, FIELD_SDEV = range(10)
+    FIELD_PREV_DEPS, FIELD_Q, FIELD_SDEV, FIELD_LAMBDA, FIELD_MU = range(12)
 
 
 class Params(C.Structure):

@@ -228,7 +228,10 @@ void mixed_constants(stz_ctx* c) {
 }
 
 // ------------------------------------------------------------- solves
+int solve_inhom(stz_ctx* c, const int* gate, const double* ebar);
+
 int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
+  if (c->inhom) return solve_inhom(c, gate, ebar);
   SolveArgs a{};
   a.eps = c->f.eps0;
   a.ebar = ebar;
@@ -241,6 +244,62 @@ int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
   a.spec = c->f.spec;
   a.fp32 = 0;
   return fft_solve(*plan_of(c), a, c->stream, &c->launches);
+}
+
+// A spatially varying medium (InhomogeneousStressSolver, elastic.c:977-1066):
+// the polarisation fixed point around the reference medium of the params'
+// moduli. Each iteration is one homogeneous FP64 solve of the effective
+// eigenstrain (into sig and msum, as solve_plain) and one update; the host
+// reads the change (AvgChange) and stops as the reference does: below 1e-3
+// of the mean strain's norm, or at once when that norm is below 1e-4, or after
+// 101 iterations. sig and msum hold the last solve. Runs outside CUDA graphs
+// (the gate, when given, is read first).
+int solve_inhom(stz_ctx* c, const int* gate, const double* ebar) {
+  const KParams& kp = c->kp;
+  Fields& f = c->f;
+  const long long N = kp.N;
+  const int nc = kp.nc;
+  if (gate) {
+    int g = 0;
+    CK(cudaMemcpyAsync(&g, gate, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!g) return STZ_OK;
+  }
+  double eb[6] = {0, 0, 0, 0, 0, 0};
+  if (ebar) CK(cudaMemcpyAsync(eb, ebar, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  // the reference's norm of EpsAvg (its three 2D components; all six in 3D)
+  double nrm = 0;
+  for (int k = 0; k < nc; k++) nrm += eb[k] * eb[k];
+  nrm = std::sqrt(nrm);
+  double* d_ebar = ebar ? const_cast<double*>(ebar) : c->f.scratch;
+  if (!ebar) CK(cudaMemsetAsync(c->f.scratch, 0, sizeof(double) * 6, c->stream));
+  launch_inhom_init(kp, f, d_ebar, c->stream);
+  std::vector<double> part(kInhomBlocks);
+  for (int step = 1;; step++) {
+    CK(cudaMemcpyAsync(f.inh_last, f.inh_eeff, sizeof(double) * nc * N, cudaMemcpyDeviceToDevice, c->stream));
+    SolveArgs a{};
+    a.eps = f.inh_last;
+    a.ebar = ebar;
+    a.lambda = kp.lambda;
+    a.mu = kp.mu;
+    a.out = kOutSig64;
+    a.sig64 = f.sig;
+    a.msum = f.msum;
+    a.spec = f.spec;
+    int st = fft_solve(*plan_of(c), a, c->stream, &c->launches);
+    if (st) return st;
+    launch_inhom_update(kp, f, c->stream);
+    c->launches += 1;
+    CK(cudaMemcpyAsync(part.data(), f.inh_part, sizeof(double) * kInhomBlocks, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double sum = 0;
+    for (double v : part) sum += v;
+    const double convg = std::sqrt(sum / (double)N);
+    if (convg < 1e-3 * nrm || nrm < 1e-4) break;
+    if (step > 100) break;
+  }
+  return STZ_OK;
 }
 
 // Full re-solve into the FP32 deviatoric field (mixed form), in FP32 pairs
@@ -669,7 +728,8 @@ extern "C" void stz_destroy(stz_ctx* c) {
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
                   f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.psum, f.spec, f.ktab, f.log,
-                  f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf};
+                  f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf, f.lam_site, f.mu_site,
+                  f.inh_tau0, f.inh_eeff, f.inh_last, f.inh_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fft) {
@@ -831,6 +891,13 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
   if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
   const long long N = c->kp.N;
+  if (which == STZ_FIELD_LAMBDA || which == STZ_FIELD_MU) {
+    if (comp != 0) return STZ_ERR_INVALID;
+    const std::vector<double>& h = which == STZ_FIELD_LAMBDA ? c->lam_h : c->mu_h;
+    const double u = which == STZ_FIELD_LAMBDA ? c->kp.lambda : c->kp.mu;
+    for (long long s = 0; s < N; s++) host[s] = h.empty() ? u : h[(size_t)s];
+    return STZ_OK;
+  }
   if (which == STZ_FIELD_Q) {
     if (comp < 0 || comp >= STZ_MODES) return STZ_ERR_INVALID;
     // a persistent buffer: the reference-style driver reads every mode each step
@@ -939,9 +1006,47 @@ extern "C" int stz_set_mean_strain(stz_ctx* c, const double* eps_avg) {
   return STZ_OK;
 }
 
+// The site moduli of a plain form (and the buffers of its fixed point),
+// allocated on first use with the params' uniform values.
+static int ensure_moduli(stz_ctx* c) {
+  if (!c->lam_h.empty()) return STZ_OK;
+  const long long N = c->kp.N;
+  const int nc = c->kp.nc;
+  int st;
+  if ((st = dalloc(&c->f.lam_site, (size_t)N)) || (st = dalloc(&c->f.mu_site, (size_t)N)) ||
+      (st = dalloc(&c->f.inh_tau0, (size_t)nc * N)) || (st = dalloc(&c->f.inh_eeff, (size_t)nc * N)) ||
+      (st = dalloc(&c->f.inh_last, (size_t)nc * N)) || (st = dalloc(&c->f.inh_part, (size_t)kInhomBlocks)))
+    return st;
+  c->lam_h.assign((size_t)N, c->kp.lambda);
+  c->mu_h.assign((size_t)N, c->kp.mu);
+  CK(cudaMemcpyAsync(c->f.lam_site, c->lam_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->f.mu_site, c->mu_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+  return STZ_OK;
+}
+
 extern "C" int stz_set_field(stz_ctx* c, int32_t which, int32_t comp, const double* host, int64_t count) {
   if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
+  if (which == STZ_FIELD_LAMBDA || which == STZ_FIELD_MU) {
+    // the mixed form's response table assumes one uniform medium
+    if (c->f.sdev) return STZ_ERR_UNSUPPORTED;
+    if (comp != 0) return STZ_ERR_INVALID;
+    int st = ensure_moduli(c);
+    if (st) return st;
+    std::vector<double>& h = which == STZ_FIELD_LAMBDA ? c->lam_h : c->mu_h;
+    std::copy(host, host + count, h.begin());
+    CK(cudaMemcpyAsync(which == STZ_FIELD_LAMBDA ? c->f.lam_site : c->f.mu_site, host, sizeof(double) * count,
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->h2d_bytes += (int64_t)sizeof(double) * count;
+    int varies = 0;
+    for (long long s = 0; s < count && !varies; s++)
+      varies = c->lam_h[(size_t)s] != c->kp.lambda || c->mu_h[(size_t)s] != c->kp.mu;
+    c->inhom = varies;
+    // the fixed point's iteration count depends on the data: no graph
+    if (c->inhom) c->use_graph = 0;
+    return STZ_OK;
+  }
   double* d64;
   float* d32;
   int st = field_ptr(c, which, comp, &d64, &d32);

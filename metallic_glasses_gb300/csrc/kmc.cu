@@ -2260,6 +2260,80 @@ __global__ void k_ktab_column(KParams kp, const double* sig, float* ktab, int b)
   }
 }
 
+// ------------------------------------------- spatially varying moduli
+// The polarisation fixed point of InhomogeneousStressSolver (elastic.c:977-
+// 1066) per site: C(x):e with the site's Lambda, Mu (IsotropicMul_RF,
+// elastic.c:905-920) and (C0 - C(x)):e (IsotropicMul_RF_D, elastic.c:922-938).
+__device__ __forceinline__ void site_C(int nc, double lam, double mu, const double* e, double* s) {
+  const int nd = ndiag(nc);
+  double tr = 0;
+  for (int c = 0; c < nd; c++) tr += e[c];
+  const double tra = lam * tr;
+  for (int c = 0; c < nc; c++) s[c] = (c < nd ? tra : 0.0) + 2 * mu * e[c];
+}
+
+// Start (elastic.c:993-1009): tau0 = C(x):eps*, and the reference medium's
+// effective eigenstrain eeff = C0^-1:(tau0 + (C0 - C(x)):(eps* + ebar)).
+__global__ void k_inhom_init(KParams kp, const double* __restrict__ eps0, const double* __restrict__ ebar,
+                             const double* __restrict__ lam_s, const double* __restrict__ mu_s,
+                             double* __restrict__ tau0, double* __restrict__ eeff) {
+  const int nc = kp.nc;
+  double eb[6];
+  for (int c = 0; c < nc; c++) eb[c] = ebar[c];
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < kp.N; s += (long long)gridDim.x * blockDim.x) {
+    double e0[6], e1[6], t0[6], t1[6], T[6], ee[6];
+    for (int c = 0; c < nc; c++) {
+      e0[c] = eps0[c * kp.N + s];
+      e1[c] = e0[c] + eb[c];
+    }
+    site_C(nc, lam_s[s], mu_s[s], e0, t0);
+    site_C(nc, kp.lambda - lam_s[s], kp.mu - mu_s[s], e1, t1);
+    for (int c = 0; c < nc; c++) T[c] = t0[c] + t1[c];
+    iso_inv(kp, T, ee);
+    for (int c = 0; c < nc; c++) {
+      tau0[c * kp.N + s] = t0[c];
+      eeff[c * kp.N + s] = ee[c];
+    }
+  }
+}
+
+// One iteration after the homogeneous solve of the reference medium with
+// eigenstrain `last` (elastic.c:1027-1049): total strain e = C0^-1:sigma +
+// last, tau = tau0 + (C0 - C(x)):e, eeff = (C0^-1:tau + last) / 2 (mix 0.5),
+// and this block's sum of (eeff - last)^2 in part[blockIdx.x] (AvgChange,
+// elastic.c:957-975; a fixed tree, so the sum does not depend on timing).
+__global__ void k_inhom_update(KParams kp, const double* __restrict__ sig, const double* __restrict__ last,
+                               const double* __restrict__ lam_s, const double* __restrict__ mu_s,
+                               const double* __restrict__ tau0, double* __restrict__ eeff,
+                               double* __restrict__ part) {
+  const int nc = kp.nc;
+  double acc = 0;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < kp.N; s += (long long)gridDim.x * blockDim.x) {
+    double sg[6], el[6], et[6], t1[6], T[6], en[6];
+    for (int c = 0; c < nc; c++) sg[c] = sig[c * kp.N + s];
+    iso_inv(kp, sg, el);
+    for (int c = 0; c < nc; c++) et[c] = el[c] + last[c * kp.N + s];
+    site_C(nc, kp.lambda - lam_s[s], kp.mu - mu_s[s], et, t1);
+    for (int c = 0; c < nc; c++) T[c] = tau0[c * kp.N + s] + t1[c];
+    iso_inv(kp, T, en);
+    for (int c = 0; c < nc; c++) {
+      const double lv = last[c * kp.N + s];
+      const double v = 0.5 * en[c] + (1 - 0.5) * lv;
+      eeff[c * kp.N + s] = v;
+      acc += (v - lv) * (v - lv);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
+  __shared__ double red[TH / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += red[k];
+    part[blockIdx.x] = t;
+  }
+}
+
 __global__ void k_fill_f32(const double* in, float* out, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = (float)in[i];
@@ -2442,6 +2516,15 @@ void launch_ktab_column(const KParams& kp, const double* sig, float* ktab, int b
   const long long tn = (long long)kp.kt0 * kp.kt1 * kp.kt2;
   const long long nb = std::min<long long>((tn + 255) / 256, 4096);
   k_ktab_column<<<(unsigned)nb, 256, 0, st>>>(kp, sig, ktab, b);
+}
+
+void launch_inhom_init(const KParams& kp, const Fields& f, const double* ebar, cudaStream_t st) {
+  k_inhom_init<<<kInhomBlocks, TH, 0, st>>>(kp, f.eps0, ebar, f.lam_site, f.mu_site, f.inh_tau0, f.inh_eeff);
+}
+
+void launch_inhom_update(const KParams& kp, const Fields& f, cudaStream_t st) {
+  k_inhom_update<<<kInhomBlocks, TH, 0, st>>>(kp, f.sig, f.inh_last, f.lam_site, f.mu_site, f.inh_tau0, f.inh_eeff,
+                                              f.inh_part);
 }
 
 void launch_fill_f32(const double* in, float* out, long long n, cudaStream_t st) {

@@ -61,6 +61,13 @@ void launch_q_mode(const KParams& kp, const Fields& f, int mode, double* out, cu
 void launch_dev_from_sig(const KParams& kp, const double* sig, float* sdev, cudaStream_t st);
 void launch_ktab_column(const KParams& kp, const double* sig, float* ktab, int b, cudaStream_t st);
 void launch_fill_f32(const double* in, float* out, long long n, cudaStream_t st);
+// Polarisation fixed point of a spatially varying medium (plain forms): the
+// start (tau0, eeff from eps0 and the device mean strain ebar) and one update
+// after a homogeneous solve of eigenstrain inh_last into sig; the update
+// leaves kInhomBlocks partial sums of the squared change in inh_part.
+constexpr int kInhomBlocks = 608;
+void launch_inhom_init(const KParams& kp, const Fields& f, const double* ebar, cudaStream_t st);
+void launch_inhom_update(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_l2_flush(void* buf, size_t bytes, cudaStream_t st);
 
 }  // namespace stz

@@ -120,6 +120,13 @@ struct Fields {
   Ctl* ctl = nullptr;
   double* scratch = nullptr;  // small scratch (error statistics nobody reads)
   double* msum = nullptr;     // [nc][c2r_blocks] block sums of the solved field
+  // spatially varying moduli (plain forms; allocated when first set)
+  double* lam_site = nullptr;  // [N] Lambda
+  double* mu_site = nullptr;   // [N] Mu
+  double* inh_tau0 = nullptr;  // [nc][N] C(x):eps*  of the polarisation fixed point
+  double* inh_eeff = nullptr;  // [nc][N] effective eigenstrain of the reference medium
+  double* inh_last = nullptr;  // [nc][N] its previous iterate
+  double* inh_part = nullptr;  // [blocks] partial sums of the iterate's squared change
 };
 
 // Constant parameters of one context, passed to kernels by value.
@@ -193,6 +200,8 @@ struct stz_ctx {
   double ktime_ms = 0;
   int64_t ktime_n = 0;
   int use_graph = 1;
+  int inhom = 0;                      // some site's moduli differ from the params' (plain forms)
+  std::vector<double> lam_h, mu_h;    // host copies of the site moduli (empty until set)
   cudaGraphExec_t graph = nullptr;
   int graph_batch = 0;
   int64_t graph_launches = 0;        // kernels per graph launch

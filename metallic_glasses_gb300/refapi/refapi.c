@@ -29,9 +29,12 @@
  * displacement field of the eigenstrain plus the supercell position, as
  * elastic.c:866-900 and io.c:137-240 write them.
  *
+ * Spatially varying Lambda/Mu passed to InhomogeneousStressSolver go to the
+ * engine, whose solves (those of the steps too) then run the reference's
+ * polarisation fixed point.
+ *
  * Not provided: SOC counters (UpdateSOC leaves main's arrays as they are),
- * spatially varying Lambda/Mu (the solve is homogeneous; a non-uniform field
- * is reported), MRO maps, residual-stress generation.
+ * MRO maps, residual-stress generation.
  */
 #include <math.h>
 #include <stdio.h>
@@ -304,18 +307,24 @@ static void positions(real** xr, const real* epsavg) {
 }
 
 #ifdef INHOM_ELAST
-/* elastic.c:977-1066 with uniform moduli: one homogeneous solve */
+/* elastic.c:977-1066: the engine's solve with the site moduli Lambdao, Muo
+ * (a uniform medium is one homogeneous solve; a varying one is the
+ * polarisation fixed point around lambda_, mu_). The moduli go to the device
+ * when they differ from what it holds. */
 void InhomogeneousStressSolver(real* Lambdao, real* Muo, real** eps0o, real* epsavg, real lambda_, real mu_,
                                real** uo, real** epso, real** sigmao, real* stress, int uflag) {
-  static int warned = 0;
+  static real* held[2] = {NULL, NULL};  /* the moduli last passed to the engine */
+  real* mod[2] = {Lambdao, Muo};
+  const real uni[2] = {lambda_, mu_};
   (void)eps0o;
-  if (!warned) {
-    for (int s = 0; s < NXY; s++)
-      if (Lambdao[s] != lambda_ || Muo[s] != mu_) {
-        fprintf(stderr, "refapi: non-uniform Lambda/Mu; solving with the uniform lambda, mu\n");
-        warned = 1;
-        break;
-      }
+  for (int k = 0; k < 2; k++) {
+    int push = 0;
+    for (int s = 0; s < NXY && !push; s++) push = held[k] ? mod[k][s] != held[k][s] : mod[k][s] != uni[k];
+    if (!push) continue;
+    if (!held[k]) held[k] = alloc_field();
+    for (int s = 0; s < NXY; s++) held[k][s] = mod[k][s];
+    int st = stz_set_field(g_ctx, k ? STZ_FIELD_MU : STZ_FIELD_LAMBDA, 0, mod[k], NXY);
+    if (st) fail("stz_set_field (moduli)", st);
   }
   solve_into(epso, sigmao, stress, epsavg);
   if (uflag != 0 && uo) positions(uo, epsavg);

@@ -16,7 +16,9 @@ directory and stores, per case:
                                    wrote at P = 4 of its prints spread over the
                                    run (X1R/X2R files, "%lf" text: 6 decimals)
                xr_k       int64 [P]  their print numbers (the files' %03d)
-and the MT19937 known answers of the GSL conventions (mt19937_kat.npz).
+and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
+the reference's InhomogeneousStressSolver on a spatially varying medium
+(inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
 
 Only this script reads the reference tree; tests read the .npz files.
 Usage: python tests/golden/make_golden.py
@@ -122,8 +124,36 @@ int main(){ std::mt19937 a(5489u); unsigned v=0; for(int i=0;i<10000;i++) v=a();
     print("mt19937 kat", v10000, s123[:2])
 
 
+def inhom_case(nx=32, ny=32):
+    """The reference's polarisation solver on a medium whose Lame moduli vary
+    between 0.7 and 1.3 of the uniform ones (inhom_ref.c is the main; the
+    reference's io.c, init.c, elastic.c, evolution.c compile unmodified against
+    the stand-ins of oracle/shim)."""
+    from oracle.build_oracle import HERE as OR, REF_DIR, CFLAGS
+    d = tempfile.mkdtemp(prefix="stz_inhom_")
+    exe = os.path.join(d, "inhom_ref")
+    srcs = [os.path.join(REF_DIR, f) for f in ("io.c", "init.c", "elastic.c", "evolution.c")]
+    cmd = (["gcc", *CFLAGS, "-w", "-DSTZ_SHIM_NX=%d" % nx, "-DSTZ_SHIM_NY=%d" % ny, "-I", os.path.join(OR, "shim"),
+            "-I", REF_DIR] + srcs + [os.path.join(HERE, "inhom_ref.c"), os.path.join(OR, "shim", "shim.c"),
+                                     os.path.join(OR, "stz_oracle.c"), "-o", exe, "-lm"])
+    subprocess.run(cmd, check=True)
+    configs.write_input(os.path.join(d, "input"), end="0.5", seed="5", soft="0")
+    subprocess.run([exe], cwd=d, stdout=subprocess.DEVNULL, check=True)
+    raw = open(os.path.join(d, "inhom.bin"), "rb").read()
+    NX, NY = np.frombuffer(raw[:16], np.int64)
+    N = int(NX * NY)
+    sc = np.frombuffer(raw[16:80], np.float64)
+    arr = np.frombuffer(raw[80:], np.float64)
+    eps0, lam, mu, sigma = arr[:3 * N].reshape(3, N), arr[3 * N:4 * N], arr[4 * N:5 * N], arr[5 * N:8 * N].reshape(3, N)
+    out = os.path.join(HERE, "inhom_%d.npz" % nx)
+    np.savez_compressed(out, nx=nx, ny=ny, lame=sc[:2], epsavg=sc[2:5], stress=sc[5:8], eps0=eps0, lam=lam, mu=mu,
+                        sigma=sigma)
+    print("inhom", nx, ny, "stress", sc[5:8], "->", out)
+
+
 if __name__ == "__main__":
     build_oracle_lib()
+    inhom_case()
     mt_kat()
     for name, (nx, ny, loading, ov, ev) in CASES.items():
         run_case(name, nx, ny, loading, ov, ev)

@@ -248,3 +248,55 @@ def test_displacement_gradient_is_the_solved_strain_3d(engine_lib):
         grad = np.real(np.fft.ifftn(0.5j * (k[a] * U[b] + k[b] * U[a]) * mask))
         want = np.real(np.fft.ifftn(np.fft.fftn(eps[c].reshape(n, n, n)) * mask))
         assert np.abs(grad - want).max() <= 1e-9 * scale, c
+
+
+# -------------------------------------------- spatially varying moduli
+def test_inhomogeneous_solve_matches_reference(engine_lib):
+    """The polarisation fixed point of a medium whose Lame moduli vary between
+    0.7 and 1.3 of the uniform ones, against the reference's own
+    InhomogeneousStressSolver on the same eigenstrain, moduli and mean strain
+    (tests/golden/inhom_32.npz, generated from the reference's sources): the
+    stress field and its mean to 1e-9 of the field's size."""
+    g = golden("inhom_32")
+    p = configs.ref2d(int(g["nx"]), int(g["ny"]), end="0.5", seed="5", soft="0")
+    assert np.allclose([p.lambda_, p.mu], g["lame"], rtol=1e-15)
+    e = api.Engine(p)
+    for c in range(3):
+        e.set_field(api.FIELD_EPS0, c, g["eps0"][c])
+    e.set_field(api.FIELD_LAMBDA, 0, g["lam"])
+    e.set_field(api.FIELD_MU, 0, g["mu"])
+    e.set_mean_strain(list(g["epsavg"]))
+    e.solve()
+    sig = np.stack([e.field(api.FIELD_SIGMA, c) for c in range(3)])
+    stress = np.array(e.scalars()["stress"][:3])
+    e.close()
+    scale = np.abs(g["sigma"]).max()
+    assert np.abs(sig - g["sigma"]).max() <= 1e-9 * scale
+    assert np.abs(stress - g["stress"]).max() <= 1e-9 * scale
+
+
+def test_inhomogeneous_medium_steps(engine_lib):
+    """The plain form steps with spatially varying moduli (every solve the
+    fixed point); uniform moduli set explicitly leave the event sequence of the
+    uniform medium unchanged."""
+    def run(moduli):
+        p = configs.ref2d(32, 32, end="0.5", seed="5", soft="0")
+        e = api.Engine(p)
+        if moduli is not None:
+            lam, mu = moduli(p)
+            e.set_field(api.FIELD_LAMBDA, 0, lam)
+            e.set_field(api.FIELD_MU, 0, mu)
+        e.run(max_events=30)
+        ev, sc = e.events(), e.scalars()
+        e.close()
+        return ev, sc
+    n = 32 * 32
+    ev0, sc0 = run(None)
+    ev1, sc1 = run(lambda p: (np.full(n, p.lambda_), np.full(n, p.mu)))
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(ev0[k], ev1[k]), k
+    rng = np.random.default_rng(3)
+    ev2, sc2 = run(lambda p: (p.lambda_ * rng.uniform(0.8, 1.2, n), p.mu * rng.uniform(0.8, 1.2, n)))
+    assert sc2["status"] == 0 and sc2["kstep"] == 30
+    assert np.all(np.isfinite(sc2["stress"]))
+    assert not np.array_equal(ev0["site"], ev2["site"])
