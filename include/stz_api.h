@@ -79,9 +79,10 @@ enum {                      /* direction-softening schemes, bmgFlags.h:30-35 */
 
 enum {
   STZ_PREC_FP64 = 0,        /* "plain": FP64 throughout */
-  STZ_PREC_MIXED = 1        /* FP32 stress field, contraction and rates; FP64
-                               total rate, cumulative search, clock, eigenstrain
-                               and mean strain; periodic FP64 re-solve */
+  STZ_PREC_MIXED = 1        /* FP32 stress field, contraction and rates; exact
+                               fixed-point selection; FP64 clock, eigenstrain and
+                               mean strain; periodic full re-solve (FP32 pairs, or
+                               FP64 with resolve_fp64) */
 };
 
 enum {
@@ -140,7 +141,7 @@ typedef struct stz_params {
   /* engine controls */
   int32_t precision;         /* STZ_PREC_* */
   int32_t solver;            /* STZ_SOLVER_* */
-  int32_t resolve_period;    /* mixed: FP64 full re-solve every this many events (0 = never) */
+  int32_t resolve_period;    /* mixed: full re-solve every this many events (0 = never) */
   int32_t device;            /* CUDA device ordinal */
   int32_t log_capacity;      /* device event-ring entries (0: 1 << 20) */
   int32_t mode_seed_set;     /* GLOBAL3D: 1 = the 20 modes come from their own MT19937
@@ -179,12 +180,12 @@ typedef struct stz_scalars {
   int64_t n_events_logged;
   int32_t stopped;           /* 1: end strain reached, 2: unstable (bmg.c:382-409) */
   int32_t status;            /* sticky device error status */
-  double  stress_err_max;    /* mixed, last FP64 re-solve: max |ds| / max |s| of the
-                                deviatoric stress s against the FP64 re-solve */
-  double  stress_err_rms;    /* mixed, last FP64 re-solve: |ds|_2 / |s|_2 */
+  double  stress_err_max;    /* mixed, last full re-solve: max |ds| / max |s| of the
+                                deviatoric stress s against the re-solve */
+  double  stress_err_rms;    /* mixed, last full re-solve: |ds|_2 / |s|_2 */
   int64_t near_ties;         /* selections whose cumulative margin was below 1e-12 R */
   int64_t log_dropped;       /* events not logged (ring full) */
-  int64_t n_resolves;        /* periodic FP64 re-solves done */
+  int64_t n_resolves;        /* periodic full re-solves done */
   double  stress_err_rms_worst;  /* worst of stress_err_rms over all re-solves */
   double  stress_err_max_worst;
   int64_t reserved[2];

@@ -4,7 +4,7 @@ ref2d(...)      the reference's own 2D model, built from a reference-format
                 input file (labels of io.c:4-101) at a chosen grid
 stress32()      32^3, FP64, constant applied pure shear stress 1 GPa, seed 0
 shear64(seed)   64^3, FP64, shear strain rate, seeds 0-3
-mixed128()      128^3, mixed form, periodic FP64 re-solve every 1000 events
+mixed128()      128^3, mixed form, periodic full re-solve every 1000 events
 grf256()        256^3, mixed form, correlated barrier field
 replicas(...)   uneven 3D replicas (grids 32/48/64/96, T in [325, 585] K,
                 log-uniform strain rates), seeds 0-255

@@ -469,8 +469,9 @@ int mixed_service(stz_ctx* c, int* done) {
     c->launches += 6;
   } else {
     if (kp.resolve_period > 0 && h.kstep >= h.next_resolve) {
-      // periodic FP64 re-solve: bring the FP32 field up to date, re-solve it
-      // in FP64 with the same mean strain and offsets, record the difference
+      // periodic full re-solve: bring the FP32 field up to date, re-solve it
+      // (FP32 pairs or FP64) with the same mean strain and offsets, record the
+      // difference
       launch_mixed(kp, f, 1, c->stream);
       double zero[4] = {0, 0, 0, 0};
       CK(cudaMemcpyAsync(c->err_dev, zero, sizeof(zero), cudaMemcpyHostToDevice, c->stream));

@@ -2192,7 +2192,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __
   }
 }
 
-// After a full FP64 re-solve into sdev (mixed form).
+// After a full re-solve into sdev (mixed form).
 __global__ void k_mixed_after_resolve(KParams kp, Fields f, int kind) {
   Ctl* ctl = f.ctl;
   ctl->has_pend = 0;

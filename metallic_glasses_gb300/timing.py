@@ -6,7 +6,7 @@
 
 `kernel` times one per-event kernel of the mixed form launch by launch with
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
-only, 2: a whole event including selection). `solve` times the FP64 re-solve
+only, 2: a whole event including selection). `solve` times the full re-solve
 of the full field (the FFT passes) with the tuned schedule. `batch` advances independent
 replicas (grid sizes 32^3..96^3, temperatures and strain rates drawn from the
 seed) together in one batch, then the same replicas one at a time, and prints
