@@ -653,6 +653,20 @@ __global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __rest
   V* a = reinterpret_cast<V*>(smraw);
   V* b = a + NC * L * ld;
   const long long r0 = (long long)blockIdx.x * L;
+  // the old FP32 coordinates of this thread's sites (the epilogue's only
+  // global reads; beyond L2 at large grids), loaded now so that the transform
+  // hides their latency; threads with more than kPre sites read the rest late
+  constexpr int kPre = 4;
+  float pre[kPre][5];
+#pragma unroll
+  for (int q = 0; q < kPre; q++) {
+    const int idx = threadIdx.x + q * blockDim.x;
+    const int l = idx / n2, i = idx - l * n2;
+    const long long r = r0 + l;
+    const bool ok = idx < L * n2 && r < rows;
+#pragma unroll
+    for (int k = 0; k < 5; k++) pre[q][k] = ok ? sdev[k * N + r * n2 + i] : 0.f;
+  }
   for (int idx = threadIdx.x; idx < NC * L * nh; idx += blockDim.x) {
     const int c = idx / (L * nh), rem = idx - c * L * nh;
     const int l = rem / nh, k = rem - l * nh;
@@ -678,7 +692,7 @@ __global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __rest
   T ua[NC];
   for (int c = 0; c < NC; c++) ua[c] = uadd ? (T)uadd[c] : (T)0.0;
   A mxa = 0, ssa = 0, sra = 0, mra = 0;
-  for (int idx = threadIdx.x; idx < L * n2; idx += blockDim.x) {
+  for (int idx = threadIdx.x, q = 0; idx < L * n2; idx += blockDim.x, q++) {
     const int l = idx / n2, i = idx - l * n2;
     const long long r = r0 + l;
     if (r >= rows) continue;
@@ -690,8 +704,13 @@ __global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __rest
     }
     dev_coords<T>(sv, d);
     A e2 = 0, n2s = 0;
+#pragma unroll
     for (int k = 0; k < 5; k++) {
-      const float old = sdev[k * N + s];
+      float old = 0.f;
+#pragma unroll
+      for (int qq = 0; qq < kPre; qq++)
+        if (qq == q) old = pre[qq][k];
+      if (q >= kPre) old = sdev[k * N + s];
       const A dd = acc_of(from_f32<T>(old) - d[k]);
       const A dk = acc_of(d[k]);
       e2 += dd * dd;

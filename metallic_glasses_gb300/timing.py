@@ -15,6 +15,7 @@ context through stz_run, the single-run path). Both are the commands the ncu sum
 taken on.
 """
 import argparse
+import ctypes
 import json
 import time
 
@@ -28,7 +29,17 @@ def kernel(grid, which, steps, resolve_period=0):
     return {"grid": grid, "which": which, "launch_ms": ms, "launches": n}
 
 
-def solve(grid, reps=5, mixed=True, fp64=False):
+def _profiler(on):
+    """Open or close the CUDA profiler's range (cuProfilerStart/Stop of the
+    driver), so that `ncu --profile-from-start off` sees only the timed calls."""
+    try:
+        drv = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return
+    (drv.cuProfilerStart if on else drv.cuProfilerStop)()
+
+
+def solve(grid, reps=5, mixed=True, fp64=False, profile_range=False):
     """Green's-function re-solves of the mixed form's full field at grid^3
     (the FFT passes), in FP32 pairs or (fp64) in FP64, timed with CUDA events.
     alg_bytes: what one solve must move
@@ -41,10 +52,15 @@ def solve(grid, reps=5, mixed=True, fp64=False):
     eng = api.Engine(p)
     eng.solve()
     eng.sync()
+    if profile_range:
+        eng.sync()
+        _profiler(True)
     eng.timer_start()
     for _ in range(reps):
         eng.solve()
     ms = eng.timer_stop() / reps
+    if profile_range:
+        _profiler(False)
     sch = eng.fft_schedule()
     eng.close()
     n = grid ** 3
@@ -102,6 +118,8 @@ def main(argv=None):
     sv.add_argument("--grid", type=int, default=256)
     sv.add_argument("--reps", type=int, default=5)
     sv.add_argument("--fp64", action="store_true")
+    sv.add_argument("--profile-range", action="store_true",
+                    help="open the CUDA profiler range around the timed solves only")
     b = sub.add_parser("batch")
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
@@ -110,7 +128,7 @@ def main(argv=None):
     if a.cmd == "kernel":
         out = kernel(a.grid, a.which, a.steps)
     elif a.cmd == "solve":
-        out = solve(a.grid, a.reps, fp64=a.fp64)
+        out = solve(a.grid, a.reps, fp64=a.fp64, profile_range=a.profile_range)
     else:
         out = batch(a.replicas, a.events, a.alone)
     print(json.dumps(out), flush=True)
