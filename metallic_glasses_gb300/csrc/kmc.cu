@@ -2372,10 +2372,13 @@ static void mixed_smem_init() {
   raise((const void*)k_mixed<0>);
   raise((const void*)k_mixed<0, 128>);
   raise((const void*)k_mixed<1>);
+  raise((const void*)k_mixed<0, 32>);
   raise((const void*)k_mixed<0, 64>);
   raise((const void*)k_mixed<0, 96>);
   raise((const void*)k_mixed_batched<0, 0>);
   raise((const void*)k_mixed_batched<1, 0>);
+  raise((const void*)k_mixed_batched<0, 32>);
+  raise((const void*)k_mixed_batched<1, 32>);
   raise((const void*)k_mixed_batched<0, 64>);
   raise((const void*)k_mixed_batched<1, 64>);
   raise((const void*)k_mixed_batched<0, 96>);
@@ -2450,6 +2453,7 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
       cudaStreamWaitEvent(s, bl.fork, 0);
     }
     switch (kBatchClassN2[c]) {
+      case 32: launch_batched_class<32>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s); break;
       case 64: launch_batched_class<64>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s); break;
       case 96: launch_batched_class<96>(d, blk_rep, rep_first, bl.start[c], bl.count[c], bl.max_n2[c], shared, s); break;
       case 128:
@@ -2471,6 +2475,7 @@ void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cuda
   else if (kp.n2 == 128) launch_pdl(k_mixed<0, 128>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 96) launch_pdl(k_mixed<0, 96>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 64) launch_pdl(k_mixed<0, 64>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
+  else if (kp.n2 == 32) launch_pdl(k_mixed<0, 32>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else launch_pdl(k_mixed<0>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
 }
 

@@ -21,12 +21,12 @@ void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStrea
 // Kernels per thermal event of the mixed form: main pass, plane sums with the
 // selection in their last block.
 constexpr int kMixedLaunches = 2;
-// Line-length classes of a batch: replicas with lines of 64, 96 or 128 sites
+// Line-length classes of a batch: replicas with lines of 32, 64, 96 or 128 sites
 // run the main pass specialised to that length, the rest the general pass.
 // Their blocks occupy contiguous ranges of blk_rep, one launch per class,
 // side by side on forked streams.
-constexpr int kBatchClasses = 4;
-constexpr int kBatchClassN2[kBatchClasses] = {64, 96, 128, 0};
+constexpr int kBatchClasses = 5;
+constexpr int kBatchClassN2[kBatchClasses] = {32, 64, 96, 128, 0};
 int batch_class(int n2);
 struct BatchLaunch {
   int start[kBatchClasses] = {};   // first block of the class in blk_rep
