@@ -6,7 +6,9 @@ drawn from seed 0, all state resident in HBM). L2 is flushed between steps
 (a 256 MB write). The line also carries the FP64 plain form measured on the
 same grid, the stress error of the mixed form against its full re-solves, the
 roofline of the per-event kernel, the end-to-end figure through the C ABI
-with host-side event and scalar reads, and the CPU oracle timed on the host.
+with host-side event and scalar reads, the CPU oracle timed on the host, the
+batched replicas against the same replicas one at a time, and the 256^3
+correlated-barrier run (event rate and stress error).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -170,6 +172,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-replicas", type=int, default=256)
+    ap.add_argument("--no-grf", action="store_true", help="skip the 256^3 correlated-barrier run")
+    ap.add_argument("--grf-events", type=int, default=20000)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -303,6 +307,15 @@ def main():
                           % (args.batch_replicas, args.batch_replicas - 1))
         bt["ratio"] = bt["batched_events_per_s"] / bt["alone_events_per_s"]
         line["batched"] = bt
+    if not args.no_grf:
+        # 256^3 with a correlated barrier field (Gaussian covariance, 4 voxels,
+        # sd 0.15 eV), strain rate 5e-4 /s, autotuned FFT schedules
+        from metallic_glasses_gb300 import timing
+        gr = timing.run("grf256", events=args.grf_events, warmup=1000)
+        gr["workload"] = ("256^3 mixed form, correlated barriers N(1.2, 0.15) eV with Gaussian covariance of "
+                          "length 4 voxels, shear strain rate 5e-4 /s, %d thermal events after 1000 warm-up "
+                          "events, full re-solve (FP32 pairs) every 1000 events" % args.grf_events)
+        line["grf256"] = gr
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
         line["cpu_baseline_1core"] = cpu_baseline(seconds=8.0, grid=n, threads=1)

@@ -83,6 +83,38 @@ template <> struct VT<double> { using V = double2; };
 template <> struct VT<float> { using V = float2; };
 template <> struct VT<dfl> { using V = df2; };
 
+// An FP64 value as a pair without FP64 instructions (GB300 issues FP64 at
+// 1/64 of its FP32 rate, and the conversions of dfl(double) run there): hi is
+// x with its significand cut to 24 bits, built from the bit fields; the 29
+// bits cut off are exactly r * 2^(e - 1075) and are rounded to a float; the
+// pair is then renormalised (|x - hi - lo| <= 2^-48 |x|). Below 2^-74 in
+// magnitude lo is dropped, below 2^-126 the value becomes a signed zero
+// (absolute errors under 2^-98 and 2^-126); beyond the float range it becomes
+// the infinity of its sign, and a NaN stays a NaN. Every case is integer work:
+// an FP64 conversion in a rarely taken branch is still executed for every
+// value once the compiler turns the branch into a select.
+__device__ __forceinline__ dfl split_f64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const int e = (int)((hw >> 20) & 0x7ffu);
+  const unsigned sg = hw & 0x80000000u;
+  if (e > 1023 + 127) {
+    const bool nan = e == 2047 && ((hw & 0xfffffu) | lw) != 0u;
+    return dfl(__uint_as_float(nan ? 0x7fc00000u : (sg | 0x7f800000u)), 0.f);
+  }
+  if (e < 1023 - 126) return dfl(__uint_as_float(sg), 0.f);
+  const float h = __uint_as_float(sg | ((unsigned)(e - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+  float l = 0.f;
+  if (e >= 1075 - 126) {
+    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);
+    l = __uint_as_float(__float_as_uint(__fmul_rn(__uint2float_rn(lw & 0x1fffffffu), scale)) | sg);
+  }
+  const float s = __fadd_rn(h, l);
+  return dfl(s, __fsub_rn(l, __fsub_rn(s, h)));
+}
+template <typename T> __device__ __forceinline__ T from_f64(double x) { return (T)x; }
+template <> __device__ __forceinline__ dfl from_f64<dfl>(double x) { return split_f64(x); }
+
 template <typename V> __device__ __forceinline__ V vadd(V a, V b) { return V{a.x + b.x, a.y + b.y}; }
 template <typename V> __device__ __forceinline__ V vsub(V a, V b) { return V{a.x - b.x, a.y - b.y}; }
 template <typename V> __device__ __forceinline__ V vmul(V a, V b) {
@@ -213,7 +245,7 @@ __global__ void __launch_bounds__(256) k_r2c_x(const double* __restrict__ in, ty
     V z = V{0, 0};
     if (r < rows) {
       double2 v = src[(r * n2) / 2 + j];
-      z = V{(T)v.x, (T)v.y};
+      z = V{from_f64<T>(v.x), from_f64<T>(v.y)};
     }
     a[l * ld + j] = z;
   }
@@ -269,7 +301,15 @@ struct GreenArgs {
   int disp;  // write the displacement spectrum (components 0 .. dim-1) instead of the stress
   double lambda, mu;
   double Ntot;
+  // the same constants as FP32 pairs (hi, lo) for the pair transforms:
+  // lambda, mu, alpha = (lambda + mu) / (lambda + 2 mu), 1/n0, 1/n1, 1/n2
+  float pr[6][2];
 };
+
+// A constant of GreenArgs in the transform's arithmetic: the double, or its
+// pair made on the host.
+template <typename T> __device__ __forceinline__ T green_const(double d, const float* pr) { return (T)d; }
+template <> __device__ __forceinline__ dfl green_const<dfl>(double d, const float* pr) { return dfl(pr[0], pr[1]); }
 
 // stress = C:(e), Voigt with tensor shear; nc = 3 (xx yy xy) or 6 (xx yy zz yz xz xy)
 template <typename T, typename V>
@@ -284,9 +324,10 @@ __device__ __forceinline__ void apply_C(int nc, T lam, T mu, const V* e, V* out)
   }
 }
 
-// sigma_hat = C:(Gamma(g):C:e - e) for one unit wave vector g (x, y, z)
+// sigma_hat = C:(Gamma(g):C:e - e) for one unit wave vector g (x, y, z);
+// h = 1/(2 mu), am = -alpha/mu with alpha = (lambda + mu)/(lambda + 2 mu)
 template <typename T, typename V>
-__device__ __forceinline__ void green_op(int nc, T lam, T mu, T alpha, const T* g, const V* e, V* sig) {
+__device__ __forceinline__ void green_op(int nc, T lam, T mu, T h, T am, const T* g, const V* e, V* sig) {
   V tau[6];
   apply_C<T, V>(nc, lam, mu, e, tau);
   // tensor form of tau
@@ -306,7 +347,6 @@ __device__ __forceinline__ void green_op(int nc, T lam, T mu, T alpha, const T* 
              t[a][0].y * g[0] + t[a][1].y * g[1] + t[a][2].y * g[2]};
   }
   V G = V{g[0] * F[0].x + g[1] * F[1].x + g[2] * F[2].x, g[0] * F[0].y + g[1] * F[1].y + g[2] * F[2].y};
-  const T h = (T)0.5 / mu, am = -alpha / mu;
   const int ia3[6] = {0, 1, 2, 1, 0, 0}, ib3[6] = {0, 1, 2, 2, 2, 1};
   const int ia2[3] = {0, 1, 0}, ib2[3] = {0, 1, 1};
   V d[6];
@@ -358,6 +398,41 @@ __device__ __forceinline__ double wrapf(int k, int n) {
   return s - round(s);
 }
 
+// Unit wave vector g (axis order 2, 1, 0) of the wave numbers (k0, k1, k2):
+// f_a = wrapf(k_a, n_a), g = f / |f|, in FP64 for FP64 transforms.
+template <typename T>
+__device__ __forceinline__ void unit_wave(int k0, int k1, int k2, const GreenArgs& ga, T* g) {
+  const double f2 = wrapf(k2, ga.n2), f1 = wrapf(k1, ga.n1), f0 = ga.is3d ? wrapf(k0, ga.n0) : 0.0;
+  const double gn = sqrt(f2 * f2 + f1 * f1 + f0 * f0);
+  g[0] = (T)(f2 / gn);
+  g[1] = (T)(f1 / gn);
+  g[2] = (T)(f0 / gn);
+}
+// For pair transforms without FP64 instructions: the wrapped wave number w
+// (the Nyquist number maps to -n/2, as in wrapf) times the pair 1/n, then
+// 1/|f| by Newton's iteration for the reciprocal square root,
+// y <- y + y (1 - F y^2) / 2, two steps in pairs from the FP32 estimate
+// (relative error near the pairs' 2^-47).
+__device__ __forceinline__ dfl wrap_pair(int k, int n, const float* inv) {
+  const int w = 2 * k < n ? k : k - n;
+  return dfl((float)w, 0.f) * dfl(inv[0], inv[1]);
+}
+template <>
+__device__ __forceinline__ void unit_wave<dfl>(int k0, int k1, int k2, const GreenArgs& ga, dfl* g) {
+  const dfl f2 = wrap_pair(k2, ga.n2, ga.pr[5]), f1 = wrap_pair(k1, ga.n1, ga.pr[4]);
+  const dfl f0 = ga.is3d ? wrap_pair(k0, ga.n0, ga.pr[3]) : dfl(0.f, 0.f);
+  const dfl F = f2 * f2 + f1 * f1 + f0 * f0;
+  dfl y(rsqrtf(F.hi), 0.f);
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const dfl e = dfl(1.f, 0.f) - F * (y * y);
+    y = y + y * e * dfl(0.5f, 0.f);
+  }
+  g[0] = f2 * y;
+  g[1] = f1 * y;
+  g[2] = f0 * y;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ spec, int n, long long stride,
                                                long long inner, long long Nk, int L, Sched sc,
@@ -380,8 +455,9 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
   }
   __syncthreads();
   V* res = fft_lines<V, -1>(a, b, nc * L, ld, sc, tw);
-  const T lam = (T)ga.lambda, mu = (T)ga.mu;
-  const T alpha = (T)((ga.lambda + ga.mu) / (ga.lambda + 2.0 * ga.mu));
+  const T lam = green_const<T>(ga.lambda, ga.pr[0]), mu = green_const<T>(ga.mu, ga.pr[1]);
+  const T alpha = green_const<T>((ga.lambda + ga.mu) / (ga.lambda + 2.0 * ga.mu), ga.pr[2]);
+  const T hm = (T)0.5 / mu, am = -alpha / mu;
   for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
     const int p = idx / L, l = idx - p * L;
     const long long q = q0 + l;
@@ -432,20 +508,19 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
       }
       apply_C<T, V>(nc, lam, mu, d, sig);
     } else {
-      const double f2 = wrapf(k2, ga.n2), f1 = wrapf(k1, ga.n1), f0 = ga.is3d ? wrapf(k0, ga.n0) : 0.0;
-      const double gn = sqrt(f2 * f2 + f1 * f1 + f0 * f0);
-      T g[3] = {(T)(f2 / gn), (T)(f1 / gn), (T)(f0 / gn)};
+      T g[3];
+      unit_wave<T>(k0, k1, k2, ga, g);
       const bool ny2 = (ga.n2 % 2 == 0) && (2 * k2 == ga.n2);
       const bool ny1 = (ga.n1 % 2 == 0) && (2 * k1 == ga.n1);
       const bool ny0 = ga.is3d && (ga.n0 % 2 == 0) && (2 * k0 == ga.n0);
-      green_op<T, V>(nc, lam, mu, alpha, g, e, sig);
+      green_op<T, V>(nc, lam, mu, hm, am, g, e, sig);
       if (ny2 || ny1 || ny0) {
         if (nc == 3) {
           // 2D: the reference's real part of a complex transform, i.e. the
           // average of the operators at k and -k
           T gm[3] = {ny2 ? -g[0] : g[0], ny1 ? -g[1] : g[1], ny0 ? -g[2] : g[2]};
           V s2[6];
-          green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
+          green_op<T, V>(nc, lam, mu, hm, am, gm, e, s2);
           for (int c = 0; c < nc; c++) sig[c] = V{(T)0.5 * (sig[c].x + s2[c].x), (T)0.5 * (sig[c].y + s2[c].y)};
         } else {
           // 3D: average over every sign choice of the Nyquist components,
@@ -456,7 +531,7 @@ __global__ void __launch_bounds__(256) k_green(typename VT<T>::V* __restrict__ s
             if (((sg & 1) && !ny2) || ((sg & 2) && !ny1) || ((sg & 4) && !ny0)) continue;
             T gm[3] = {(sg & 1) ? -g[0] : g[0], (sg & 2) ? -g[1] : g[1], (sg & 4) ? -g[2] : g[2]};
             V s2[6];
-            green_op<T, V>(nc, lam, mu, alpha, gm, e, s2);
+            green_op<T, V>(nc, lam, mu, hm, am, gm, e, s2);
             for (int c = 0; c < nc; c++) sig[c] = vadd(sig[c], s2[c]);
             nv++;
           }
@@ -504,6 +579,8 @@ template <> __device__ __forceinline__ dfl from_f32<dfl>(float v) { return dfl(v
 template <typename T> struct ErrAcc { using A = float; };
 template <> struct ErrAcc<double> { using A = double; };
 __device__ __forceinline__ double acc_of(double x) { return x; }
+__device__ __forceinline__ double amax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float amax(float a, float b) { return fmaxf(a, b); }
 __device__ __forceinline__ float acc_of(float x) { return x; }
 __device__ __forceinline__ float acc_of(dfl x) { return to_f32(x); }
 
@@ -687,10 +764,10 @@ __global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __rest
   }
   __syncthreads();
   const V* res = fft_lines<V, +1>(b, a, NC * L, ld, sh, tw_h);
-  const T invNT = (T)invN;
+  const T invNT = from_f64<T>(invN);
   using A = typename ErrAcc<T>::A;
   T ua[NC];
-  for (int c = 0; c < NC; c++) ua[c] = uadd ? (T)uadd[c] : (T)0.0;
+  for (int c = 0; c < NC; c++) ua[c] = uadd ? from_f64<T>(uadd[c]) : (T)0.0;
   A mxa = 0, ssa = 0, sra = 0, mra = 0;
   for (int idx = threadIdx.x, q = 0; idx < L * n2; idx += blockDim.x, q++) {
     const int l = idx / n2, i = idx - l * n2;
@@ -722,13 +799,14 @@ __global__ void __launch_bounds__(256) k_c2r_dev(const typename VT<T>::V* __rest
     ssa += e2;
     sra += n2s;
   }
-  double mx = (double)mxa, ss = (double)ssa, sr = (double)sra, mr = (double)mra;
+  // warp totals in the accumulator's type, block totals in FP64
   for (int off = 16; off > 0; off >>= 1) {
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, off));
-    ss += __shfl_xor_sync(0xffffffffu, ss, off);
-    sr += __shfl_xor_sync(0xffffffffu, sr, off);
+    mxa = amax(mxa, __shfl_xor_sync(0xffffffffu, mxa, off));
+    mra = amax(mra, __shfl_xor_sync(0xffffffffu, mra, off));
+    ssa += __shfl_xor_sync(0xffffffffu, ssa, off);
+    sra += __shfl_xor_sync(0xffffffffu, sra, off);
   }
+  double mx = (double)mxa, ss = (double)ssa, sr = (double)sra, mr = (double)mra;
   __shared__ double red[4][8];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) { red[0][w] = mx; red[1][w] = ss; red[2][w] = sr; red[3][w] = mr; }
@@ -895,6 +973,14 @@ int solve_t(const FFTPlan& p, const SolveArgs& a, cudaStream_t st, int64_t* laun
   ga.lambda = a.lambda; ga.mu = a.mu;
   ga.Ntot = (double)p.N;
   ga.disp = a.disp;
+  {
+    const double cst[6] = {a.lambda, a.mu, (a.lambda + a.mu) / (a.lambda + 2.0 * a.mu), 1.0 / p.n0, 1.0 / p.n1,
+                           1.0 / p.n2};
+    for (int i = 0; i < 6; i++) {
+      ga.pr[i][0] = (float)cst[i];
+      ga.pr[i][1] = (float)(cst[i] - (double)ga.pr[i][0]);
+    }
+  }
   // components left for the inverse passes: the displacement has one per axis
   const int nco = a.disp ? (p.n0 > 1 ? 3 : 2) : p.nc;
   if (p.n0 > 1) {

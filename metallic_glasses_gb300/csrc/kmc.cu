@@ -1250,26 +1250,39 @@ __host__ __device__ __forceinline__ int mix_stage_floats(int n2) {
 __host__ __device__ __forceinline__ size_t mix_smem_bytes(int n2) {
   return (size_t)(TH / 32) * 2 * mix_stage_floats(n2) * sizeof(float);
 }
+// Run length of the single-grid main pass's stages: lines of 256 sites are
+// staged and computed in two pieces of 128 (a block's stages then stay at
+// 49 KB, three blocks to an SM); other lines whole.
+__host__ __device__ constexpr int mix_piece(int n2) { return n2 == 256 ? 128 : n2; }
+// Dynamic shared memory of a single-grid main block: the stages of its
+// pieces, and for lines in pieces each thread's 20 rate sums parked between
+// pieces (20 KB).
+__host__ __device__ __forceinline__ size_t mix_smem_main_bytes(int n2) {
+  return mix_smem_bytes(mix_piece(n2)) + (mix_piece(n2) != n2 ? (size_t)TH * STZ_MODES * sizeof(float) : 0);
+}
 
+// Stage the sites off .. off + len - 1 of line (i0, i1).
 template <int UPDATE_ONLY>
-__device__ __forceinline__ void issue_line(const MixK& kp, int i0, int i1, float* stage, unsigned long long* bar) {
-  const long long base = ((long long)i0 * kp.n1 + i1) * kp.n2;
-  const unsigned bytes = (unsigned)kp.n2 * 4u;
+__device__ __forceinline__ void issue_line(const MixK& kp, int i0, int i1, int off, int len, float* stage,
+                                           unsigned long long* bar) {
+  const long long base = ((long long)i0 * kp.n1 + i1) * kp.n2 + off;
+  const unsigned bytes = (unsigned)len * 4u;
   // the generic-proxy reads and writes of this stage are done (syncwarp by
   // the caller); order them before the asynchronous writes
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   mbar_expect_tx(bar, (UPDATE_ONLY ? 5u : 6u) * bytes);
 #pragma unroll
-  for (int k = 0; k < 5; k++) bulk_g2s(stage + k * kp.n2, kp.sdev + (long long)k * kp.N + base, bytes, bar);
-  if (!UPDATE_ONLY) bulk_g2s(stage + 5 * kp.n2, kp.dF32 + base, bytes, bar);
+  for (int k = 0; k < 5; k++) bulk_g2s(stage + k * len, kp.sdev + (long long)k * kp.N + base, bytes, bar);
+  if (!UPDATE_ONLY) bulk_g2s(stage + 5 * len, kp.dF32 + base, bytes, bar);
 }
 
-// One line (i0, i1) by one warp from its staged inputs: update every site,
-// and (unless UPDATE_ONLY) accumulate the lane's 20 rate sums in acc2. Unless
-// LINEVOTE (the athermal test is then made per line from the mode sums), set
-// neg when a site's largest argument exceeds thr_neg.
+// One line (i0, i1), or its piece h of mix_piece(N2) sites, by one warp from
+// its staged inputs: update every site, and (unless UPDATE_ONLY) accumulate
+// the lane's 20 rate sums in acc2. Unless LINEVOTE (the athermal test is then
+// made per line from the mode sums), set neg when a site's largest argument
+// exceeds thr_neg.
 template <int UPDATE_ONLY, int LINEVOTE, int N2>
-__device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int i0, int i1,
+__device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int i0, int i1, int h,
                                            int p0, int p1, int p2, const float* de, const float* Ud,
                                            const float2* md, const float* stage, float2* acc2, unsigned& neg,
                                            float thr_neg) {
@@ -1290,21 +1303,22 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
   dl[7] = sy;
   const int base = (i0 * kp.n1 + i1) * n2;
   if constexpr (N2 > 0 && LINEVOTE && !UPDATE_ONLY) {
-    // each lane's N2 / 32 sites lane + 32 q in one pass; offsets are immediates
-    constexpr int kKt2 = N2 / 2 + 1, kQ = N2 / 32;
+    // each lane's sites lane + 32 q of the piece in one pass; offsets are
+    // immediates
+    constexpr int kKt2 = N2 / 2 + 1, kP = mix_piece(N2), kQ = kP / 32;
     float t[kQ][5], a[kQ];
 #pragma unroll
     for (int q = 0; q < kQ; q++) {
-      const int i2 = lane + 32 * q;
+      const int si = lane + 32 * q, i2 = si + kP * h;
       int fx;
       const int d2 = fold(i2 - p2, N2, &fx);
       float sv[5];
 #pragma unroll
-      for (int k = 0; k < 5; k++) sv[k] = stage[k * N2 + i2];
+      for (int k = 0; k < 5; k++) sv[k] = stage[k * kP + si];
       mixed_update(kp.sdev, N32, base + i2, hp, row + d2, kKt2, fx ? -1.f : 1.f, dl, Ud, sv);
 #pragma unroll
       for (int k = 0; k < 5; k++) t[q][k] = __fmul_rn(sv[k], kp.inv_kt);
-      a[q] = (kp.q_ref - stage[5 * N2 + i2]) * kp.a_scale;
+      a[q] = (kp.q_ref - stage[5 * kP + si]) * kp.a_scale;
     }
     mixed_rates_q<kQ>(t, a, md, acc2);
     return;
@@ -1470,8 +1484,12 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   unsigned neg = 0;
   const int N32 = (int)k.N;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sf = mix_stage_floats(k.n2);
+  // pieces per line and their length (whole lines but for the 256-site pass)
+  constexpr int kPieces = (N2 > 0 && LINEVOTE && !UPDATE_ONLY) ? N2 / mix_piece(N2) : 1;
+  const int plen = kPieces > 1 ? mix_piece(N2) : k.n2;
+  const int sf = mix_stage_floats(plen);
   float* stages = mix_smem + (size_t)w * 2 * sf;
+  float4* park = reinterpret_cast<float4*>(mix_smem + (size_t)(TH / 32) * 2 * sf) + threadIdx.x * (STZ_MODES / 4);
   unsigned long long* bar = &mbar[w][0];
   if (lane == 0) {
     mbar_init(&bar[0], 1);
@@ -1480,38 +1498,64 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   }
   __syncwarp();
   // this warp's lines: units b, b + nblk, ... (skipping the ones where the
-  // warp idles); line j lives in stage j & 1
+  // warp idles), each in kPieces pieces; piece j of the warp lives in stage
+  // j & 1, and the next piece's copy is in flight while a piece is computed.
+  // The next line is found before the line's first piece; between the pieces
+  // of a line the rate sums wait in shared memory (the registers are at the
+  // three-block limit).
   int u = b;
   LineOf L{0, 0, 0};
   for (; u < k.mx_units; u += k.nblk)
     if ((L = unit_line(k, u, w, p0, p1)).valid) break;
-  if (u < k.mx_units && lane == 0) issue_line<UPDATE_ONLY>(k, L.i0, L.i1, stages, &bar[0]);
+  if (u < k.mx_units && lane == 0) issue_line<UPDATE_ONLY>(k, L.i0, L.i1, 0, plen, stages, &bar[0]);
   unsigned pending = u < k.mx_units ? 1u : 0u;  // stages with a copy in flight
   unsigned ppar = 0;                                // bit k: parity the copy of stage k completes
   bool timed_out = false;
-  for (int j = 0; u < k.mx_units; j++) {
+  for (int j = 0; u < k.mx_units;) {
     int un = u + k.nblk;
     LineOf Ln{0, 0, 0};
     for (; un < k.mx_units; un += k.nblk)
       if ((Ln = unit_line(k, un, w, p0, p1)).valid) break;
-    float* cur = stages + (j & 1) * sf;
-    float* nxt = stages + ((j + 1) & 1) * sf;
-    __syncwarp();
-    if (un < k.mx_units) {
-      if (lane == 0) issue_line<UPDATE_ONLY>(k, Ln.i0, Ln.i1, nxt, &bar[(j + 1) & 1]);
-      pending |= 1u << ((j + 1) & 1);
-      ppar = (ppar & ~(1u << ((j + 1) & 1))) | ((((unsigned)(j + 1) >> 1) & 1u) << ((j + 1) & 1));
-    }
-    if (!mbar_wait(&bar[j & 1], (unsigned)(j >> 1) & 1u)) {
-      pending &= ~(1u << (j & 1));  // waited for already, to the limit
-      timed_out = true;
-      break;
-    }
-    pending &= ~(1u << (j & 1));
     float2 acc2[STZ_MODES / 2];
 #pragma unroll
     for (int q = 0; q < STZ_MODES / 2; q++) acc2[q] = make_float2(0.f, 0.f);
-    mixed_line<UPDATE_ONLY, LINEVOTE, N2>(k, N32, hp, L.i0, L.i1, p0, p1, p2, de, Ud, md, cur, acc2, neg, thr_neg);
+    float* cur = stages;
+#pragma unroll 1
+    for (int h = 0; h < kPieces; h++, j++) {
+      const bool last = h == kPieces - 1;
+      cur = stages + (j & 1) * sf;
+      float* nxt = stages + ((j + 1) & 1) * sf;
+      __syncwarp();
+      if (!last || un < k.mx_units) {
+        if (lane == 0)
+          issue_line<UPDATE_ONLY>(k, last ? Ln.i0 : L.i0, last ? Ln.i1 : L.i1, last ? 0 : (h + 1) * plen, plen, nxt,
+                                  &bar[(j + 1) & 1]);
+        pending |= 1u << ((j + 1) & 1);
+        ppar = (ppar & ~(1u << ((j + 1) & 1))) | ((((unsigned)(j + 1) >> 1) & 1u) << ((j + 1) & 1));
+      }
+      if (!mbar_wait(&bar[j & 1], (unsigned)(j >> 1) & 1u)) {
+        pending &= ~(1u << (j & 1));  // waited for already, to the limit
+        timed_out = true;
+        break;
+      }
+      pending &= ~(1u << (j & 1));
+      if (kPieces > 1 && h > 0) {
+#pragma unroll
+        for (int q = 0; q < STZ_MODES / 4; q++) {
+          const float4 v = park[q];
+          acc2[2 * q] = make_float2(v.x, v.y);
+          acc2[2 * q + 1] = make_float2(v.z, v.w);
+        }
+      }
+      mixed_line<UPDATE_ONLY, LINEVOTE, N2>(k, N32, hp, L.i0, L.i1, h, p0, p1, p2, de, Ud, md, cur, acc2, neg,
+                                            thr_neg);
+      if (kPieces > 1 && !last) {
+#pragma unroll
+        for (int q = 0; q < STZ_MODES / 4; q++)
+          park[q] = make_float4(acc2[2 * q].x, acc2[2 * q].y, acc2[2 * q + 1].x, acc2[2 * q + 1].y);
+      }
+    }
+    if (timed_out) break;
     if (!UPDATE_ONLY) {
       // the consumed stage holds the transpose
       __syncwarp();
@@ -2371,6 +2415,7 @@ static void mixed_smem_init() {
   };
   raise((const void*)k_mixed<0>);
   raise((const void*)k_mixed<0, 128>);
+  raise((const void*)k_mixed<0, 256>);
   raise((const void*)k_mixed<1>);
   raise((const void*)k_mixed<0, 32>);
   raise((const void*)k_mixed<0, 64>);
@@ -2392,7 +2437,7 @@ size_t mixed_smem(int n2) { return mix_smem_bytes(n2); }
 int mixed_blocks_per_sm(int n2) {
   mixed_smem_init();
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed<0>, TH, mix_smem_bytes(n2)) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mixed<0>, TH, mix_smem_main_bytes(n2)) != cudaSuccess ||
       occ < 1) {
     (void)cudaGetLastError();
     occ = 1;
@@ -2472,6 +2517,7 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   mixed_smem_init();
   if (update_only) k_mixed<1><<<kp.nblk, TH, mix_smem_bytes(kp.n2), st>>>(kp, f);
+  else if (kp.n2 == 256) launch_pdl(k_mixed<0, 256>, dim3(kp.nblk), mix_smem_main_bytes(256), st, kp, f);
   else if (kp.n2 == 128) launch_pdl(k_mixed<0, 128>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 96) launch_pdl(k_mixed<0, 96>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 64) launch_pdl(k_mixed<0, 64>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);

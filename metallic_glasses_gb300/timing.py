@@ -3,6 +3,7 @@
   python -m metallic_glasses_gb300.timing kernel --grid 128 --which 0 --steps 8
   python -m metallic_glasses_gb300.timing solve --grid 256
   python -m metallic_glasses_gb300.timing batch --replicas 256 --events 32
+  python -m metallic_glasses_gb300.timing run --config grf256 --events 20000
 
 `kernel` times one per-event kernel of the mixed form launch by launch with
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
@@ -11,7 +12,9 @@ of the full field (the FFT passes) with the tuned schedule. `batch` advances ind
 replicas (grid sizes 32^3..96^3, temperatures and strain rates drawn from the
 seed) together in one batch, then the same replicas one at a time, and prints
 both aggregate rates (one at a time = each replica in its own
-context through stz_run, the single-run path). Both are the commands the ncu summaries are
+context through stz_run, the single-run path). `run` advances one study
+configuration through stz_run and reports its event rate and the stress error
+of its periodic re-solves. These are the commands the ncu summaries are
 taken on.
 """
 import argparse
@@ -107,6 +110,39 @@ def batch(replicas, events, alone=None, seed0=0):
             "alone_sample": n1}
 
 
+RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128}
+
+
+def run(config, events, warmup=1000, grid=None):
+    """Thermal events per second of one configuration through stz_run.
+
+    Context creation (response table, FFT tuning, the first solve) and
+    `warmup` events come before the timed region; the timed region holds
+    `events` driver steps and the periodic full re-solves that fall in them,
+    timed with CUDA events on the context's stream. stress_err_* are the
+    worst differences between the incremental stress and a full re-solve seen
+    so far (rms over sites and max, relative to the field's scale)."""
+    p = RUN_CONFIGS[config]() if grid is None else RUN_CONFIGS[config](n=grid)
+    t0 = time.perf_counter()
+    eng = api.Engine(p)
+    eng.sync()
+    create_s = time.perf_counter() - t0
+    eng.run(max_events=warmup)
+    s0 = eng.scalars()
+    eng.timer_start()
+    eng.run(max_events=events)
+    ms = eng.timer_stop()
+    s1 = eng.scalars()
+    eng.close()
+    k = s1["kstep"] - s0["kstep"]
+    return {"config": config, "grid": list(p.n), "sites": p.n[0] * p.n[1] * p.n[2], "create_s": create_s,
+            "events": k, "athermal_steps": s1["astep"] - s0["astep"], "ms": ms,
+            "events_per_s": k / (ms / 1e3), "us_per_event": ms * 1e3 / max(k, 1),
+            "resolves": s1["n_resolves"] - s0["n_resolves"],
+            "stress_err_rms_worst": s1["stress_err_rms_worst"], "stress_err_max_worst": s1["stress_err_max_worst"],
+            "strain": s1["eps_avg"], "stopped": s1["stopped"]}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m metallic_glasses_gb300.timing")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -124,11 +160,18 @@ def main(argv=None):
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
     b.add_argument("--alone", type=int, default=None)
+    r = sub.add_parser("run")
+    r.add_argument("--config", choices=sorted(RUN_CONFIGS), default="grf256")
+    r.add_argument("--events", type=int, default=20000)
+    r.add_argument("--warmup", type=int, default=1000)
+    r.add_argument("--grid", type=int, default=None)
     a = ap.parse_args(argv)
     if a.cmd == "kernel":
         out = kernel(a.grid, a.which, a.steps)
     elif a.cmd == "solve":
         out = solve(a.grid, a.reps, fp64=a.fp64, profile_range=a.profile_range)
+    elif a.cmd == "run":
+        out = run(a.config, a.events, a.warmup, a.grid)
     else:
         out = batch(a.replicas, a.events, a.alone)
     print(json.dumps(out), flush=True)

@@ -74,3 +74,27 @@ def test_athermal_trigger_forms_agree(engine_lib):
     assert np.array_equal(a["time"], b["time"])
     eng.close()
     batch.close()
+
+
+def test_256_site_lines_match_general_pass(engine_lib):
+    """The single-grid main pass for 256-site lines (staged and computed in two
+    pieces of 128, the rate sums parked in shared memory between them) against
+    the general pass that the batched form runs for such lines: the same
+    events at the same times and the same stored field on a 16 x 16 x 256
+    grid."""
+    p = configs.mixed128(n=256, resolve_period=100)
+    p.n[0], p.n[1], p.n[2] = 16, 16, 256
+    eng = api.Engine(p)
+    eng.run(max_events=250)
+    batch = api.Batch([p])
+    batch.run(250)
+    r = batch.replicas[0]
+    a, b = eng.events(), r.events()
+    assert len(a) == len(b) == 250
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(a["time"], b["time"])
+    for c in range(5):
+        assert np.array_equal(eng.field(api.FIELD_SDEV, c), r.field(api.FIELD_SDEV, c)), c
+    eng.close()
+    batch.close()

@@ -191,16 +191,19 @@ def test_mixed_first_resolve_error_small(engine_lib):
     assert sc["stress_err_max_worst"] < 1e-6
 
 
-def test_mixed_pair_resolve_matches_fp64(engine_lib):
+@pytest.mark.parametrize("n", [32, 24])
+def test_mixed_pair_resolve_matches_fp64(engine_lib, n):
     """The mixed form's field solves in FP32 pairs (the default) against the
     same solves in FP64 (resolve_fp64 = 1): after the start solve and three
-    periodic re-solves of a 32^3 run the stored FP32 field agrees to within one
+    periodic re-solves of an n^3 run the stored FP32 field agrees to within one
     FP32 rounding, the events are the same, and the measured stress errors of
     the incremental field agree to 1e-4 of their size (the pair transform
-    carries about 48 bits; its error norms are summed in FP32 per thread)."""
+    carries about 48 bits; its error norms are summed in FP32 per warp). At
+    24^3 the wave numbers' 1/n is not a binary fraction and the transforms
+    take radix-3 passes."""
     out = {}
     for fp64 in (0, 1):
-        p = configs.mixed128(n=32, resolve_period=100)
+        p = configs.mixed128(n=n, resolve_period=100)
         p.resolve_fp64 = fp64
         e = api.Engine(p)
         e.run(max_events=300)
