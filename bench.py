@@ -253,7 +253,8 @@ def main():
     tr = traffic_record("k_mixed", n)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": tr,
-            "kernel": "k_mixed (incremental update + rates + FP64 partial sums + last-block select/commit)",
+            "kernel": "k_mixed<0, 128> (incremental stress update, 20 mode rates, FP32 line sums and the "
+                      "athermal vote per line; the plane sums and the selection follow in k_mixed_select)",
             "alg_bytes_per_launch": alg_bytes, "launch_ms": k_ms, "launches_timed": k_n,
             "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
             "alg_bytes_full_resolve_per_event": 24 * N * 4,
