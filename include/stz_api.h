@@ -23,8 +23,10 @@
  *                                  elastic.c:977-1066, elastic.c:779-903
  *   stz_elastic_energy          <- ElasticEnergy()                     elastic.c:533-547
  *   stz_destroy                 <- Free()                              init.c:482-559
- * The reference-named entry points themselves (KMC, ActEnergy, ...) are
- * declared in stz_refapi.h.
+ * The reference-named entry points themselves (KMC, ActEnergy, ...,
+ * WriteScalarMPI) are defined in metallic_glasses_gb300/refapi/refapi.c on
+ * top of this interface; the reference's own bmg.h declares them, so that
+ * file is compiled against the user's bmg.h, my_fft.h and bmgFlags.h.
  */
 #ifndef STZ_API_H
 #define STZ_API_H

@@ -414,6 +414,31 @@ void RecordFree(void) {
   EqStrain = EqStress = NULL;
 }
 
+/* io.c:289-347: a field as the reference's binary record "<s>_S<step>.iout",
+ * the raw native values of the ranks' slabs in rank order (what MPI-IO
+ * writes with the view rank * lsize). Here one rank holds the whole grid, so
+ * rank 0 writes the file alone; the bytes are those of a single-rank run of
+ * the reference. A file that cannot be written ends the run, as the
+ * reference's other record files do. */
+static void write_record(const void* field, size_t elem, const char* s, int step) {
+  if (rank != 0) return;
+  char fname[256];
+  snprintf(fname, sizeof fname, "%s_S%03d.iout", s, step);
+  FILE* f = fopen(fname, "wb");
+  if (!f || fwrite(field, elem, (size_t)lsize, f) != (size_t)lsize) {
+    perror(fname);
+    if (f) fclose(f);
+    MPI_Abort(MPI_COMM_WORLD, -1);
+    return;
+  }
+  fclose(f);
+}
+
+void WriteScalarMPI(real* field, char* s, int step) { write_record(field, sizeof(real), s, step); }
+void WriteScalarMPI_INT(int* field, char* s, int step) { write_record(field, sizeof(int), s, step); }
+/* the reference copies the map before writing it; the bytes are the same */
+void WriteMROMPI_INT(int* field, char* s, int step) { write_record(field, sizeof(int), s, step); }
+
 void ParameterPrint(void) {
   printf("\nSimulation Geometry:\n");
   printf("System size:\t[%d x %d]\n", NX, NY);

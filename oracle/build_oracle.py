@@ -50,13 +50,15 @@ def ref_available():
     return os.path.isdir(REF_DIR)
 
 
-def build_ref2d(nx=64, ny=64, loading="TENSION", force=False):
-    """Compile the reference at an NX x NY grid; returns the binary path."""
+def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False):
+    """Compile the reference at an NX x NY grid; returns the binary path.
+    full_tensor: also define FULL_TENSOR_RECORD, so that the reference's main
+    writes Eps0 and Sigma of every print as .iout records (bmg.c:269-277)."""
     if not ref_available():
         raise FileNotFoundError("reference tree not present")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
-    out = os.path.join(out_dir, "ref2d_%dx%d_%s" % (nx, ny, loading))
+    out = os.path.join(out_dir, "ref2d_%dx%d_%s%s" % (nx, ny, loading, "_ftr" if full_tensor else ""))
     mine = [os.path.join(HERE, f) for f in ("ref_wrap.c", "stz_oracle.c", "stz_oracle.h",
                                             "shim/shim.c", "shim/mpi.h", "shim/fftw_mpi.h",
                                             "shim/gsl/gsl_rng.h", "shim/gsl/gsl_randist.h")]
@@ -66,6 +68,8 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False):
     defs = ["-DSTZ_SHIM_NX=%d" % nx, "-DSTZ_SHIM_NY=%d" % ny]
     if loading == "SHEAR":
         defs.append("-DSTZ_SHIM_LOAD_SHEAR")
+    if full_tensor:
+        defs.append("-DFULL_TENSOR_RECORD")
     inc = ["-I", os.path.join(HERE, "shim"), "-I", REF_DIR]
     wraps = ["-Wl,--wrap=VoxelShearTransform", "-Wl,--wrap=KMC",
              "-Wl,--wrap=athermal_plasticity", "-Wl,--wrap=ActEnergy", "-Wl,--wrap=Free"]

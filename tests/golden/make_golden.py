@@ -16,12 +16,16 @@ directory and stores, per case:
                                    wrote at P = 4 of its prints spread over the
                                    run (X1R/X2R files, "%lf" text: 6 decimals)
                xr_k       int64 [P]  their print numbers (the files' %03d)
+               iout       float64 [P, 2, 3, N] (cases in IOUT_CASES) Eps0 and
+                                   Sigma of the same prints as the reference's
+                                   main writes them with FULL_TENSOR_RECORD
+                                   (Strain_0c/Stress_0c_S%03d.iout, raw FP64)
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
 
 Only this script reads the reference tree; tests read the .npz files.
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [case ...]   (all fixtures when no case is named)
 """
 import os
 import subprocess
@@ -47,8 +51,13 @@ CASES = {
 }
 
 
+# cases whose reference build also writes the .iout records of its prints
+IOUT_CASES = {"ref2d_32_tension_nosoft_s5"}
+
+
 def run_case(name, nx, ny, loading, overrides, events):
-    exe = build_ref2d(nx, ny, loading)
+    ftr = name in IOUT_CASES
+    exe = build_ref2d(nx, ny, loading, full_tensor=ftr)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
     env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS=str(events),
@@ -89,13 +98,17 @@ def run_case(name, nx, ny, loading, overrides, events):
     xr_k = sorted({max(1, n_prints // 8), max(1, n_prints // 3), max(1, 2 * n_prints // 3), n_prints})
     xr = [[np.loadtxt(os.path.join(d, "X%dR%03d_P00.out" % (a, k))).reshape(-1) for a in (1, 2)] for k in xr_k]
     xr = np.array(xr, np.float64).reshape(len(xr_k), 2, N)
+    extra = {}
+    if ftr:
+        extra["iout"] = np.array([[[np.fromfile(os.path.join(d, "%s_%02d_S%03d.iout" % (w, c + 1, k)), np.float64)
+                                    for c in range(3)] for w in ("Strain", "Stress")] for k in xr_k])
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
     np.savez_compressed(out, X=np.array(X, np.int64), S=S[:, :3], S10=S[::10], hdr=hdr, sc=sc, sigma=sigma,
                         eps0=eps0, tlast=tlast, perm_soft=perm, temp_soft=temp, deps_sum=deps.sum(axis=(0, 2)),
                         nx=nx, ny=ny, loading=loading, overrides=repr(overrides), events=events, xr=xr,
-                        xr_k=np.array(xr_k, np.int64))
+                        xr_k=np.array(xr_k, np.int64), **extra)
     print(name, "transforms", len(X), "steps", len(S), "hdr", hdr, "->", out)
 
 
@@ -153,7 +166,10 @@ def inhom_case(nx=32, ny=32):
 
 if __name__ == "__main__":
     build_oracle_lib()
-    inhom_case()
-    mt_kat()
+    only = sys.argv[1:]
+    if not only:
+        inhom_case()
+        mt_kat()
     for name, (nx, ny, loading, ov, ev) in CASES.items():
-        run_case(name, nx, ny, loading, ov, ev)
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev)

@@ -78,6 +78,9 @@ void ParameterPrint(void);
 void PrintFlags(void);
 void RecordPrep(void);
 void RecordFree(void);
+void WriteScalarMPI(real* field, char* s, int step);
+void WriteScalarMPI_INT(int* field, char* s, int step);
+void WriteMROMPI_INT(int* field, char* s, int step);
 void DispField(real* XR[2]);
 void ActEnergy(int step);
 void SofteningFactor(void);

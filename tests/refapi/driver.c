@@ -1,6 +1,6 @@
 /* Test driver of the reference API on the GB300 engine: the call sequence
  * of the reference's main loop (bmg.c:30-410, 2D, INHOM_ELAST), without its
- * output files, stopped after REFAPI_MAX_EVENTS thermal events. It writes
+ * text output files, stopped after REFAPI_MAX_EVENTS thermal events. It writes
  *   steps.txt   per driver step: step kind time EpsAvg[3] Stress[3]
  *               (kind 0 thermal, 1 athermal, 2 elastic)
  *   events.txt  per transformation: step kind site mode (from the engine log)
@@ -8,6 +8,9 @@
  *               REFAPI_XR_PRINTS (comma-separated print numbers; all prints when
  *               unset), named and formatted as the reference's main writes them
  *               (bmg.c:300-330)
+ *   Strain_0c_S%03d.iout, Stress_0c_S%03d.iout  Eps0 and Sigma of the same
+ *               prints through WriteScalarMPI, where the reference's main writes
+ *               them under FULL_TENSOR_RECORD (bmg.c:269-277)
  * in the working directory, which holds the reference's "input" file. */
 #define BMG_GLOBALS_ONCE
 #include "bmg.h"
@@ -70,22 +73,29 @@ int main(int argc, char** argv) {
             EpsAvg[2], Stress[0], Stress[1], Stress[2]);
     if (fabs(EpsAvg[lc] - last_print) >= (printperiod * strainincrement * 0.99)) {
       last_print = EpsAvg[lc];
-      RecordPrep();
-      for (m = 0; m < MODES; m++)
-        for (i = 0; i < lnx; i++)
-          for (j = 0; j < NY; j++) Q0[m][i * NY + j] = Q1[m][i * NY + j];
-      RecordFree();
-      InhomogeneousStressSolver(Lambda, Mu, Eps0, EpsAvg, lambda, mu, XR, TotEps, Sigma, Stress, 2);
-      n_print++;
       int want = !xr_list;
       if (xr_list) {
         const char* q = xr_list;
         while (*q && !want) {
-          if (atoi(q) == n_print - 1) want = 1;
+          if (atoi(q) == n_print) want = 1;
           while (*q && *q != ',') q++;
           if (*q == ',') q++;
         }
       }
+      RecordPrep();
+      for (m = 0; m < MODES; m++)
+        for (i = 0; i < lnx; i++)
+          for (j = 0; j < NY; j++) Q0[m][i * NY + j] = Q1[m][i * NY + j];
+      for (int c = 0; c < 3 && want; c++) {
+        char fname[32];
+        sprintf(fname, "Strain_%02d", c + 1);
+        WriteScalarMPI(Eps0[c], fname, n_print);
+        sprintf(fname, "Stress_%02d", c + 1);
+        WriteScalarMPI(Sigma[c], fname, n_print);
+      }
+      RecordFree();
+      InhomogeneousStressSolver(Lambda, Mu, Eps0, EpsAvg, lambda, mu, XR, TotEps, Sigma, Stress, 2);
+      n_print++;
       for (int a = 0; a < 2 && want; a++) {
         char fname[64];
         sprintf(fname, "X%dR%03d_P%02d.out", a + 1, n_print - 1, rank);

@@ -8,8 +8,9 @@ GPU: the test driver, which follows the reference main's call sequence
 (ReadInput ... Alloc, Energy_Init, DStrain, solve, then per step ActEnergy,
 the Q < 0 scan, athermal_plasticity or KMC, ElasticEnergy, the print-time
 RecordPrep / Q0 reset / uflag-2 solve), reproduces the reference's own
-(step, kind, site, mode) sequence of the 32x32 tension fixture, its clock and
-the positions XR (supercell position plus displacement field) its prints write.
+(step, kind, site, mode) sequence of the 32x32 tension fixture, its clock,
+the positions XR (supercell position plus displacement field) its prints write
+and the .iout records of Eps0 and Sigma (WriteScalarMPI, FULL_TENSOR_RECORD).
 """
 import os
 import subprocess
@@ -54,10 +55,13 @@ def test_driver_links(engine_lib):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_DIR), reason="reference tree not present")
-def test_reference_main_links_unchanged(engine_lib):
+@pytest.mark.parametrize("defs", [[], ["-DFULL_TENSOR_RECORD"]])
+def test_reference_main_links_unchanged(engine_lib, defs):
+    """bmg.c as shipped, and with the FULL_TENSOR_RECORD switch of its print
+    block on (its .iout records through WriteScalarMPI)."""
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "bmg_gb300")
-        cmd = (["gcc", *CFLAGS, "-DSTZ_SHIM_NX=32", "-DSTZ_SHIM_NY=32", "-I", SHIM, "-I", REF_DIR,
+        cmd = (["gcc", *CFLAGS, *defs, "-DSTZ_SHIM_NX=32", "-DSTZ_SHIM_NY=32", "-I", SHIM, "-I", REF_DIR,
                 "-I", os.path.join(ROOT, "include"), os.path.join(REF_DIR, "bmg.c"), REFAPI] + _support() +
                ["-o", out] + _lib_args())
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -81,6 +85,8 @@ def test_driver_reproduces_reference_events(engine_lib):
         actq = np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2)
         xr = np.array([[np.loadtxt(os.path.join(d, "X%dR%03d_P00.out" % (a, int(k)))).reshape(-1) for a in (1, 2)]
                        for k in g["xr_k"]])
+        iout = np.array([[[np.fromfile(os.path.join(d, "%s_%02d_S%03d.iout" % (w, c + 1, int(k))), np.float64)
+                           for c in range(3)] for w in ("Strain", "Stress")] for k in g["xr_k"]])
     X = g["X"]
     assert ev.shape == X.shape
     for col, name in enumerate(("step", "kind", "site", "mode")):
@@ -106,3 +112,10 @@ def test_driver_reproduces_reference_events(engine_lib):
     ref_xr = g["xr"]
     assert xr.shape == ref_xr.shape
     assert np.abs(xr - ref_xr).max() <= 2e-6
+    # the same prints' .iout records (raw FP64 Eps0 and Sigma, FULL_TENSOR_RECORD
+    # in the reference's main): the eigenstrain is the same sum of the same
+    # draws; the stress is a different FFT of it
+    ref_io = g["iout"]
+    assert iout.shape == ref_io.shape
+    assert np.abs(iout[:, 0] - ref_io[:, 0]).max() <= 1e-12 * np.abs(ref_io[:, 0]).max()
+    assert np.abs(iout[:, 1] - ref_io[:, 1]).max() <= 1e-9 * np.abs(ref_io[:, 1]).max()
