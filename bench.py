@@ -7,8 +7,10 @@ drawn from seed 0, all state resident in HBM). L2 is flushed between steps
 same grid, the stress error of the mixed form against its full re-solves, the
 roofline of the per-event kernel, the end-to-end figure through the C ABI
 with host-side event and scalar reads, the CPU oracle timed on the host, the
-batched replicas against the same replicas one at a time, and the 256^3
-correlated-barrier run (event rate and stress error).
+batched replicas against the same replicas one at a time, the 256^3
+correlated-barrier run (event rate and stress error), the ensemble-mean
+stress-strain curves of the mixed and the plain form on the same seeds, and
+the FP64 plain form at 64^3 next to the CPU oracle on that grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -174,6 +176,8 @@ def main():
     ap.add_argument("--batch-replicas", type=int, default=256)
     ap.add_argument("--no-grf", action="store_true", help="skip the 256^3 correlated-barrier run")
     ap.add_argument("--grf-events", type=int, default=20000)
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the stress-strain ensemble of both forms")
+    ap.add_argument("--no-plain64", action="store_true", help="skip the 64^3 FP64 plain run and its CPU oracle")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -317,6 +321,26 @@ def main():
                           "length 4 voxels, shear strain rate 5e-4 /s, %d thermal events after 1000 warm-up "
                           "events, full re-solve (FP32 pairs) every 1000 events" % args.grf_events)
         line["grf256"] = gr
+    if not args.no_ensemble:
+        # ensemble-mean stress-strain curves, mixed vs FP64 plain, same seeds
+        from metallic_glasses_gb300 import timing
+        en = timing.ensemble(n, 4, max_steps=600)
+        en["workload"] = ("%d^3, barrier seeds 0..3 in both forms, shear loading at 250 K, first 600 steps "
+                          "(the elastic rise to about 0.25 GPa); rel_diff_max = largest difference of the "
+                          "two mean curves over the plain curve's peak" % n)
+        line["ensemble"] = en
+    if not args.no_plain64:
+        # the FP64 plain form at 64^3 (the reference's method: a full re-solve
+        # per event) next to the CPU oracle on the same grid, in the same run
+        from metallic_glasses_gb300 import timing
+        pl = timing.run("plain64", events=2000, warmup=100)
+        pl = {k: pl[k] for k in ("grid", "sites", "events", "athermal_steps", "ms", "events_per_s", "us_per_event")}
+        if not args.no_cpu:
+            pl["cpu_baseline"] = cpu_baseline(seconds=8.0, grid=64)
+            pl["gpu_over_cpu"] = pl["events_per_s"] / pl["cpu_baseline"]["value"]
+        pl["workload"] = ("64^3 FP64 plain form, shear strain rate 5e-5 /s, T = 455 K, seed 0, 2000 thermal "
+                          "events after 100 warm-up events, every event a full FP64 re-solve")
+        line["plain64"] = pl
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
         line["cpu_baseline_1core"] = cpu_baseline(seconds=8.0, grid=n, threads=1)

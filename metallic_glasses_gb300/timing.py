@@ -4,6 +4,7 @@
   python -m metallic_glasses_gb300.timing solve --grid 256
   python -m metallic_glasses_gb300.timing batch --replicas 256 --events 32
   python -m metallic_glasses_gb300.timing run --config grf256 --events 20000
+  python -m metallic_glasses_gb300.timing ensemble --grid 32 --seeds 8
 
 `kernel` times one per-event kernel of the mixed form launch by launch with
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
@@ -14,13 +15,18 @@ seed) together in one batch, then the same replicas one at a time, and prints
 both aggregate rates (one at a time = each replica in its own
 context through stz_run, the single-run path). `run` advances one study
 configuration through stz_run and reports its event rate and the stress error
-of its periodic re-solves. These are the commands the ncu summaries are
-taken on.
+of its periodic re-solves. `ensemble` runs the mixed and the FP64 plain form
+on the same seeds through a shear loading at low temperature and compares
+their ensemble-mean stress-strain curves. These are the commands the ncu
+summaries are taken on.
 """
 import argparse
 import ctypes
 import json
+import math
 import time
+
+import numpy as np
 
 from . import api, configs
 
@@ -110,7 +116,7 @@ def batch(replicas, events, alone=None, seed0=0):
             "alone_sample": n1}
 
 
-RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128}
+RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128, "plain64": configs.plain128}
 
 
 def run(config, events, warmup=1000, grid=None):
@@ -122,6 +128,8 @@ def run(config, events, warmup=1000, grid=None):
     timed with CUDA events on the context's stream. stress_err_* are the
     worst differences between the incremental stress and a full re-solve seen
     so far (rms over sites and max, relative to the field's scale)."""
+    if grid is None and config == "plain64":
+        grid = 64
     p = RUN_CONFIGS[config]() if grid is None else RUN_CONFIGS[config](n=grid)
     t0 = time.perf_counter()
     eng = api.Engine(p)
@@ -143,6 +151,62 @@ def run(config, events, warmup=1000, grid=None):
             "strain": s1["eps_avg"], "stopped": s1["stopped"]}
 
 
+def _ensemble_params(grid, seed, mixed, temperature, eng_rate, eng_end):
+    p = configs.shear64(seed, grid, eng_rate=eng_rate, eng_end=eng_end)
+    p.temperature = temperature
+    p.t_temp = 1 / (p.trial_frequency * math.exp(-0.37 / (temperature * 1.380658e-23 / 1.60217733e-19)))
+    if mixed:
+        p.precision = api.PREC_MIXED
+        p.solver = api.SOLVER_KERNEL
+    return p
+
+
+def ensemble(grid, seeds, max_steps=100000, temperature=250.0, eng_rate=1e-4, eng_end=0.06, chunk=10,
+             points=64):
+    """Ensemble-mean stress-strain curves of the mixed form and the FP64
+    plain form: shear loading at `eng_rate` (engineering) to `eng_end` or
+    `max_steps` driver steps, barrier seeds 0..seeds-1 (each seed runs in both
+    forms), sigma_xy and eps_xy sampled every `chunk` steps. At 250 K a curve
+    has an elastic rise (steps of 1e-4 strain while the total rate times the
+    step is below one), thermal yield and strain softening. Every run is
+    interpolated onto `points` strains from 0 to the smallest final strain of
+    all runs; the curves are the means over seeds. rel_diff_max: the largest
+    difference of the two mean curves over the plain curve's largest
+    magnitude."""
+    runs = {0: [], 1: []}
+    info = {}
+    for mixed in (1, 0):
+        t0 = time.perf_counter()
+        steps = events = ath = 0
+        for seed in range(seeds):
+            e = api.Engine(_ensemble_params(grid, seed, mixed, temperature, eng_rate, eng_end))
+            xs, ys = [0.0], [0.0]
+            while True:
+                e.run(max_steps=chunk)
+                s = e.scalars()
+                xs.append(s["eps_avg"][5])
+                ys.append(s["stress"][5])
+                if s["stopped"] or s["step"] >= max_steps:
+                    break
+            steps += s["step"]
+            events += s["kstep"]
+            ath += s["astep"]
+            e.close()
+            runs[mixed].append((np.array(xs), np.array(ys)))
+        info["mixed" if mixed else "plain"] = {"steps": steps, "thermal_events": events, "athermal_steps": ath,
+                                               "wall_s": time.perf_counter() - t0}
+    top = min(x[-1] for r in runs.values() for x, _ in r)
+    grid_x = np.linspace(0.0, top, points)
+    mean = {k: np.mean([np.interp(grid_x, x, y) for x, y in r], axis=0) for k, r in runs.items()}
+    scale = float(np.abs(mean[0]).max())
+    diff = np.abs(mean[1] - mean[0])
+    return {"grid": grid, "seeds": seeds, "temperature_K": temperature, "eng_rate": eng_rate, "eng_end": eng_end,
+            "strain_xy_max": float(top), "rel_diff_max": float(diff.max() / scale) if scale > 0 else None,
+            "rel_diff_mean": float(diff.mean() / scale) if scale > 0 else None,
+            "peak_stress_plain": scale, "forms": info,
+            "curve": {"eps_xy": grid_x[::8].tolist(), "plain": mean[0][::8].tolist(), "mixed": mean[1][::8].tolist()}}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m metallic_glasses_gb300.timing")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -160,6 +224,11 @@ def main(argv=None):
     b.add_argument("--replicas", type=int, default=256)
     b.add_argument("--events", type=int, default=32)
     b.add_argument("--alone", type=int, default=None)
+    en = sub.add_parser("ensemble")
+    en.add_argument("--grid", type=int, default=32)
+    en.add_argument("--seeds", type=int, default=8)
+    en.add_argument("--max-steps", type=int, default=100000)
+    en.add_argument("--temperature", type=float, default=250.0)
     r = sub.add_parser("run")
     r.add_argument("--config", choices=sorted(RUN_CONFIGS), default="grf256")
     r.add_argument("--events", type=int, default=20000)
@@ -172,6 +241,8 @@ def main(argv=None):
         out = solve(a.grid, a.reps, fp64=a.fp64, profile_range=a.profile_range)
     elif a.cmd == "run":
         out = run(a.config, a.events, a.warmup, a.grid)
+    elif a.cmd == "ensemble":
+        out = ensemble(a.grid, a.seeds, a.max_steps, a.temperature)
     else:
         out = batch(a.replicas, a.events, a.alone)
     print(json.dumps(out), flush=True)

@@ -136,6 +136,41 @@ def test_global3d_plain_matches_oracle(engine_lib, oracle_lib, cfg, events):
     assert rel_err(eng.field(api.FIELD_DF), ora.field(api.FIELD_DF)) < 1e-15
 
 
+def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib):
+    """The 32^3 stress-controlled configuration (1 GPa of shear, seed 0): the
+    plain FP64 form takes the oracle's (step, kind, site, mode) sequence for the
+    first 10^4 events, at its times, and ends with its stress and eigenstrain
+    fields within 1e-10 of their size."""
+    p = configs.stress32()
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(p)
+    eng.run(max_events=10000)
+    ora.run(max_events=10000)
+    a, b = eng.events(), ora.events()
+    assert len(a) == len(b) and (a["kind"] == api.EV_THERMAL).sum() == 10000
+    for k in ("step", "kind", "site", "mode"):
+        bad = np.nonzero(a[k] != b[k])[0]
+        assert bad.size == 0, "first mismatch in %s at %d" % (k, bad[0])
+    assert np.abs(a["time"] - b["time"]).max() <= FIELD_RTOL * np.abs(b["time"]).max()
+    for c in range(6):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), ora.field(api.FIELD_SIGMA, c)) < FIELD_RTOL
+        assert rel_err(eng.field(api.FIELD_EPS0, c), ora.field(api.FIELD_EPS0, c)) < FIELD_RTOL
+    eng.close()
+    ora.close()
+
+
+def test_ensemble_stress_strain_curves_agree():
+    """Ensemble-mean stress-strain curves of the mixed form and the FP64 plain
+    form (shear loading at 250 K to 3 % shear strain through the elastic rise,
+    thermal yield and softening; 16^3, seeds 0..5, the same seeds in both
+    forms) within 1 % of the plain curve's peak."""
+    from metallic_glasses_gb300 import timing
+    out = timing.ensemble(16, 6)
+    assert out["strain_xy_max"] > 0.029
+    assert out["forms"]["plain"]["thermal_events"] > 1000
+    assert out["rel_diff_max"] < 0.01, out["rel_diff_max"]
+
+
 def test_correlated_barrier_field_matches_oracle(engine_lib, oracle_lib):
     p = configs.grf256(n=16)
     p.precision = api.PREC_FP64
