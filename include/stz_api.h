@@ -304,17 +304,19 @@ int stz_flush_l2(stz_ctx* ctx);                      /* writes a buffer larger t
 int64_t stz_kernel_launches(stz_ctx* ctx);           /* kernels launched by this ctx so far */
 /* Bytes copied host->device and device->host by this ctx so far. */
 int stz_transfer_bytes(stz_ctx* ctx, int64_t* h2d, int64_t* d2h);
-/* Mixed form: average device-clock time per event of the stress update + rate
- * phase (all blocks) and of the selection/commit tail (one block), since the
- * context was created. */
+/* Mixed form: average device-clock time per event from the start of the
+ * stress-update/rate pass to the start of the selection tail (the pass and the
+ * plane sums), and of the tail (total rate, search, commit; one block), since
+ * the context was created. */
 int stz_phase_times(stz_ctx* ctx, double* main_us, double* tail_us, int64_t* n);
 /* sizeof the ABI structs, for bindings: 0 stz_params, 1 stz_event, 2 stz_scalars */
 int64_t stz_sizeof(int32_t which);
 /* Mixed form, timed with CUDA events on the ctx stream over *launches events
  * launched one by one: which = 0 the grid-wide stress-update/rate kernel,
- * 2 the whole event (that kernel and the one-block selection/commit kernel),
- * 1 the update-only variant (the stress-field streaming floor). Returns the
- * average ms; *launches receives the number of events timed. */
+ * 2 the whole event (that kernel and the selection kernel: one block per plane
+ * for the plane sums, the last of them running the tail), 1 the update-only
+ * variant (the stress-field streaming floor). Returns the average ms;
+ * *launches receives the number of events timed. */
 int stz_kernel_time(stz_ctx* ctx, int32_t which, double* ms_avg, int64_t* launches);
 
 #ifdef __cplusplus
