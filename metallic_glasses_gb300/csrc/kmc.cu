@@ -1233,6 +1233,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// L2 prefetch of a contiguous run (16-byte aligned, a multiple of 16 bytes)
+// by the bulk-copy unit; no completion to wait for.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_u32(dst)),
@@ -1503,6 +1508,15 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   // The next line is found before the line's first piece; between the pieces
   // of a line the rate sums wait in shared memory (the registers are at the
   // three-block limit).
+  // Response tables larger than a share of L2 (grids above ~190^3) come from
+  // HBM: warps 0 and 2, whose lines take the unit's two table rows (d0, 2c)
+  // and (d0, 2c + 1) and are valid whenever the row exists, prefetch the rows
+  // of their next unit into L2 (8 KB each, one bulk prefetch) a line ahead.
+  // (compiled into the passes that meet such grids: 256-site lines and the
+  // general pass)
+  constexpr bool kRowPrefetch = !UPDATE_ONLY && (N2 == 0 || N2 == 256);
+  const bool pf_rows = kRowPrefetch && (w == 0 || w == 2) &&
+                       (long long)(k.n0 / 2 + 1) * k.kt1 * k.kt2 * 64 > (48ll << 20);
   int u = b;
   LineOf L{0, 0, 0};
   for (; u < k.mx_units; u += k.nblk)
@@ -1527,9 +1541,16 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
       float* nxt = stages + ((j + 1) & 1) * sf;
       __syncwarp();
       if (!last || un < k.mx_units) {
-        if (lane == 0)
+        if (lane == 0) {
           issue_line<UPDATE_ONLY>(k, last ? Ln.i0 : L.i0, last ? Ln.i1 : L.i1, last ? 0 : (h + 1) * plen, plen, nxt,
                                   &bar[(j + 1) & 1]);
+          if (kRowPrefetch && pf_rows && last) {
+            const int d0 = (int)__umulhi((unsigned)un, k.c1_magic);
+            const int d1 = 2 * (un - d0 * k.mx_c1) + ((w >> 1) & 1);
+            bulk_prefetch_l2(reinterpret_cast<const float4*>(k.ktab) + 4LL * ((d0 * k.kt1 + d1) * k.kt2),
+                             (unsigned)k.kt2 * 64u);
+          }
+        }
         pending |= 1u << ((j + 1) & 1);
         ppar = (ppar & ~(1u << ((j + 1) & 1))) | ((((unsigned)(j + 1) >> 1) & 1u) << ((j + 1) & 1));
       }
@@ -1802,7 +1823,7 @@ __device__ __forceinline__ int chunk_find(const long long* v, long long E, long 
 // the site (or -1) in every lane, the distance of the target from the nearer
 // edge of the chosen site's interval in *margin and the chosen (site, mode)'s
 // scaled log2-rate argument (the chain of mx_x) in *x_sel.
-constexpr int kLaneChunk = 16;  // lines or sites per lane: n1, n2 <= 512
+constexpr int kLaneChunk = 20;  // plane sums per thread held in registers: 20 n0 <= 20 TH, n0 <= 256
 // KL: the lines or sites a lane holds (n1, n2 <= 32 KL)
 template <int KL>
 __device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
