@@ -9,8 +9,9 @@ roofline of the per-event kernel, the end-to-end figure through the C ABI
 with host-side event and scalar reads, the CPU oracle timed on the host, the
 batched replicas against the same replicas one at a time, the 256^3
 correlated-barrier run (event rate and stress error), the ensemble-mean
-stress-strain curves of the mixed and the plain form on the same seeds, and
-the FP64 plain form at 64^3 next to the CPU oracle on that grid.
+stress-strain curves of the mixed and the plain form on the same seeds, the
+FP64 plain form at 64^3 next to the CPU oracle on that grid, and the
+reference's own 2D model at its shipped 512 x 512 grid next to the oracle.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -107,12 +108,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(seconds=15.0, grid=GRID, threads=None):
+def cpu_baseline(seconds=15.0, grid=GRID, threads=None, params=None, what=None):
     """The CPU oracle (FP64, the reference's full re-solve per event) on all
-    host threads (or `threads`), on a bounded sample of the same workload."""
+    host threads (or `threads`), on a bounded sample of the same workload
+    (the 3D shear configuration at grid^3, or `params`)."""
     from metallic_glasses_gb300 import configs
     from oracle import pyoracle
-    p = configs.plain128(n=grid)
+    p = configs.plain128(n=grid) if params is None else params
     m = pyoracle.Model(p)
     all_threads = pyoracle.threads()
     if threads:
@@ -128,9 +130,9 @@ def cpu_baseline(seconds=15.0, grid=GRID, threads=None):
         cores = pyoracle.threads()
     finally:
         pyoracle.set_threads(all_threads)
+    what = what or "the %d^3 FP64 shear configuration (seed 0)" % grid
     return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d thermal events of the %d^3 FP64 shear configuration (seed 0) after setup, %.1f s" %
-                      (n, grid, dt)}
+            "sample": "%d thermal events of %s after setup, %.1f s" % (n, what, dt)}
 
 
 def reduce_ranks(ms, events, dist=None):
@@ -178,6 +180,7 @@ def main():
     ap.add_argument("--grf-events", type=int, default=20000)
     ap.add_argument("--no-ensemble", action="store_true", help="skip the stress-strain ensemble of both forms")
     ap.add_argument("--no-plain64", action="store_true", help="skip the 64^3 FP64 plain run and its CPU oracle")
+    ap.add_argument("--no-ref2d", action="store_true", help="skip the reference's 2D model at 512^2")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -341,6 +344,20 @@ def main():
         pl["workload"] = ("64^3 FP64 plain form, shear strain rate 5e-5 /s, T = 455 K, seed 0, 2000 thermal "
                           "events after 100 warm-up events, every event a full FP64 re-solve")
         line["plain64"] = pl
+    if not args.no_ref2d:
+        # the reference's own 2D model at its shipped 512 x 512 grid and input
+        # (FP64 plain form, the reference's method), next to the CPU oracle
+        from metallic_glasses_gb300 import configs, timing
+        r2 = timing.run("ref2d512", events=2000, warmup=100)
+        r2 = {k: r2[k] for k in ("grid", "sites", "events", "athermal_steps", "ms", "events_per_s", "us_per_event")}
+        if not args.no_cpu:
+            r2["cpu_baseline"] = cpu_baseline(seconds=8.0, params=configs.ref2d(512, 512),
+                                              what="the reference's 2D model at 512 x 512 (shipped input)")
+            r2["gpu_over_cpu"] = r2["events_per_s"] / r2["cpu_baseline"]["value"]
+        r2["workload"] = ("the reference's 2D model (per-site barriers and eigenstrains re-drawn after each "
+                          "transformation, softening on) at its shipped 512 x 512 grid and input file, TENSION, "
+                          "2000 thermal events after 100 warm-up events, every event a full FP64 re-solve")
+        line["ref2d512"] = r2
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
         line["cpu_baseline_1core"] = cpu_baseline(seconds=8.0, grid=n, threads=1)

@@ -116,7 +116,9 @@ def batch(replicas, events, alone=None, seed0=0):
             "alone_sample": n1}
 
 
-RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128, "plain64": configs.plain128}
+RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128, "plain64": configs.plain128,
+               # the reference's own 2D model at its shipped grid and input
+               "ref2d512": lambda: configs.ref2d(512, 512)}
 
 
 def run(config, events, warmup=1000, grid=None):
