@@ -591,7 +591,17 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
     kp.nblk = (int)std::max(1LL, nb);
     kp.bsites = 0;
   } else {
-    kp.bsites = kRateThreads * kSptFp64;
+    // sites per thread: kSptFp64 while that still gives four blocks per SM,
+    // fewer on smaller grids (a 512^2 grid at four per thread is 256 blocks,
+    // under two per SM, and the FP64 rate pass needs the warps to cover its
+    // latencies)
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device);
+    int spt = kSptFp64;
+    while (spt > 1 && (kp.N + (long long)kRateThreads * spt - 1) / ((long long)kRateThreads * spt) <
+                          4LL * std::max(sms, 1))
+      spt >>= 1;
+    kp.bsites = kRateThreads * spt;
     kp.nblk = (int)((kp.N + kp.bsites - 1) / kp.bsites);
   }
   kp.ngroups = (kp.nblk + kGroup - 1) / kGroup;

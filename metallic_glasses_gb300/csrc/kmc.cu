@@ -327,7 +327,12 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
     d.pd[c] = f.prev_deps[c * N + s];
   }
   d.n2 = sqrt(d.pd[0] * d.pd[0] + d.pd[1] * d.pd[1] + 2 * d.pd[2] * d.pd[2]);
-  d.soft = kp.softening ? f.perm_soft[s] + f.temp_soft[s] * exp((f.tlast[s] - totime) / kp.t_temp) : 0.0;
+  // a site without temporary softening skips the decay's exponential: its
+  // term is 0 times a finite positive factor, +0 exactly
+  const double ts = kp.softening ? f.temp_soft[s] : 0.0;
+  d.soft = kp.softening ? (ts != 0.0 ? f.perm_soft[s] + ts * exp((f.tlast[s] - totime) / kp.t_temp)
+                                     : f.perm_soft[s])
+                        : 0.0;
   return d;
 }
 
@@ -337,6 +342,11 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
   const double* dd = f.deps + (long long)m * 3 * N;
   const double d0 = dd[s], d1 = dd[N + s], d2 = dd[2 * N + s];
   const double DWork = (d.sg[0] * d0 + d.sg[1] * d1 + 2 * d.sg[2] * d2) * kp.V0 * 1e-18 * kJInEv;
+  // an unsoftened site (every site before its first transformation): the
+  // direction modifier is finite (its norms carry kEpsilon), so the factor
+  // exp(-DM * 0) is exactly 1 and the barrier is Q0 - W/2 to the bit; the
+  // square root, two divisions and an exponential per mode are skipped
+  if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
   const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
   const double n1 = sqrt(d0 * d0 + d1 * d1 + 2 * d2 * d2);
   const double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
