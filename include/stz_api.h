@@ -309,6 +309,14 @@ int stz_transfer_bytes(stz_ctx* ctx, int64_t* h2d, int64_t* d2h);
  * plane sums), and of the tail (total rate, search, commit; one block), since
  * the context was created. */
 int stz_phase_times(stz_ctx* ctx, double* main_us, double* tail_us, int64_t* n);
+/* Self-test of the kernels' bounded device waits, without a fault: one block
+ * waits with `tries` attempts on a barrier armed for bytes that never arrive,
+ * as the per-event pass waits on its staged lines, and gives up.
+ * *status = STZ_ERR_TIMEOUT when the wait ran out (the expected result),
+ * *ms = the kernel's duration, *kernel_tries = the limit the per-event kernels
+ * use (their wait lasts about ms * kernel_tries / tries). The device stays
+ * usable afterwards. */
+int stz_selftest_wait(int32_t device, int32_t tries, int32_t* status, double* ms, int32_t* kernel_tries);
 /* sizeof the ABI structs, for bindings: 0 stz_params, 1 stz_event, 2 stz_scalars */
 int64_t stz_sizeof(int32_t which);
 /* Mixed form, timed with CUDA events on the ctx stream over *launches events

@@ -97,6 +97,8 @@ def load_library(path=None):
     lib.stz_elastic_energy.argtypes = [vp, C.POINTER(C.c_double)]
     lib.stz_sync.argtypes = [vp]
     lib.stz_timer_start.argtypes = [vp]
+    lib.stz_selftest_wait.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int32)]
     lib.stz_timer_stop.argtypes = [vp, C.POINTER(C.c_float)]
     lib.stz_flush_l2.argtypes = [vp]
     lib.stz_kernel_launches.argtypes = [vp]
@@ -276,6 +278,15 @@ class Engine:
         n = C.c_int64(steps)
         _check(self.lib.stz_kernel_time(self.h, which, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+
+def selftest_wait(tries, device=0):
+    """Run the bounded-wait self-test (stz_selftest_wait): returns (status,
+    ms, kernel_tries); status is STZ_ERR_TIMEOUT when the wait ran out."""
+    lib = load_library()
+    st, ms, km = C.c_int32(), C.c_double(), C.c_int32()
+    _check(lib.stz_selftest_wait(device, tries, C.byref(st), C.byref(ms), C.byref(km)))
+    return st.value, ms.value, km.value
 
 
 class Batch:

@@ -1130,6 +1130,37 @@ extern "C" int stz_flush_l2(stz_ctx* c) {
 
 extern "C" int64_t stz_kernel_launches(stz_ctx* c) { return c ? c->launches : 0; }
 
+extern "C" int stz_selftest_wait(int32_t device, int32_t tries, int32_t* status, double* ms, int32_t* kernel_tries) {
+  if (!status || tries < 1) return STZ_ERR_INVALID;
+  CK(cudaSetDevice(device));
+  int* d = nullptr;
+  int st;
+  if ((st = dalloc(&d, 1))) return st;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int kmax = 0;
+  CK(cudaEventRecord(e0, 0));
+  if (wait_selftest(tries, d, &kmax, 0)) {
+    cudaFree(d);
+    set_error("wait self-test launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return STZ_ERR_CUDA;
+  }
+  CK(cudaEventRecord(e1, 0));
+  CK(cudaEventSynchronize(e1));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  int h = -1;
+  CK(cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost));
+  cudaFree(d);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *status = h;
+  if (ms) *ms = t;
+  if (kernel_tries) *kernel_tries = kmax;
+  return STZ_OK;
+}
+
 extern "C" int stz_phase_times(stz_ctx* c, double* main_us, double* tail_us, int64_t* n) {
   if (!c) return STZ_ERR_INVALID;
   int st = sync_ctl(c);

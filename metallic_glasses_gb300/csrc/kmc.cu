@@ -1235,13 +1235,30 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
       : "memory");
   return ok != 0;
 }
-// Bounded wait (each try_wait suspends for a hardware-chosen interval); false
-// after kMbarTries attempts.
-constexpr int kMbarTries = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-  for (int it = 0; it < kMbarTries; it++)
+// Bounded wait (each try_wait suspends for a hardware-chosen interval, about
+// 4 us on GB300); false after `tries` attempts. kMbarTries, the kernels'
+// limit, is about a second: a staged line lands within microseconds.
+constexpr int kMbarTries = 1 << 18;
+__device__ __forceinline__ bool mbar_wait_n(unsigned long long* bar, unsigned parity, int tries) {
+  for (int it = 0; it < tries; it++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  return mbar_wait_n(bar, parity, kMbarTries);
+}
+
+// Self-test of the bounded wait: thread 0 arms an mbarrier for 16 bytes that
+// no copy will deliver and waits on it with `tries` attempts, as the main
+// pass waits on its staged lines; the wait runs out and the status says so.
+// Nothing is in flight on the barrier, so the block may leave at once.
+__global__ void k_wait_selftest(int tries, int* out) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_expect_tx(&bar, 16u);
+  *out = mbar_wait_n(&bar, 0u, tries) ? STZ_OK : STZ_ERR_TIMEOUT;
 }
 // L2 prefetch of a contiguous run (16-byte aligned, a multiple of 16 bytes)
 // by the bulk-copy unit; no completion to wait for.
@@ -2559,6 +2576,12 @@ void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cuda
 void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
   else launch_pdl(k_mixed_select, dim3(kp.n0), 0, st, kp, f);
+}
+
+int wait_selftest(int tries, int* status_dev, int* kmax, cudaStream_t st) {
+  *kmax = kMbarTries;
+  k_wait_selftest<<<1, 32, 0, st>>>(tries, status_dev);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
 void launch_mixed(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
