@@ -319,9 +319,6 @@ int solve_dev(stz_ctx* c, const double* ebar, const double* uadd, double* err) {
   return fft_solve(*plan_of(c), a, c->stream, &c->launches);
 }
 
-double* ctl_field(stz_ctx* c, size_t offset) {
-  return reinterpret_cast<double*>(reinterpret_cast<char*>(c->f.ctl) + offset);
-}
 
 // The response of one voxel: five FP64 solves with a unit deviatoric
 // eigenstrain at the origin, projected on the deviatoric basis.
