@@ -71,3 +71,28 @@ def test_stress_control_holds_applied_stress(oracle_lib, engine_lib):
     assert all(abs(sc["stress"][c]) < 1e-12 for c in range(5))
     sig = np.stack([m.field(api.FIELD_SIGMA, c) for c in range(6)])
     assert abs(sig[api.XY].mean() - 1.0) < 1e-10
+
+
+def test_ensemble_curve_machinery(oracle_lib, monkeypatch):
+    """The stress-strain ensemble comparison (timing.ensemble) on CPU, with the
+    FP64 oracle standing in for both forms: identical runs give identical
+    curves, and the curves start at the origin with the elastic slope
+    sigma_xy = 2 mu eps_xy (tensor shear strain) before the first events."""
+    from metallic_glasses_gb300 import timing
+
+    class Oracle(oracle_lib.Model):
+        def __init__(self, p):
+            p.precision = api.PREC_FP64
+            p.solver = api.SOLVER_FFT
+            super().__init__(p)
+
+    monkeypatch.setattr(api, "Engine", Oracle)
+    out = timing.ensemble(8, 2, max_steps=400, eng_end=0.02)
+    assert out["rel_diff_max"] == 0.0
+    for k in ("steps", "thermal_events", "athermal_steps"):
+        assert out["forms"]["mixed"][k] == out["forms"]["plain"][k]
+    assert out["forms"]["plain"]["steps"] > 0
+    eps, sig = np.array(out["curve"]["eps_xy"]), np.array(out["curve"]["plain"])
+    assert eps[0] == 0.0 and sig[0] == 0.0 and out["strain_xy_max"] > 0.005
+    mu = timing._ensemble_params(8, 0, 0, 250.0, 1e-4, 0.02).mu
+    assert abs(sig[1] / eps[1] - 2 * mu) < 1e-6 * 2 * mu
