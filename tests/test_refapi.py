@@ -21,11 +21,11 @@ import pytest
 
 from conftest import ROOT, golden
 from metallic_glasses_gb300 import build, configs
+from oracle.build_oracle import REF_DIR  # the reference tree, where present
 
 REFAPI = os.path.join(ROOT, "metallic_glasses_gb300", "refapi", "refapi.c")
 TESTHDR = os.path.join(ROOT, "tests", "refapi")
 SHIM = os.path.join(ROOT, "oracle", "shim")
-REF_DIR = "/root/reference/Mesoscale simulation STZ model"
 CFLAGS = ["-O2", "-std=gnu11", "-w"]
 
 
