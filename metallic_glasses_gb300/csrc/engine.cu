@@ -143,6 +143,8 @@ int init_ref2d(stz_ctx* c, MT* rng) {
   int st;
   if ((st = upload(c->f.Q0, Q0.data(), sizeof(double) * Q0.size(), c->stream))) return st;
   if ((st = upload(c->f.deps, deps.data(), sizeof(double) * deps.size(), c->stream))) return st;
+  launch_mode_norms(c->kp, c->f, c->stream);
+  CK(cudaGetLastError());
   std::vector<double> tl((size_t)N, -100 * p.t_temp);
   if ((st = upload(c->f.tlast, tl.data(), sizeof(double) * N, c->stream))) return st;
   CK(cudaStreamSynchronize(c->stream));
@@ -665,6 +667,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   if (ref2d) {
     if ((st = dalloc(&f.Q0, (size_t)STZ_MODES * N))) return fail(st);
     if ((st = dalloc(&f.deps, (size_t)STZ_MODES * 3 * N))) return fail(st);
+    if ((st = dalloc(&f.dnorm, (size_t)STZ_MODES * N))) return fail(st);
     if ((st = dalloc(&f.perm_soft, (size_t)N))) return fail(st);
     if ((st = dalloc(&f.temp_soft, (size_t)N))) return fail(st);
     if ((st = dalloc(&f.tlast, (size_t)N))) return fail(st);
@@ -734,7 +737,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   cudaSetDevice(c->p.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
-  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.prev_deps, f.perm_soft, f.temp_soft,
+  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.dnorm, f.prev_deps, f.perm_soft, f.temp_soft,
                   f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.psum, f.spec, f.ktab, f.log,
                   f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf, f.lam_site, f.mu_site,
                   f.inh_tau0, f.inh_eeff, f.inh_last, f.inh_part};
@@ -1061,6 +1064,7 @@ extern "C" int stz_set_field(stz_ctx* c, int32_t which, int32_t comp, const doub
   if (st) return st;
   CK(cudaMemcpyAsync(d64, host, sizeof(double) * c->kp.N, cudaMemcpyHostToDevice, c->stream));
   if (which == STZ_FIELD_DF && c->f.dF32) launch_fill_f32(c->f.dF, c->f.dF32, c->kp.N, c->stream);
+  if (which == STZ_FIELD_DEPS && c->f.dnorm) launch_mode_norms(c->kp, c->f, c->stream);
   CK(cudaStreamSynchronize(c->stream));
   return STZ_OK;
 }

@@ -336,6 +336,14 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
   return d;
 }
 
+// Norm of a 2D mode increment, sqrt(de_xx^2 + de_yy^2 + 2 de_xy^2)
+// (init.c:600-603), every operation rounded on its own as the reference's C
+// evaluates it. Stored per mode and site whenever the modes are drawn, so the
+// rate passes load it instead of taking a square root per mode.
+__device__ __forceinline__ double mode_norm(double d0, double d1, double d2) {
+  return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(__dmul_rn(2.0, d2), d2)));
+}
+
 // ActEnergy for one (mode, site) of the reference model (init.c:585-686)
 __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m) {
   const long long N = kp.N;
@@ -348,7 +356,7 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
   // square root, two divisions and an exponential per mode are skipped
   if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
   const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
-  const double n1 = sqrt(d0 * d0 + d1 * d1 + 2 * d2 * d2);
+  const double n1 = f.dnorm[(long long)m * N + s];
   const double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
   return f.Q0[(long long)m * N + s] * exp(-DM * d.soft) - DWork / 2;
 }
@@ -718,9 +726,11 @@ __device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, 
     for (int i = 0; i < STZ_MODES; i++) {
       double* dd = f.deps + (long long)i * 3 * N;
       const double a = 0.5 * kp.gamma0 * mt_gaussian(rng, 1.0);
+      const double c2 = 0.5 * kp.gamma0 * mt_gaussian(rng, 1.0);
       dd[s] = a;
       dd[N + s] = -a;
-      dd[2 * N + s] = 0.5 * kp.gamma0 * mt_gaussian(rng, 1.0);
+      dd[2 * N + s] = c2;
+      f.dnorm[(long long)i * N + s] = mode_norm(a, -a, c2);
     }
   }
 }
@@ -2576,6 +2586,23 @@ void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cuda
 void launch_mixed_tail(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   if (update_only) k_mixed_tail<<<1, TH, 0, st>>>(kp, f, update_only);
   else launch_pdl(k_mixed_select, dim3(kp.n0), 0, st, kp, f);
+}
+
+// The stored mode norms of every (mode, site) from the mode increments.
+__global__ void k_mode_norms(KParams kp, Fields f) {
+  const long long N = kp.N, total = (long long)STZ_MODES * N;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long m = i / N, s = i - m * N;
+    const double* dd = f.deps + m * 3 * N;
+    f.dnorm[i] = mode_norm(dd[s], dd[N + s], dd[2 * N + s]);
+  }
+}
+
+void launch_mode_norms(const KParams& kp, const Fields& f, cudaStream_t st) {
+  const long long total = (long long)STZ_MODES * kp.N;
+  const unsigned nb = (unsigned)std::min<long long>((total + TH - 1) / TH, 152LL * 16);
+  k_mode_norms<<<nb, TH, 0, st>>>(kp, f);
 }
 
 int wait_selftest(int tries, int* status_dev, int* kmax, cudaStream_t st) {

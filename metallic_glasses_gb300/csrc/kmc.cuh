@@ -41,6 +41,8 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
 int mixed_blocks_per_sm(int n2);
 // Dynamic shared memory of one mixed-form main block for lines of n2 sites.
 size_t mixed_smem(int n2);
+// the stored mode norms of the 2D model, after its mode increments were written
+void launch_mode_norms(const KParams& kp, const Fields& f, cudaStream_t st);
 // bounded-wait self-test kernel (one block); *kmax receives the kernels' limit
 int wait_selftest(int tries, int* status_dev, int* kmax, cudaStream_t st);
 // The two halves of launch_mixed: the grid-wide update/rate kernel and the

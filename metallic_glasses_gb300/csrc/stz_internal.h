@@ -104,6 +104,7 @@ struct Fields {
   float* dF32 = nullptr;     // [N] barrier (mixed form)
   double* Q0 = nullptr;      // [MODES][N] (REF2D)
   double* deps = nullptr;    // [MODES][3][N] (REF2D)
+  double* dnorm = nullptr;   // [MODES][N] |deps| of each mode (REF2D), kept with deps
   double* prev_deps = nullptr;  // [nc][N]
   double* perm_soft = nullptr;
   double* temp_soft = nullptr;
