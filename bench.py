@@ -305,7 +305,10 @@ def main():
             "stress_err": stress_err,
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
             "wall_s": t_wall}
-    if not args.no_batch:
+    # the single-GPU studies and the CPU baselines run at N = 1 only: under
+    # torchrun the other GPUs would idle while rank 0 runs them
+    single = world == 1
+    if single and not args.no_batch:
         # independent replicas of uneven sizes advanced together vs one at a time
         from metallic_glasses_gb300 import timing
         bt = timing.batch(args.batch_replicas, events=128)
@@ -315,7 +318,7 @@ def main():
                           % (args.batch_replicas, args.batch_replicas - 1))
         bt["ratio"] = bt["batched_events_per_s"] / bt["alone_events_per_s"]
         line["batched"] = bt
-    if not args.no_grf:
+    if single and not args.no_grf:
         # 256^3 with a correlated barrier field (Gaussian covariance, 4 voxels,
         # sd 0.15 eV), strain rate 5e-4 /s, autotuned FFT schedules
         from metallic_glasses_gb300 import timing
@@ -328,7 +331,7 @@ def main():
                           "length 4 voxels, shear strain rate 5e-4 /s, %d thermal events after 1000 warm-up "
                           "events, full re-solve (FP32 pairs) every 1000 events" % args.grf_events)
         line["grf256"] = gr
-    if not args.no_ensemble:
+    if single and not args.no_ensemble:
         # ensemble-mean stress-strain curves, mixed vs FP64 plain, same seeds
         from metallic_glasses_gb300 import timing
         en = timing.ensemble(n, 4, max_steps=600)
@@ -336,7 +339,7 @@ def main():
                           "(the elastic rise to about 0.25 GPa); rel_diff_max = largest difference of the "
                           "two mean curves over the plain curve's peak" % n)
         line["ensemble"] = en
-    if not args.no_plain64:
+    if single and not args.no_plain64:
         # the FP64 plain form at 64^3 (the reference's method: a full re-solve
         # per event) next to the CPU oracle on the same grid, in the same run
         from metallic_glasses_gb300 import timing
@@ -348,7 +351,7 @@ def main():
         pl["workload"] = ("64^3 FP64 plain form, shear strain rate 5e-5 /s, T = 455 K, seed 0, 2000 thermal "
                           "events after 100 warm-up events, every event a full FP64 re-solve")
         line["plain64"] = pl
-    if not args.no_ref2d:
+    if single and not args.no_ref2d:
         # the reference's own 2D model at its shipped 512 x 512 grid and input
         # (FP64 plain form, the reference's method), next to the CPU oracle
         from metallic_glasses_gb300 import configs, timing
@@ -362,7 +365,7 @@ def main():
                           "transformation, softening on) at its shipped 512 x 512 grid and input file, TENSION, "
                           "2000 thermal events after 100 warm-up events, every event a full FP64 re-solve")
         line["ref2d512"] = r2
-    if not args.no_cpu:
+    if single and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)
         line["cpu_baseline_1core"] = cpu_baseline(seconds=8.0, grid=n, threads=1)
     print(json.dumps(line), flush=True)
