@@ -58,3 +58,42 @@ def test_shear_instability_stop(oracle_lib, engine_lib):
     sc = m.scalars()
     assert sc["stopped"] == 2
     assert sc["step"] == int(g["hdr"][1])
+
+
+def test_oracle_matches_reference_at_512(oracle_lib, engine_lib):
+    """At the reference's own 512 x 512 grid on its shipped input, live: the
+    reference's sources built against the single-rank stand-ins and the oracle
+    take the same transformations and end with the same fields, bit for bit,
+    over 8 thermal events (only where the reference tree is present)."""
+    import os
+    import subprocess
+    import tempfile
+
+    from metallic_glasses_gb300 import configs
+    from oracle.build_oracle import build_ref2d, ref_available
+    if not ref_available():
+        pytest.skip("reference tree not present")
+    exe = build_ref2d(512, 512, "TENSION")
+    d = tempfile.mkdtemp(prefix="stz_ref512_")
+    configs.write_input(os.path.join(d, "input"))
+    env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS="8",
+               STZ_REF_DUMP=os.path.join(d, "dump.bin"))
+    subprocess.run([exe], cwd=d, env=env, stdout=subprocess.DEVNULL, check=True, timeout=300)
+    X = np.array([[int(v) for v in line.split()[1:5]] for line in open(os.path.join(d, "log.txt"))
+                  if line.startswith("X")], np.int64)
+    raw = open(os.path.join(d, "dump.bin"), "rb").read()
+    hdr = np.frombuffer(raw[:40], np.int64)
+    N = int(hdr[0])
+    arr = np.frombuffer(raw[96:], np.float64)
+    sigma, eps0 = arr[:3 * N].reshape(3, N), arr[3 * N:6 * N].reshape(3, N)
+    m = oracle_lib.Model(configs.ref2d(512, 512, input_path=os.path.join(d, "input")))
+    m.run(max_steps=int(hdr[1]))
+    ev = m.events()
+    tr = ev[ev["kind"] != api.EV_ELASTIC]
+    assert N == 512 * 512 and len(X) >= 8
+    assert np.array_equal(np.stack([tr["step"], tr["kind"], tr["site"], tr["mode"]], 1), X)
+    sc = m.scalars()
+    assert [sc["step"], sc["kstep"], sc["astep"], sc["estep"]] == [int(v) for v in hdr[1:]]
+    for c in range(3):
+        assert np.array_equal(m.field(api.FIELD_SIGMA, c), sigma[c])
+        assert np.array_equal(m.field(api.FIELD_EPS0, c), eps0[c])
