@@ -171,6 +171,28 @@ def test_ensemble_stress_strain_curves_agree():
     assert out["rel_diff_max"] < 0.01, out["rel_diff_max"]
 
 
+def test_ref2d_512_matches_oracle(engine_lib, oracle_lib):
+    """The reference's 2D model at its own 512 x 512 grid on its shipped input
+    (softening on): the engine takes the oracle's transformations (the oracle
+    is pinned to the reference's code at this grid) for 30 thermal events,
+    with the clock and fields within 1e-10."""
+    p = configs.ref2d(512, 512)
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(configs.ref2d(512, 512))
+    eng.run(max_events=30)
+    ora.run(max_events=30)
+    a, b = eng.events(), ora.events()
+    assert len(a) == len(b) and (a["kind"] == api.EV_THERMAL).sum() == 30
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.abs(a["time"] - b["time"]).max() <= FIELD_RTOL * np.abs(b["time"]).max()
+    for c in range(3):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), ora.field(api.FIELD_SIGMA, c)) < FIELD_RTOL
+        assert rel_err(eng.field(api.FIELD_EPS0, c), ora.field(api.FIELD_EPS0, c)) < FIELD_RTOL
+    eng.close()
+    ora.close()
+
+
 def test_correlated_barrier_field_matches_oracle(engine_lib, oracle_lib):
     p = configs.grf256(n=16)
     p.precision = api.PREC_FP64
