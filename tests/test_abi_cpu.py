@@ -61,3 +61,22 @@ def test_bad_input_reports_io_error(engine_lib, tmp_path):
     assert ei.value.code == api.ERR_IO
     with pytest.raises(api.StzError):
         api.params_from_input(str(tmp_path / "missing"))
+
+
+def test_missing_engine_library_fails_loudly(tmp_path):
+    """Without its CUDA library the package raises instead of running any
+    other implementation."""
+    from metallic_glasses_gb300 import api
+    with pytest.raises(RuntimeError, match="not built"):
+        api.load_library(str(tmp_path / "libstz_gb300.so"))
+
+
+def test_no_device_reports_an_error_status(engine_lib):
+    """Creating a context where no GPU answers (this CPU host) returns an error
+    status from the C ABI, not a host fallback."""
+    from metallic_glasses_gb300 import api, configs
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(api.StzError):
+        api.Engine(configs.ref2d(16, 16))
