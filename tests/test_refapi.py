@@ -119,3 +119,23 @@ def test_driver_reproduces_reference_events(engine_lib):
     assert iout.shape == ref_io.shape
     assert np.abs(iout[:, 0] - ref_io[:, 0]).max() <= 1e-12 * np.abs(ref_io[:, 0]).max()
     assert np.abs(iout[:, 1] - ref_io[:, 1]).max() <= 1e-9 * np.abs(ref_io[:, 1]).max()
+
+
+def test_iout_records_are_the_raw_fields(engine_lib):
+    """WriteScalarMPI / WriteScalarMPI_INT write "<name>_S<step>.iout" with the
+    raw native values of the whole field in site order (one rank holds the
+    grid): the bytes a single-rank reference run writes (CPU, no device)."""
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "iout_check")
+        cmd = (["gcc", *CFLAGS, "-DREFAPI_NX=8", "-DREFAPI_NY=6", "-I", TESTHDR, "-I", SHIM,
+                "-I", os.path.join(ROOT, "include"), os.path.join(TESTHDR, "iout_check.c"), REFAPI] + _support() +
+               ["-o", exe] + _lib_args())
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr[-2000:]
+        s = np.arange(48)
+        f = np.fromfile(os.path.join(d, "Stress_02_S012.iout"), dtype=np.float64)
+        assert np.array_equal(f, 0.25 * s - 3.0)
+        g = np.fromfile(os.path.join(d, "Map_S003.iout"), dtype=np.int32)
+        assert np.array_equal(g, 7 * s - 11)
