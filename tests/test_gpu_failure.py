@@ -28,3 +28,22 @@ def test_bounded_wait_reports_timeout_and_device_stays_usable(engine_lib):
     sc = e.scalars()
     assert sc["kstep"] == 20 and sc["status"] == 0
     e.close()
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_nan_in_a_host_staged_field_is_reported(engine_lib, mixed):
+    """A NaN written into one site's barrier through the C ABI (a fault made on
+    the host): the next step stops with STZ_ERR_NAN in the returned status and
+    in the scalars, in the FP64 plain form and in the mixed form."""
+    import numpy as np
+    p = configs.mixed128(n=16, resolve_period=100) if mixed else configs.shear64(seed=1, n=16)
+    e = api.Engine(p)
+    e.run(max_events=5)
+    dF = e.field(api.FIELD_DF)
+    dF[123] = np.nan
+    e.set_field(api.FIELD_DF, 0, dF)
+    with pytest.raises(api.StzError) as ei:
+        e.run(max_events=5)
+    assert ei.value.code == api.ERR_NAN
+    assert e.scalars()["status"] == api.ERR_NAN
+    e.close()
