@@ -1860,7 +1860,7 @@ __device__ __forceinline__ int chunk_find(const long long* v, long long E, long 
 // the site (or -1) in every lane, the distance of the target from the nearer
 // edge of the chosen site's interval in *margin and the chosen (site, mode)'s
 // scaled log2-rate argument (the chain of mx_x) in *x_sel.
-constexpr int kLaneChunk = 20;  // plane sums per thread held in registers: 20 n0 <= 20 TH, n0 <= 256
+constexpr int kLaneChunk = 20;  // plane sums per thread held in registers (20 n0 over TH threads: n0 <= 256)
 // KL: the lines or sites a lane holds (n1, n2 <= 32 KL)
 template <int KL>
 __device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
