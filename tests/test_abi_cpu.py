@@ -80,3 +80,13 @@ def test_no_device_reports_an_error_status(engine_lib):
         pytest.skip("a GPU is present")
     with pytest.raises(api.StzError):
         api.Engine(configs.ref2d(16, 16))
+
+
+@pytest.mark.parametrize("cmd", ["kernel", "solve", "batch", "run", "ensemble"])
+def test_timing_commands_parse(cmd):
+    """Every documented timing subcommand parses its options."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-m", "metallic_glasses_gb300.timing", cmd, "--help"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "usage" in r.stdout, r.stderr[-1000:]
