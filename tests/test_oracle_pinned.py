@@ -60,11 +60,13 @@ def test_shear_instability_stop(oracle_lib, engine_lib):
     assert sc["step"] == int(g["hdr"][1])
 
 
-def test_oracle_matches_reference_at_512(oracle_lib, engine_lib):
-    """At the reference's own 512 x 512 grid on its shipped input, live: the
-    reference's sources built against the single-rank stand-ins and the oracle
-    take the same transformations and end with the same fields, bit for bit,
-    over 8 thermal events (only where the reference tree is present)."""
+@pytest.mark.parametrize("loading", ["TENSION", "SHEAR"])
+def test_oracle_matches_reference_at_512(oracle_lib, engine_lib, loading):
+    """At the reference's own 512 x 512 grid on its shipped input, live, under
+    both loading switches: the reference's sources built against the
+    single-rank stand-ins and the oracle take the same transformations and end
+    with the same fields, bit for bit, over 8 thermal events (only where the
+    reference tree is present)."""
     import os
     import subprocess
     import tempfile
@@ -73,7 +75,7 @@ def test_oracle_matches_reference_at_512(oracle_lib, engine_lib):
     from oracle.build_oracle import build_ref2d, ref_available
     if not ref_available():
         pytest.skip("reference tree not present")
-    exe = build_ref2d(512, 512, "TENSION")
+    exe = build_ref2d(512, 512, loading)
     d = tempfile.mkdtemp(prefix="stz_ref512_")
     configs.write_input(os.path.join(d, "input"))
     env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS="8",
@@ -86,7 +88,8 @@ def test_oracle_matches_reference_at_512(oracle_lib, engine_lib):
     N = int(hdr[0])
     arr = np.frombuffer(raw[96:], np.float64)
     sigma, eps0 = arr[:3 * N].reshape(3, N), arr[3 * N:6 * N].reshape(3, N)
-    m = oracle_lib.Model(configs.ref2d(512, 512, input_path=os.path.join(d, "input")))
+    lc = api.LOAD_TENSION if loading == "TENSION" else api.LOAD_SHEAR
+    m = oracle_lib.Model(configs.ref2d(512, 512, input_path=os.path.join(d, "input"), loading=lc))
     m.run(max_steps=int(hdr[1]))
     ev = m.events()
     tr = ev[ev["kind"] != api.EV_ELASTIC]
