@@ -259,7 +259,8 @@ int stz_solve(stz_ctx* ctx);
 
 /* The same solve without any device allocation, for callers that cannot call
  * cudaMalloc (code running inside another framework's memory pool or budget,
- * or inside a region recorded for replay). No counterpart in the reference.
+ * or in a process whose allocator someone else owns). No counterpart in the
+ * reference.
  * The caller passes device buffers eps0_dev [nc][N] and sigma_dev [nc][N]
  * (nc = 3 for dim 2 with n0 == 1, 6 for dim 3), the mean strain eps_avg
  * (nc host doubles) and a cudaStream_t (or NULL); sigma = C:(eps - eps*)
@@ -268,7 +269,9 @@ int stz_solve(stz_ctx* ctx);
  * components of 64^3 (2D up to 512^2); larger grids return STZ_ERR_INVALID.
  * The first call on a device looks up the array's device address; make that
  * first call before any stream capture. All calls share the array: calls
- * that overlap on the GPU race. Synchronises the stream before returning. */
+ * that overlap on the GPU race. Each call copies its twiddle tables and the
+ * mean strain from host memory to the array and synchronises the stream
+ * before returning. */
 int stz_solve_noalloc(int32_t dim, int32_t n0, int32_t n1, int32_t n2, double lambda, double mu,
                       const double* eps0_dev, const double* eps_avg, double* sigma_dev, void* stream);
 

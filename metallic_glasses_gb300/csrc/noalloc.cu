@@ -3,14 +3,15 @@
 //
 // Some callers run where allocating device memory is not allowed or not
 // possible: code that executes inside another framework's memory budget or
-// pool, inside a region recorded for replay where an allocation would be
-// recorded too, or in a process whose allocator is owned by someone else.
-// They still own their input and output buffers. This entry point performs
+// pool, or in a process whose allocator is owned by someone else. They still
+// own their input and output buffers. This entry point performs
 // the same solve as stz_solve (the reference's HomogeneousStressSolver with
 // uflag 0) on buffers the caller passes, and keeps its scratch -- the half
 // spectrum, the twiddle tables and the mean strain -- in one file-scope
 // device array of fixed size. Every GPU that loads this library holds that
-// array (about 13 MB) until the process exits.
+// array (about 13 MB) until the process exits. Each call uploads its twiddle
+// tables and the mean strain from host memory and synchronises the stream
+// before it returns.
 #include <cstdio>
 #include <cstring>
 
@@ -82,7 +83,10 @@ extern "C" int stz_solve_noalloc(int32_t dim, int32_t n0, int32_t n1, int32_t n2
   double2* extra = base + kNoAllocSpec;
   stz::FFTPlan plan;
   if ((st = stz::fft_plan_init_in(&plan, n0, n1, n2, nc, extra, kNoAllocExtra - 8, s))) {
-    stz::set_error("stz_solve_noalloc: grid %dx%dx%d not supported by the FFT", n0, n1, n2);
+    if (st == STZ_ERR_INVALID)
+      stz::set_error("stz_solve_noalloc: grid %dx%dx%d not supported by the FFT", n0, n1, n2);
+    else
+      stz::set_error("stz_solve_noalloc: twiddle upload failed: %s", cudaGetErrorString(cudaGetLastError()));
     return st;
   }
   // the mean strain goes behind the twiddles (8 values of 16 bytes reserved)

@@ -45,6 +45,34 @@
 #include "my_fft.h"
 #include "stz_api.h"
 
+/* bmgFlags.h switches whose physics the engine does not implement. Each one
+ * stops the build here, so that a drop-in build never runs the default
+ * physics in place of the switched-on one. Switches that only change what
+ * ParameterPrint/PrintFlags print (PRE_RELAXATION, RESIDUAL_STRESS,
+ * UNIFORM_DEFECTS) or that no reference source reads (STZ_DILATATION,
+ * FCC_SYMMETRY, TWO_FOLD_SYMMETRY) are accepted. */
+#if defined(STRAIN_RATE_SENSITIVITY) || defined(LOCAL_RATE_V2)
+#error "refapi: STRAIN_RATE_SENSITIVITY / LOCAL_RATE_V2 (rate-sensitive barriers, init.c:670-682) are not implemented by the engine"
+#endif
+#if defined(RELX_BIMOLE_FLAG) || defined(RELX_FVT_FLAG) || defined(AVG_PERMSOFTENING)
+#error "refapi: RELX_BIMOLE_FLAG / RELX_FVT_FLAG / AVG_PERMSOFTENING (softening relaxation laws, init.c:717-729) are not implemented by the engine"
+#endif
+#if defined(HEAT_CONDUCT)
+#error "refapi: HEAT_CONDUCT (local heating and conduction, elastic.c:549-582, evolution.c:247-249) is not implemented by the engine"
+#endif
+#if defined(RESIDUAL_STRESS_CONST) || defined(RESIDUAL_STRESS_RELX)
+#error "refapi: RESIDUAL_STRESS_CONST / RESIDUAL_STRESS_RELX (residual-stress work terms, init.c:576-583, bmg.c:86-102) are not implemented by the engine"
+#endif
+#if defined(XTAL_VARIANTS)
+#error "refapi: XTAL_VARIANTS (crystal variants, init.c:9-17, elastic.c:9, 398) is not implemented by the engine"
+#endif
+#if defined(STRESS_FREE_BOUNDARY)
+#error "refapi: STRESS_FREE_BOUNDARY (elastic.c:220-262) is not implemented by the engine"
+#endif
+#if !defined(MICRO_MEMORY)
+#error "refapi: builds without MICRO_MEMORY are not implemented by the engine (the direction modifier of init.c:572-640 reads the micro-memory state)"
+#endif
+
 static stz_ctx* g_ctx = NULL;
 static stz_params g_p;
 static int64_t g_events_seen = 0;  /* events already written to fq */

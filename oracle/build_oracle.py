@@ -8,7 +8,11 @@ Builds
                                    logger oracle/ref_wrap.c (only where the
                                    reference tree is present)
 
-Usage: python oracle/build_oracle.py [--ref] [--nx 64 --ny 64 --loading TENSION]
+Usage: python oracle/build_oracle.py [--ref] [--ref-dir DIR] [--nx 64 --ny 64 --loading TENSION]
+
+The reference's STZ source directory is taken from --ref-dir, else from the
+environment variable STZ_REFERENCE_DIR, else from the default checkout
+location below.
 """
 import argparse
 import os
@@ -16,7 +20,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = "/root/reference/Mesoscale simulation STZ model"
+DEFAULT_REF_DIR = "/root/reference/Mesoscale simulation STZ model"
+REF_DIR = os.environ.get("STZ_REFERENCE_DIR", DEFAULT_REF_DIR)
 REF_SOURCES = ["bmg.c", "io.c", "init.c", "elastic.c", "evolution.c"]
 CFLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fno-strict-aliasing"]
 
@@ -83,11 +88,15 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False)
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", action="store_true")
+    ap.add_argument("--ref-dir", default=None, help="the reference's STZ source directory")
     ap.add_argument("--nx", type=int, default=64)
     ap.add_argument("--ny", type=int, default=64)
     ap.add_argument("--loading", default="TENSION")
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args(argv)
+    if a.ref_dir:
+        global REF_DIR
+        REF_DIR = a.ref_dir
     print(build_oracle_lib(a.force))
     if a.ref:
         print(build_ref2d(a.nx, a.ny, a.loading, a.force))

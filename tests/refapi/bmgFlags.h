@@ -11,6 +11,8 @@
 #endif
 #define SF_SQUARE_FWD
 #define LOW_T
+#ifndef REFAPI_TEST_NO_MICRO_MEMORY
 #define MICRO_MEMORY
+#endif
 #define INHOM_ELAST
 #endif

@@ -139,3 +139,41 @@ def test_iout_records_are_the_raw_fields(engine_lib):
         assert np.array_equal(f, 0.25 * s - 3.0)
         g = np.fromfile(os.path.join(d, "Map_S003.iout"), dtype=np.int32)
         assert np.array_equal(g, 7 * s - 11)
+
+
+REFUSED_SWITCHES = [
+    (["-DSTRAIN_RATE_SENSITIVITY"], "STRAIN_RATE_SENSITIVITY"),
+    (["-DSTRAIN_RATE_SENSITIVITY", "-DLOCAL_RATE_V2"], "LOCAL_RATE_V2"),
+    (["-DRELX_BIMOLE_FLAG"], "RELX_BIMOLE_FLAG"),
+    (["-DRELX_FVT_FLAG"], "RELX_FVT_FLAG"),
+    (["-DAVG_PERMSOFTENING"], "AVG_PERMSOFTENING"),
+    (["-DHEAT_CONDUCT"], "HEAT_CONDUCT"),
+    (["-DRESIDUAL_STRESS_CONST"], "RESIDUAL_STRESS_CONST"),
+    (["-DRESIDUAL_STRESS_RELX"], "RESIDUAL_STRESS_RELX"),
+    (["-DXTAL_VARIANTS"], "XTAL_VARIANTS"),
+    (["-DSTRESS_FREE_BOUNDARY"], "STRESS_FREE_BOUNDARY"),
+    (["-DREFAPI_TEST_NO_MICRO_MEMORY"], "MICRO_MEMORY"),
+]
+
+
+def _syntax_check(defs):
+    cmd = (["gcc", "-fsyntax-only", "-std=gnu11", *defs, "-DREFAPI_NX=8", "-DREFAPI_NY=8", "-I", TESTHDR,
+            "-I", SHIM, "-I", os.path.join(ROOT, "include"), REFAPI])
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
+def test_drop_in_compiles_with_the_implemented_switches():
+    for defs in ([], ["-DREFAPI_TEST_SHEAR"], ["-DNO_SUBTRACT_ERROR"], ["-DFULL_TENSOR_RECORD"],
+                 ["-DPRE_RELAXATION", "-DUNIFORM_DEFECTS", "-DSTZ_DILATATION"]):
+        r = _syntax_check(defs)
+        assert r.returncode == 0, (defs, r.stderr[-2000:])
+
+
+@pytest.mark.parametrize("defs,name", REFUSED_SWITCHES, ids=[n for _, n in REFUSED_SWITCHES])
+def test_drop_in_refuses_unimplemented_switches(defs, name):
+    """A bmgFlags.h switch whose physics the engine does not implement stops
+    the drop-in build with an error that names it (instead of running the
+    default physics)."""
+    r = _syntax_check(defs)
+    assert r.returncode != 0
+    assert "#error" in r.stderr and name in r.stderr, r.stderr[-2000:]

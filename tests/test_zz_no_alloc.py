@@ -1,8 +1,8 @@
 """stz_solve_noalloc, the stress solve that allocates no device memory.
 
 It exists for callers that cannot call cudaMalloc: code that runs inside
-another framework's memory pool or budget, or inside a region recorded for
-replay. The caller passes its own device buffers; the solver's scratch sits
+another framework's memory pool or budget, or in a process whose allocator
+someone else owns. The caller passes its own device buffers; the solver's scratch sits
 in one fixed device array. Its result must equal that of the context solve
 (stz_solve) on the same eigenstrain, within the solver tolerance of the other
 tests, on two calls in a row (the second call reuses the array the first one
