@@ -114,7 +114,8 @@ def cpu_baseline(seconds=15.0, grid=GRID, threads=None, params=None, what=None):
     (the 3D shear configuration at grid^3, or `params`)."""
     from metallic_glasses_gb300 import configs
     from oracle import pyoracle
-    p = configs.plain128(n=grid) if params is None else params
+    # parameters from the oracle's own derivation: this leg loads no engine code
+    p = configs.plain128(n=grid, defaults=pyoracle.default_params) if params is None else params
     m = pyoracle.Model(p)
     all_threads = pyoracle.threads()
     if threads:
@@ -135,6 +136,41 @@ def cpu_baseline(seconds=15.0, grid=GRID, threads=None, params=None, what=None):
             "sample": "%d thermal events of %s after setup, %.1f s" % (n, what, dt)}
 
 
+def long_checkpoints(eng, events, per=1000):
+    """Continue the headline engine for `events` thermal events in steps of
+    `per` (one full FP64 re-solve ends each step) and collect the stress error
+    of the FP32 field against each re-solve."""
+    l2, mx = [], []
+    k0 = eng.scalars()["kstep"]
+    eng.sync()
+    eng.timer_start()
+    t0 = time.perf_counter()
+    for _ in range(events // per):
+        eng.run(max_events=per)
+        sc = eng.scalars()
+        l2.append(sc["stress_err_rms"])
+        mx.append(sc["stress_err_max"])
+    ms = eng.timer_stop()
+    wall = time.perf_counter() - t0
+    sc = eng.scalars()
+    done = sc["kstep"] - k0
+
+    def summ(v):
+        v = sorted(v)
+        q = lambda f: v[min(len(v) - 1, int(f * len(v)))]
+        return {"max": v[-1], "p99": q(0.99), "p50": q(0.5), "last": None}
+
+    s2, sm = summ(l2), summ(mx)
+    s2["last"], sm["last"] = l2[-1], mx[-1]
+    return {"events": done, "checkpoints": len(l2), "resolves_total": sc["n_resolves"],
+            "events_per_s": done / (ms / 1e3), "wall_s": wall, "rejections": sc["rejections"],
+            "near_ties": sc["near_ties"], "stress_err_rel_l2": s2, "stress_err_rel_max": sm,
+            "every_100th_checkpoint_rel_l2": l2[99::100],
+            "definition": "per checkpoint (every 1000 events): deviatoric stress of the FP32 incremental "
+                          "field against the full FP64 re-solve of the same eigenstrain; relative L2 norm "
+                          "and max norm (over the largest value)"}
+
+
 def reduce_ranks(ms, events, dist=None):
     """Whole-job figures of a weak-scaling run: the slowest rank's time and the
     events of all ranks (host tensors, so gloo serves as well as NCCL)."""
@@ -148,19 +184,50 @@ def reduce_ranks(ms, events, dist=None):
     return float(t.item()), int(e.item())
 
 
+DTYPE = ("f32 field/rates/line sums, int64 fixed-point plane/line/site selection, "
+         "f64 clock/eigenstrain/mean strain/periodic re-solve")
+
+
+def headline_config(n, events_per_step, world):
+    """The `config` of the headline line (both arms print the same one)."""
+    return {"workload": "STZ KMC, mixed form, %d^3 grid, 20 modes, shear strain rate 5e-5/s, T=455 K, "
+                        "%d thermal events per step, full FP64 re-solve every 1000 events" % (n, events_per_step),
+            "grid": n, "sites": n ** 3, "events_per_step": events_per_step,
+            "parallelism": "replicas" if world > 1 else "1 GPU", "l2": "flushed between steps (256 MB write)"}
+
+
 def run_reference(args, rank, world):
+    """The reference's method on the host cores: the CPU oracle (FP64, a full
+    re-solve per event; the reference's own FFTW2+MPI+GSL build is not
+    buildable here), on the headline configuration, with parameters from the
+    oracle's own derivation (no engine code is loaded). Each step is a
+    bounded sample of the workload: args.ref_events thermal events."""
     if rank != 0:
         return 0
-    cb = cpu_baseline(seconds=max(5.0, 30.0 / max(args.steps + args.warmup, 1)), grid=args.grid)
-    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "dtype": "f64",
-            "data": "synthetic", "scaling": "weak", "vs_baseline": None,
-            "config": {"workload": "FP64 STZ KMC at %d^3, shear strain rate, seed 0" % args.grid,
-                       "implementation": "CPU restatement of the reference method (oracle/stz_oracle.c, "
-                                         "OpenMP); the reference's own FFTW2+MPI+GSL build is not buildable "
-                                         "on this box"},
+    from metallic_glasses_gb300 import configs
+    from oracle import pyoracle
+    m = pyoracle.Model(configs.plain128(n=args.grid, defaults=pyoracle.default_params))
+    for _ in range(args.warmup):
+        m.run(max_events=args.ref_events)
+    k0 = m.scalars()["kstep"]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.run(max_events=args.ref_events)
+    dt = time.perf_counter() - t0
+    events = m.scalars()["kstep"] - k0
+    value = events / dt
+    cb = {"value": value, "unit": UNIT, "cores": pyoracle.threads(), "kind": "port",
+          "sample": "%d steps of %d thermal events of the %d^3 FP64 shear configuration (seed 0), %.1f s"
+                    % (args.steps, args.ref_events, args.grid, dt)}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "impl": "reference", "dtype": "f64", "data": "synthetic (seeded barriers, modes)", "scaling": "weak",
+            "vs_baseline": None, "config": headline_config(args.grid, args.events_per_step, world),
+            "implementation": "CPU restatement of the reference's method (oracle/stz_oracle.c, OpenMP, "
+                              "FP64, full re-solve per event); the reference's own FFTW2+MPI+GSL build is not "
+                              "buildable on this box",
             "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -181,6 +248,9 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the stress-strain ensemble of both forms")
     ap.add_argument("--no-plain64", action="store_true", help="skip the 64^3 FP64 plain run and its CPU oracle")
     ap.add_argument("--no-ref2d", action="store_true", help="skip the reference's 2D model at 512^2")
+    ap.add_argument("--no-long", action="store_true", help="skip the 10^6-event run with its checkpoint errors")
+    ap.add_argument("--long-events", type=int, default=1000000)
+    ap.add_argument("--ref-events", type=int, default=1, help="reference arm: thermal events per step")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -200,6 +270,7 @@ def main():
     n = args.grid
     B = args.events_per_step
     p = configs.mixed128(seed=rank, n=n, resolve_period=1000)
+    p.resolve_fp64 = 1  # the periodic full re-solve in FP64
     p.device = local
     eng = api.Engine(p)
     # warm-up
@@ -269,9 +340,13 @@ def main():
     scf = eng.scalars()
     stress_err = {"rel_l2_worst": scf["stress_err_rms_worst"], "rel_max_worst": scf["stress_err_max_worst"],
                   "resolves": scf["n_resolves"],
-                  "definition": "deviatoric stress of the FP32 incremental field vs a full re-solve of the "
-                                "same eigenstrain every 1000 events (FFT in FP32 pairs, about 48 bits); "
-                                "relative L2 norm and max norm"}
+                  "definition": "deviatoric stress of the FP32 incremental field vs a full FP64 re-solve of "
+                                "the same eigenstrain every 1000 events; relative L2 norm and max norm"}
+    long_run = None
+    if world == 1 and not args.no_long:
+        # the run as configured: 10^6 events on this engine, a full FP64
+        # re-solve every 1000 events, the stress error at every checkpoint
+        long_run = long_checkpoints(eng, args.long_events)
     eng.close()
 
     # FP64 plain form on the same grid (full FFT re-solve per event)
@@ -294,17 +369,15 @@ def main():
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 field/rates, f64 sums/clock/eigenstrain",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
             "data": "synthetic (seeded barriers, modes)",
-            "config": {"workload": "STZ KMC, mixed form, %d^3 grid, 20 modes, shear strain rate 5e-5/s, "
-                                   "T=455 K, %d thermal events per step, full re-solve (FP32 pairs) every 1000 events"
-                                   % (n, B),
-                       "grid": n, "sites": N, "events_per_step": B, "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "flushed between steps (256 MB write)"},
+            "config": headline_config(n, B, world),
             "plain_fp64_events_per_s": plain, "mixed_over_plain": value / world / plain,
             "stress_err": stress_err,
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
             "wall_s": t_wall}
+    if long_run:
+        line["long_run"] = long_run
     # the single-GPU studies and the CPU baselines run at N = 1 only: under
     # torchrun the other GPUs would idle while rank 0 runs them
     single = world == 1
@@ -358,8 +431,10 @@ def main():
         r2 = timing.run("ref2d512", events=2000, warmup=100)
         r2 = {k: r2[k] for k in ("grid", "sites", "events", "athermal_steps", "ms", "events_per_s", "us_per_event")}
         if not args.no_cpu:
-            r2["cpu_baseline"] = cpu_baseline(seconds=8.0, params=configs.ref2d(512, 512),
-                                              what="the reference's 2D model at 512 x 512 (shipped input)")
+            from oracle import pyoracle
+            r2["cpu_baseline"] = cpu_baseline(seconds=8.0, params=configs.ref2d(
+                512, 512, defaults=pyoracle.default_params, from_input=pyoracle.params_from_input),
+                what="the reference's 2D model at 512 x 512 (shipped input)")
             r2["gpu_over_cpu"] = r2["events_per_s"] / r2["cpu_baseline"]["value"]
         r2["workload"] = ("the reference's 2D model (per-site barriers and eigenstrains re-drawn after each "
                           "transformation, softening on) at its shipped 512 x 512 grid and input file, TENSION, "

@@ -81,10 +81,12 @@ enum {                      /* direction-softening schemes, bmgFlags.h:30-35 */
 
 enum {
   STZ_PREC_FP64 = 0,        /* "plain": FP64 throughout */
-  STZ_PREC_MIXED = 1        /* FP32 stress field, contraction and rates; exact
-                               fixed-point selection; FP64 clock, eigenstrain and
-                               mean strain; periodic full re-solve (FP32 pairs, or
-                               FP64 with resolve_fp64) */
+  STZ_PREC_MIXED = 1        /* FP32 stress field, contraction and rates; selection
+                               exact in distribution over the FP32 rates (64-bit
+                               fixed point, integer sums, rejection of the rare
+                               draw beyond a line's exact site sum); FP64 clock,
+                               eigenstrain and mean strain; periodic full re-solve
+                               (FP64 with resolve_fp64, else FP32 pairs) */
 };
 
 enum {
@@ -154,7 +156,14 @@ typedef struct stz_params {
   int32_t resolve_fp64;      /* mixed: 1 = the field solves (start, periodic re-solves, prints,
                                 avalanches) in FP64; 0 = in FP32 pairs (unevaluated sums of two
                                 floats, about 48 bits, at the FP32 issue rate) */
-  int32_t reserved[4];
+  int32_t sel_slack_shift;   /* mixed, for tests and analysis: the selection's per-line upper
+                                bound exceeds the FP32 line sum by 2^-sel_slack_shift of it
+                                (0: the smallest slack the line sum's rounding allows, chosen
+                                per grid); smaller values make rejected draws frequent */
+  int32_t main_pass_general; /* mixed, for tests: 1 = the per-event pass runs its general
+                                code for every line length instead of the bodies
+                                specialised to lines of 32, 64, 96, 128 and 256 sites */
+  int32_t reserved[2];
 } stz_params;
 
 /* kinds of stz_event */
@@ -169,6 +178,13 @@ typedef struct stz_event {
   double  dt;                /* clock advance of the step, s */
   double  q;                 /* activation energy of the chosen (site, mode), eV */
   double  total_rate;        /* summed rate over all (mode, site), s^-1 */
+  double  margin;            /* thermal: distance of the dice from the nearer edge of the
+                                chosen (site, mode)'s cumulative-rate interval, as a
+                                fraction of the total rate (how far a rate error must move
+                                a boundary to change the selection) */
+  int32_t draws;             /* thermal: generator words the selection took (1 unless
+                                the mixed form rejected a draw, see stz_scalars.rejections) */
+  int32_t reserved_ev;
 } stz_event;
 
 /* scalars returned by stz_get_scalars */
@@ -185,12 +201,15 @@ typedef struct stz_scalars {
   double  stress_err_max;    /* mixed, last full re-solve: max |ds| / max |s| of the
                                 deviatoric stress s against the re-solve */
   double  stress_err_rms;    /* mixed, last full re-solve: |ds|_2 / |s|_2 */
-  int64_t near_ties;         /* selections whose cumulative margin was below 1e-12 R */
+  int64_t near_ties;         /* selections whose margin was below the form's rate
+                                precision: 1e-12 of R (FP64 forms), 2^-24 of R (mixed) */
   int64_t log_dropped;       /* events not logged (ring full) */
   int64_t n_resolves;        /* periodic full re-solves done */
   double  stress_err_rms_worst;  /* worst of stress_err_rms over all re-solves */
   double  stress_err_max_worst;
-  int64_t reserved[2];
+  int64_t rejections;        /* mixed: draws rejected because the dice fell in a line's
+                                slack above the exact sum of its sites (each is redrawn) */
+  int64_t reserved[1];
 } stz_scalars;
 
 /* field selectors for stz_get_field / stz_set_field */

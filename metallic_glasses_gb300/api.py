@@ -44,13 +44,15 @@ class Params(C.Structure):
         ("init_mro", C.c_int32), ("print_period", C.c_int32), ("seed", C.c_uint64),
         ("precision", C.c_int32), ("solver", C.c_int32), ("resolve_period", C.c_int32), ("device", C.c_int32),
         ("log_capacity", C.c_int32), ("mode_seed_set", C.c_int32), ("mode_seed", C.c_int32),
-        ("resolve_fp64", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("resolve_fp64", C.c_int32), ("sel_slack_shift", C.c_int32),
+        ("main_pass_general", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 
 class Event(C.Structure):
     _fields_ = [("step", C.c_int64), ("site", C.c_int64), ("kind", C.c_int32), ("mode", C.c_int32),
-                ("time", C.c_double), ("dt", C.c_double), ("q", C.c_double), ("total_rate", C.c_double)]
+                ("time", C.c_double), ("dt", C.c_double), ("q", C.c_double), ("total_rate", C.c_double),
+                ("margin", C.c_double), ("draws", C.c_int32), ("reserved_ev", C.c_int32)]
 
 
 class Scalars(C.Structure):
@@ -60,11 +62,12 @@ class Scalars(C.Structure):
                 ("stopped", C.c_int32), ("status", C.c_int32), ("stress_err_max", C.c_double),
                 ("stress_err_rms", C.c_double), ("near_ties", C.c_int64), ("log_dropped", C.c_int64),
                 ("n_resolves", C.c_int64), ("stress_err_rms_worst", C.c_double),
-                ("stress_err_max_worst", C.c_double), ("reserved", C.c_int64 * 2)]
+                ("stress_err_max_worst", C.c_double), ("rejections", C.c_int64), ("reserved", C.c_int64 * 1)]
 
 
 EVENT_DTYPE = np.dtype([("step", np.int64), ("site", np.int64), ("kind", np.int32), ("mode", np.int32),
-                        ("time", np.float64), ("dt", np.float64), ("q", np.float64), ("total_rate", np.float64)])
+                        ("time", np.float64), ("dt", np.float64), ("q", np.float64), ("total_rate", np.float64),
+                        ("margin", np.float64), ("draws", np.int32), ("reserved_ev", np.int32)])
 
 _lib = None
 
@@ -154,7 +157,8 @@ def scalars_dict(s):
             "n_events_logged": s.n_events_logged, "stopped": s.stopped, "status": s.status,
             "stress_err_max": s.stress_err_max, "stress_err_rms": s.stress_err_rms, "near_ties": s.near_ties,
             "log_dropped": s.log_dropped, "n_resolves": s.n_resolves,
-            "stress_err_rms_worst": s.stress_err_rms_worst, "stress_err_max_worst": s.stress_err_max_worst}
+            "stress_err_rms_worst": s.stress_err_rms_worst, "stress_err_max_worst": s.stress_err_max_worst,
+            "rejections": s.rejections}
 
 
 class Engine:

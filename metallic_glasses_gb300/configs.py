@@ -9,6 +9,12 @@ grf256()        256^3, mixed form, correlated barrier field
 replicas(...)   uneven 3D replicas (grids 32/48/64/96, T in [325, 585] K,
                 log-uniform strain rates), seeds 0-255
 
+Every function takes `defaults`, the function that fills a model's default
+parameters (api.default_params, the engine library's, unless given), and
+ref2d also `from_input`, the input-file parser (api.params_from_input unless
+given): a caller that must not load the engine library (the CPU oracle's
+timing) passes the oracle's own.
+
 Common 3D physics: mu = 35 GPa, nu = 0.35, nu0 = 1e13 /s, Omega0 = 1 nm^3,
 T = 455 K, dF ~ N(1.2, 0.1) eV truncated at 3 sd, 20 traceless modes of
 magnitude 0.1 with orientations uniform on SO(3). The shear loading applies
@@ -58,35 +64,36 @@ def write_input(path, **overrides):
     return path
 
 
-def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, **overrides):
-    p = api.default_params(api.MODEL_REF2D)
+def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None, from_input=None,
+          **overrides):
+    p = (defaults or api.default_params)(api.MODEL_REF2D)
     if input_path is None:
         import tempfile
         d = tempfile.mkdtemp(prefix="stz_in_")
         input_path = write_input(os.path.join(d, "input"), **overrides)
-    api.params_from_input(input_path, p)
+    (from_input or api.params_from_input)(input_path, p)
     p.n[0], p.n[1], p.n[2] = 1, nx, ny
     p.loading = loading
     return p
 
 
-def _g3(n, seed=0):
-    p = api.default_params(api.MODEL_GLOBAL3D)
+def _g3(n, seed=0, defaults=None):
+    p = (defaults or api.default_params)(api.MODEL_GLOBAL3D)
     p.n[0] = p.n[1] = p.n[2] = n
     p.seed = seed
     return p
 
 
-def stress32(seed=0, n=32):
-    p = _g3(n, seed)
+def stress32(seed=0, n=32, defaults=None):
+    p = _g3(n, seed, defaults)
     p.loading = api.LOAD_STRESS
     p.applied_stress[api.XY] = 1.0
     p.strain_rate = 0.0
     return p
 
 
-def shear64(seed=0, n=64, eng_rate=1e-4, eng_end=0.05):
-    p = _g3(n, seed)
+def shear64(seed=0, n=64, eng_rate=1e-4, eng_end=0.05, defaults=None):
+    p = _g3(n, seed, defaults)
     p.loading = api.LOAD_SHEAR
     p.strain_rate = eng_rate / 2
     p.end_strain = eng_end / 2
@@ -94,20 +101,20 @@ def shear64(seed=0, n=64, eng_rate=1e-4, eng_end=0.05):
     return p
 
 
-def mixed128(seed=0, n=128, resolve_period=1000):
-    p = shear64(seed, n)
+def mixed128(seed=0, n=128, resolve_period=1000, defaults=None):
+    p = shear64(seed, n, defaults=defaults)
     p.precision = api.PREC_MIXED
     p.solver = api.SOLVER_KERNEL
     p.resolve_period = resolve_period
     return p
 
 
-def plain128(seed=0, n=128):
-    return shear64(seed, n)
+def plain128(seed=0, n=128, defaults=None):
+    return shear64(seed, n, defaults=defaults)
 
 
-def grf256(seed=0, n=256):
-    p = shear64(seed, n, eng_rate=1e-3, eng_end=0.08)
+def grf256(seed=0, n=256, defaults=None):
+    p = shear64(seed, n, eng_rate=1e-3, eng_end=0.08, defaults=defaults)
     p.df_kind = api.DF_CORRELATED
     p.q0_sd = 0.15
     p.q0_corr_len = 4.0

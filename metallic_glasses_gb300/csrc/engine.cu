@@ -205,6 +205,23 @@ int init_global3d(stz_ctx* c, MT* rng) {
   return STZ_OK;
 }
 
+// Slack exponent of the mixed form's per-line selection bounds. A line sum
+// of the main pass adds its sites' FP32 rates in a tree of depth at most
+// D = ceil(n2 / 32) + 31 (each lane's sites in order, then the 32 lanes in
+// order), so it is within gamma_D = D u / (1 - D u) (u = 2^-24) of the exact
+// sum of the same rates; a bound of the line sum plus 2^-slack of it plus 3
+// quanta holds the exact fixed-point sum of its sites when 2^-slack >=
+// gamma_D. The largest such slack is taken (18 for n2 <= 1024). `req` > 0
+// overrides it (tests of the rejection path).
+int selection_slack(int n2, int req) {
+  if (req > 0) return std::min(req, 40);
+  const double u = std::ldexp(1.0, -24), D = (double)((n2 + 31) / 32 + 31);
+  const double g = D * u / (1.0 - D * u);
+  int slack = 1;
+  while (slack < 40 && std::ldexp(1.0, -(slack + 1)) >= g) slack++;
+  return slack;
+}
+
 // Mixed-form constants: deviatoric mode coordinates and rate scaling.
 void mixed_constants(stz_ctx* c) {
   KParams& kp = c->kp;
@@ -630,6 +647,8 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   kp.inv_lam_coef = p.lambda / (2.0 * p.mu * ((ref2d ? 2.0 : 3.0) * p.lambda + 2.0 * p.mu));
   kp.invN = 1.0 / (double)((long long)p.n[0] * p.n[1] * p.n[2]);
   kp.resolve_period = mixed ? p.resolve_period : 0;
+  kp.sel_slack = selection_slack(kp.n2, p.sel_slack_shift);
+  kp.general_pass = p.main_pass_general ? 1 : 0;
 
   const long long N = kp.N;
   const int nc = kp.nc;
@@ -643,7 +662,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   if ((st = dalloc(&f.amark, (size_t)N))) return fail(st);
   if (mixed) {
     if ((st = dalloc(&f.lsum, (size_t)STZ_MODES * kp.n0 * kp.n1))) return fail(st);
-    if ((st = dalloc(&f.psum, (size_t)STZ_MODES * kp.n0))) return fail(st);
+    if ((st = dalloc(&f.psum, (size_t)(STZ_MODES + 1) * kp.n0))) return fail(st);
   } else {
     if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
     if ((st = dalloc(&f.gsum, (size_t)STZ_MODES * kp.ngroups))) return fail(st);
@@ -848,6 +867,7 @@ extern "C" int stz_get_scalars(stz_ctx* c, stz_scalars* o) {
   o->n_resolves = c->n_resolves;
   o->stress_err_rms_worst = c->err_rms_worst;
   o->stress_err_max_worst = c->err_max_worst;
+  o->rejections = h.rejections;
   return STZ_OK;
 }
 
@@ -1327,7 +1347,7 @@ extern "C" int stz_batch_create(const stz_params* params, int32_t count, stz_bat
     b->bl.start[c] = (int)blk_rep.size();
     for (int i = 0; i < count; i++) {
       const stz::KParams& kp = b->reps[i]->kp;
-      if (stz::batch_class(kp.n2) != c) continue;
+      if ((kp.general_pass ? stz::kBatchClasses - 1 : stz::batch_class(kp.n2)) != c) continue;
       first[i] = (int)blk_rep.size();
       for (int k = 0; k < kp.nblk; k++) blk_rep.push_back(i);
       b->bl.max_n2[c] = std::max(b->bl.max_n2[c], kp.n2);

@@ -232,8 +232,11 @@ __device__ void stop_check(const KParams& kp, Ctl* ctl) {
   }
 }
 
+// margin: a thermal event's distance of the dice from the nearer edge of the
+// chosen element's cumulative interval, as a fraction of the total rate;
+// draws: the generator words its selection took.
 __device__ void log_event(const KParams& kp, const Fields& f, Ctl* ctl, int kind, long long site, int mode,
-                          double time, double dt, double q, double R) {
+                          double time, double dt, double q, double R, double margin = 0.0, int draws = 0) {
   const long long i = ctl->nlog;
   if (i - ctl->log_base >= kp.log_cap) {
     ctl->nlog_dropped++;
@@ -248,6 +251,9 @@ __device__ void log_event(const KParams& kp, const Fields& f, Ctl* ctl, int kind
   e.dt = dt;
   e.q = q;
   e.total_rate = R;
+  e.margin = margin;
+  e.draws = draws;
+  e.reserved_ev = 0;
   f.log[i % kp.log_cap] = e;
   ctl->nlog = i + 1;
 }
@@ -403,6 +409,12 @@ __device__ __forceinline__ float mx_x(const KParams& kp, const float* sv, float 
   return x;
 }
 
+// The stored FP32 coordinates of site s (the mixed form's rates see them).
+__device__ __forceinline__ void mx_site(const KParams& kp, const Fields& f, long long s, float* sv) {
+#pragma unroll
+  for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+}
+
 // ---------------------------------------------------- block-level helpers
 // Inclusive scan of one double per thread over a 256-thread block; returns the
 // inclusive value and leaves every thread's inclusive value in sh_inc.
@@ -461,6 +473,25 @@ __device__ unsigned block_sum_u(unsigned v) {
   unsigned t = 0;
   for (int k = 0; k < TH / 32; k++) t += red[k];
   return t;
+}
+
+// Block-wide sum of v and maximum of mx (every thread of the block calls it).
+__device__ void block_sum_max_u(unsigned v, unsigned mx, unsigned* sum, unsigned* vmax) {
+  __shared__ unsigned red[2][TH / 32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+  mx = __reduce_max_sync(FULL, mx);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = v;
+    red[1][threadIdx.x >> 5] = mx;
+  }
+  __syncthreads();
+  unsigned t = 0, m = 0;
+  for (int k = 0; k < TH / 32; k++) {
+    t += red[0][k];
+    m = max(m, red[1][k]);
+  }
+  *sum = t;
+  *vmax = m;
 }
 
 // Last-block detection (threadfence reduction pattern). Returns true in the
@@ -551,7 +582,7 @@ __device__ __forceinline__ double site_rate(const KParams& kp, const Fields& f, 
     return kp.vt * exp(-g3_Q(kp, sg, f.dF[s], m) / kp.kT);
   } else {
     float sv[5];
-    for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+    mx_site(kp, f, s, sv);
     const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
     return (double)ex2_approx(mx_x(kp, sv, a, m));
   }
@@ -569,7 +600,7 @@ __device__ double site_Q(const KParams& kp, const Fields& f, const double* u, do
     return g3_Q(kp, sg, f.dF[s], m);
   } else {
     float sv[5];
-    for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+    mx_site(kp, f, s, sv);
     const float a = (kp.q_ref - f.dF32[s]) * kp.a_scale;
     return (double)kp.q_ref - (double)mx_x(kp, sv, a, m) / (double)kp.a_scale;
   }
@@ -835,7 +866,7 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
         c->sel_q = q;
         transform<MODEL>(kp, f, c, m, s, &c->rng);
         c->solve_req = 1;
-        log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue);
+        log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue, sh_margin / sh_R, 1);
       }
     } else if (kind == kElastic) {
       c->estep++;
@@ -1404,7 +1435,9 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
 
 // Per-line sums: each lane parks its 20 sums in shared memory and lanes
 // 0..19 add one mode each over the 32 lanes (a fixed order), written to
-// lsum[line][m].
+// lsum[line][m]; emx (lanes 0..19) keeps the largest biased exponent of the
+// sums written so far (0xff for a non-finite sum), from which the selection
+// takes the event's fixed-point scale.
 //
 // With LINEVOTE, also the line's athermal vote: a site argument above thr
 // gives a term of at least 2^thr (1 - 2^-22) in its mode's line sum, and FP32
@@ -1413,7 +1446,7 @@ __device__ __forceinline__ void mixed_line(const MixK& kp, int N32, int hp, int 
 // does not (or is NaN), for an exact test of the line.
 template <int LINEVOTE>
 __device__ __forceinline__ bool line_sums(const float2* acc2, float (*red)[STZ_MODES], float* lsum_line,
-                                          float thr) {
+                                          float thr, unsigned& emx) {
   const int lane = threadIdx.x & 31;
   float4* my = reinterpret_cast<float4*>(red[lane]);
 #pragma unroll
@@ -1426,6 +1459,7 @@ __device__ __forceinline__ bool line_sums(const float2* acc2, float (*red)[STZ_M
 #pragma unroll 8
     for (int r = 0; r < 32; r++) t += red[r][lane];
     lsum_line[lane] = t;
+    emx = max(emx, (__float_as_uint(t) >> 23) & 0xffu);
     if (LINEVOTE) hot = !(t < exp2f(thr - 1.0f));
   }
   if (LINEVOTE) return __any_sync(FULL, hot);
@@ -1433,38 +1467,72 @@ __device__ __forceinline__ bool line_sums(const float2* acc2, float (*red)[STZ_M
   return false;
 }
 
-// Error-free FP32 addition (Knuth's TwoSum, six operations, no branch):
-// a + b = s + e exactly, s = fl(a + b).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float bp = __fsub_rn(s, a);
-  const float ap = __fsub_rn(s, bp);
-  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+// ------------------------------------------------ fixed-point selection
+// The selection of the mixed form is exact in distribution over the FP32
+// site rates the main pass computed. Every quantity it compares is an integer
+// in one 64-bit fixed point per event (value v held as floor(v 2^e)), so sums
+// are exact and do not depend on their order:
+//   site    r = floor(rate 2^e), the rate recomputed with the main pass's
+//           exact instruction chain;
+//   line    B = floor(L 2^e) + (floor(L 2^e) >> slack) + 3 for its FP32 sum
+//           L > 0 (else 0), an upper bound of the exact sum of its sites'
+//           r: L is within gamma_D of the exact sum of the same FP32 rates
+//           (D the depth of its summation tree) and 2^-slack >= gamma_D;
+//   plane   the exact sum of its lines' B; total the exact sum of the planes.
+// A target T uniform on [0, total) selects the plane and the line whose
+// intervals hold it, exactly; within the line, the site whose interval of
+// r holds the rest, or, when the rest falls beyond the sites' exact sum (in
+// the slack of the bound, a few per million draws), the draw is rejected and
+// a new target drawn. Accepted selections therefore take (site, mode) with
+// probability r / sum of all r: no level is clamped and no rounding mass is
+// moved to a neighbour. The clock uses the exact fixed-point sum of the FP32
+// line sums (not of the bounds).
+constexpr long long kFixMax = 1LL << 62;
+__device__ __forceinline__ long long fix_f(float v, int e) {
+  const unsigned b = __float_as_uint(v);
+  const int ex = (int)(b >> 23) & 0xff;
+  if (ex == 0 || (b >> 31)) return 0;
+  const unsigned long long mant = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  const int sh = ex - 150 + e;
+  if (sh >= 38) return kFixMax;
+  if (sh <= -24) return 0;
+  return (long long)(sh >= 0 ? mant << sh : mant >> -sh);
 }
-// (hi, lo) += (h2, l2) for unevaluated sums hi + lo of FP32 pairs.
-__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
-  float s, e;
-  two_sum(hi, h2, s, e);
-  e = __fadd_rn(e, __fadd_rn(lo, l2));
-  hi = __fadd_rn(s, e);  // renormalise: |e| is below half an ulp of s or s = 0
-  lo = __fsub_rn(e, __fsub_rn(hi, s));
+// ceil(log2(n)) for n >= 1
+__device__ __forceinline__ int clog2(long long n) { return n <= 1 ? 0 : 64 - __clzll(n - 1); }
+
+// The event's scale e from the largest biased exponent emax of its line sums:
+// every line sum is below 2^(emax - 126), so floor(L 2^e) < 2^(61 - c) with
+// c = ceil(log2(n0 n1 MODES)), and the bounds of all lines and modes (each
+// below (1 + 2^-slack) 2^(61 - c) + 3) add up to less than 2^62. The quantum
+// is 2^-(42 + ...) of the largest line sum (2^-42 at 128^3).
+__device__ __forceinline__ int fix_scale(const KParams& kp, unsigned emax) {
+  return 187 - clog2((long long)kp.n0 * kp.n1 * STZ_MODES) - (int)emax;
+}
+// A line's selection bound from its FP32 sum L and v = floor(L 2^e).
+__device__ __forceinline__ long long line_bound(float L, long long v, int slack) {
+  return L > 0.f ? v + (v >> slack) + 3 : 0;
 }
 
-// Plane sums psum[m][i0] = sum over i1 of lsum[i0 n1 + i1][m] for plane i0,
-// by one block: 8 threads per mode (thread m 8 + g takes lines g, g + 8, ...)
-// add the FP32 line sums as unevaluated pairs hi + lo with error-free
-// additions (about 48 bits; GB300 issues FP64 at 1/64 of the FP32 rate, and
-// a chain of FP64 additions per mode was most of this step), combine the 8
-// pairs by shuffles in a fixed tree, and store hi + lo in FP64. The plane's
-// largest biased exponent goes to *emax (an integer maximum, independent of
-// the order of the blocks).
-__device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, double* psum, int i0,
-                                           unsigned* emax) {
-  constexpr int kG = 8;     // threads per mode
+__device__ __forceinline__ long long shfl_xor_i64(long long v, int off) {
+  return (long long)__shfl_xor_sync(FULL, (unsigned long long)v, off);
+}
+
+// Plane i0's sums by one block, in the event's fixed point (scale from the
+// main pass's largest line-sum exponent): psum[m][i0] = the sum of the line
+// bounds of mode m over the plane's lines, and psum[MODES][i0] = the sum over
+// modes and lines of floor(L 2^e) (the clock). 8 threads per mode take lines
+// g, g + 8, ...; integer sums, so the result does not depend on the order.
+__device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum, long long* psum, int i0,
+                                           unsigned emax) {
+  constexpr int kG = 8;       // threads per mode
   constexpr int kBatch = 16;  // loads in flight per thread
+  __shared__ long long wv[TH / 32];
+  const int n0 = kp.n0, n1 = kp.n1;
+  const int e = fix_scale(kp, emax), slack = kp.sel_slack;
   const int m = threadIdx.x / kG, g = threadIdx.x % kG;
   const float* ls = lsum + (long long)i0 * n1 * STZ_MODES + m;
-  float hi = 0.f, lo = 0.f;
+  long long bs = 0, vs = 0;
   if (m < STZ_MODES) {
     for (int i1 = g; i1 < n1; i1 += kG * kBatch) {
       float x[kBatch];
@@ -1472,27 +1540,29 @@ __device__ __forceinline__ void plane_sums(int n0, int n1, const float* lsum, do
       for (int q = 0; q < kBatch; q++) x[q] = i1 + q * kG < n1 ? ls[(i1 + q * kG) * STZ_MODES] : 0.f;
 #pragma unroll
       for (int q = 0; q < kBatch; q++) {
-        float s, e;
-        two_sum(hi, x[q], s, e);
-        hi = s;
-        lo = __fadd_rn(lo, e);
+        const long long v = fix_f(x[q], e);
+        vs += v;
+        bs += line_bound(x[q], v, slack);
       }
     }
   }
   // the 8 threads of a mode are consecutive lanes of one warp
 #pragma unroll
   for (int off = 1; off < kG; off <<= 1) {
-    const float h2 = __shfl_xor_sync(FULL, hi, off), l2 = __shfl_xor_sync(FULL, lo, off);
-    pair_add(hi, lo, h2, l2);
+    bs += shfl_xor_i64(bs, off);
+    vs += shfl_xor_i64(vs, off);
   }
-  unsigned ex = 0;
-  if (m < STZ_MODES && g == 0) {
-    const double v = (double)hi + (double)lo;
-    psum[(long long)m * n0 + i0] = v;
-    ex = (unsigned)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffu;
+  if (m < STZ_MODES && g == 0) psum[(long long)m * n0 + i0] = bs;
+#pragma unroll
+  for (int off = kG; off < 32; off <<= 1) vs += shfl_xor_i64(vs, off);  // the warp's modes
+  if ((threadIdx.x & 31) == 0) wv[threadIdx.x >> 5] = vs;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+#pragma unroll
+    for (int k = 0; k < TH / 32; k++) t += wv[k];
+    psum[(long long)STZ_MODES * n0 + i0] = t;
   }
-  ex = __reduce_max_sync(FULL, ex);
-  if ((threadIdx.x & 31) == 0 && ex) atomicMax(emax, ex);
 }
 
 // Body of the grid-wide mixed-form kernel for block b of one replica (kp may
@@ -1523,7 +1593,7 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   const MixK k = {kp.n0, kp.n1,    kp.n2,      kp.kt1,    kp.kt2, kp.mx_c1, kp.mx_units, kp.nblk, kp.c1_magic,
                   kp.N,  kp.q_ref, kp.a_scale, kp.inv_kt, f.sdev, f.dF32,   f.ktab,      f.lsum};
   const float thr_neg = k.q_ref * k.a_scale;
-  unsigned neg = 0;
+  unsigned neg = 0, emx = 0;
   const int N32 = (int)k.N;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // pieces per line and their length (whole lines but for the 256-site pass)
@@ -1619,7 +1689,7 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
       __syncwarp();
       const int base = (L.i0 * k.n1 + L.i1) * k.n2;
       if (line_sums<LINEVOTE>(acc2, reinterpret_cast<float(*)[STZ_MODES]>(cur),
-                              k.lsum + ((long long)L.i0 * k.n1 + L.i1) * STZ_MODES, thr_neg))
+                              k.lsum + ((long long)L.i0 * k.n1 + L.i1) * STZ_MODES, thr_neg, emx))
         neg |= line_negative(k.sdev, k.dF32, N32, base, k.n2, k.q_ref, k.a_scale, k.inv_kt, md, thr_neg) ? 1u : 0u;
     }
     u = un;
@@ -1638,8 +1708,12 @@ __device__ __forceinline__ void mixed_main_body(const KParams& kp, const Fields&
   }
   if (UPDATE_ONLY) return;
   pdl_release();
-  const unsigned nb = block_sum_u(neg);
-  if (threadIdx.x == 0 && nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
+  unsigned nb, eb;
+  block_sum_max_u(neg, emx, &nb, &eb);
+  if (threadIdx.x == 0) {
+    if (nb) atomicAdd(&ctl->neg_count, (unsigned long long)nb);
+    if (eb) atomicMax(&ctl->line_emax, eb);
+  }
 }
 
 template <int UPDATE_ONLY, int N2 = 0>
@@ -1741,38 +1815,6 @@ __device__ void mixed_commit_lanes(const KParams& kp, Ctl* c, int m) {
   __syncwarp();
 }
 
-// ------------------------------------------------ fixed-point selection
-// The selection of the mixed form runs in exact 64-bit fixed point: every
-// plane, line and site rate is held as floor(v 2^e) for one power of two e
-// per event, chosen so that the total stays below 2^62. Sums of integers do
-// not depend on their order and take integer adds, where the FP64 sums they
-// replace cost this part's FP64 units tens of cycles each; the quantum
-// 2^-e is about 2^-50 of the largest plane sum, finer than FP64 for every
-// partial sum the search compares.
-constexpr long long kFixMax = 1LL << 62;
-__device__ __forceinline__ long long fix_d(double v, int e) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const int ex = (int)(b >> 52) & 0x7ff;
-  if (ex == 0 || (b >> 63)) return 0;  // zero, subnormal or negative
-  const unsigned long long mant = (b & 0xfffffffffffffULL) | (1ULL << 52);
-  const int sh = ex - 1075 + e;
-  if (sh >= 9) return kFixMax;
-  if (sh <= -53) return 0;
-  return (long long)(sh >= 0 ? mant << sh : mant >> -sh);
-}
-__device__ __forceinline__ long long fix_f(float v, int e) {
-  const unsigned b = __float_as_uint(v);
-  const int ex = (int)(b >> 23) & 0xff;
-  if (ex == 0 || (b >> 31)) return 0;
-  const unsigned long long mant = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
-  const int sh = ex - 150 + e;
-  if (sh >= 38) return kFixMax;
-  if (sh <= -24) return 0;
-  return (long long)(sh >= 0 ? mant << sh : mant >> -sh);
-}
-// ceil(log2(n)) for n >= 1
-__device__ __forceinline__ int clog2(long long n) { return n <= 1 ? 0 : 64 - __clzll(n - 1); }
-
 __device__ __forceinline__ long long shfl_up_i64(long long v, int off) {
   return (long long)__shfl_up_sync(FULL, (unsigned long long)v, off);
 }
@@ -1807,11 +1849,9 @@ __device__ long long block_incl_scan_i64(long long v, long long* sh_inc) {
 }
 
 // Warp search over per-lane contiguous chunks with sums v: the lane whose
-// inclusive prefix first reaches T (T clamped to the total, so that the last
-// positive chunk is taken when the finer level sums to less than the coarser
-// one), its exclusive prefix in *excl and the clamped target in *tq; -1 when
-// every chunk is empty.
-__device__ __forceinline__ int warp_find_i64(long long v, long long T, long long* excl, long long* tq) {
+// interval [excl, excl + v) holds T (at most one does), its exclusive prefix
+// in *excl; -1 when T is not below the warp's total.
+__device__ __forceinline__ int warp_find_i64(long long v, long long T, long long* excl) {
   const int lane = threadIdx.x & 31;
   long long x = v;
 #pragma unroll
@@ -1819,54 +1859,50 @@ __device__ __forceinline__ int warp_find_i64(long long v, long long T, long long
     const long long y = shfl_up_i64(x, off);
     if (lane >= off) x += y;
   }
-  const long long tot = (long long)__shfl_sync(FULL, (unsigned long long)x, 31);
-  long long Tq = T > tot ? tot : T;
-  if (Tq < 1) Tq = 1;
   const long long Eu = shfl_up_i64(x, 1);  // every lane takes part in the shuffle
   const long long El = lane ? Eu : 0;
-  const unsigned hit = __ballot_sync(FULL, v > 0 && El < Tq && Tq <= x);
+  const unsigned hit = __ballot_sync(FULL, El <= T && T < x);
   const int L = hit ? __ffs(hit) - 1 : -1;
   *excl = (long long)__shfl_sync(FULL, (unsigned long long)El, L < 0 ? 0 : L);
-  *tq = Tq;
   return L;
 }
 
-// Within one lane's chunk of n values (registers, unrolled): the first
-// positive entry whose running sum from E reaches T; its index, the running
-// sum before it and after it.
+// Within one lane's chunk of K values (registers, unrolled) starting at E:
+// the entry whose interval holds T (T < E + sum of v), and the running sum
+// before it in *before.
 template <int K>
-__device__ __forceinline__ int chunk_find(const long long* v, long long E, long long T, long long* before,
-                                          long long* after) {
-  long long run = E;
-  int hit = -1, lastpos = -1;
-  long long hb = E, ha = E, lb = E, la = E;
+__device__ __forceinline__ int chunk_find(const long long* v, long long E, long long T, long long* before) {
+  long long run = E, hb = E;
+  int hit = -1;
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    const long long b0 = run;
+    if (hit < 0 && T < run + v[k]) {
+      hit = k;
+      hb = run;
+    }
     run += v[k];
-    if (v[k] > 0) { lastpos = k; lb = b0; la = run; }
-    if (hit < 0 && v[k] > 0 && run >= T) { hit = k; hb = b0; ha = run; }
   }
-  if (hit < 0) { hit = lastpos; hb = lb; ha = la; }
   *before = hb;
-  *after = ha;
   return hit;
 }
 
 // Levels 2 and 3 of the mixed-form search, by warp 0 alone: the lines of
-// plane i0 for mode m from their FP32 sums, then the sites of the chosen line
-// with their rates recomputed exactly as the main pass computed them, both in
-// the fixed point of scale e. T is the target left within (m, i0). Returns
-// the site (or -1) in every lane, the distance of the target from the nearer
-// edge of the chosen site's interval in *margin and the chosen (site, mode)'s
-// scaled log2-rate argument (the chain of mx_x) in *x_sel.
+// plane i0 for mode m by their bounds, then the sites of the chosen line with
+// their rates recomputed exactly as the main pass computed them, all in the
+// fixed point of scale e. T (in [0, the plane's bound sum)) is the target
+// left within (m, i0). Returns the site in every lane, or kRejected when the
+// target left within the line lies beyond its sites' exact sum; *margin
+// receives the distance of the target from the nearer edge of the chosen
+// site's interval and *x_sel the chosen (site, mode)'s scaled log2-rate
+// argument (the chain of mx_x).
+constexpr long long kRejected = -2;
 constexpr int kLaneChunk = 20;  // plane sums per thread held in registers (20 n0 over TH threads: n0 <= 256)
 // KL: the lines or sites a lane holds (n1, n2 <= 32 KL)
 template <int KL>
 __device__ long long search_line_site(const KParams& kp, const Fields& f, int m, int i0, long long T, int e,
                                       long long* margin, unsigned long long* t_lines, float* x_sel) {
   const int lane = threadIdx.x & 31;
-  // level 2: lines
+  // level 2: lines, by their bounds
   const int n1 = kp.n1;
   const int c2 = (n1 + 31) / 32;
   const int a1 = lane * c2;
@@ -1875,24 +1911,27 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   long long S1 = 0;
 #pragma unroll
   for (int q = 0; q < KL; q++) {
-    lv[q] = (q < c2 && a1 + q < n1) ? fix_f(lp[(a1 + q) * STZ_MODES], e) : 0;
+    lv[q] = 0;
+    if (q < c2 && a1 + q < n1) {
+      const float L = lp[(a1 + q) * STZ_MODES];
+      lv[q] = line_bound(L, fix_f(L, e), kp.sel_slack);
+    }
     S1 += lv[q];
   }
-  long long E1, T1;
-  const int L1 = warp_find_i64(S1, T, &E1, &T1);
+  long long E1;
+  const int L1 = warp_find_i64(S1, T, &E1);
   if (lane == 0) *t_lines = gtimer();
-  if (L1 < 0) return -1;
+  if (L1 < 0) return -1;  // not reached: the plane's sum is the sum of these bounds
   int i1 = -1;
   long long rem2 = 0;
   if (lane == L1) {
-    long long hb, ha;
-    const int h = chunk_find<KL>(lv, E1, T1, &hb, &ha);
-    i1 = h < 0 ? -1 : a1 + h;
-    rem2 = T1 - hb;
+    long long hb;
+    const int h = chunk_find<KL>(lv, E1, T, &hb);
+    i1 = a1 + h;
+    rem2 = T - hb;
   }
   i1 = __shfl_sync(FULL, i1, L1);
   rem2 = (long long)__shfl_sync(FULL, (unsigned long long)rem2, L1);
-  if (i1 < 0) return -1;
   // level 3: sites of line (i0, i1), rates recomputed with the main pass's chain
   const int n2 = kp.n2;
   const long long base = ((long long)i0 * n1 + i1) * n2;
@@ -1908,26 +1947,29 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
     if (q < c3 && a2 + q < n2) {
       const long long s = base + a2 + q;
       float sv[5];
-#pragma unroll
-      for (int k = 0; k < 5; k++) sv[k] = f.sdev[(long long)k * kp.N + s];
+      mx_site(kp, f, s, sv);
       xv[q] = mx_x(kp, sv, (kp.q_ref - f.dF32[s]) * kp.a_scale, m);
       rv[q] = fix_f(ex2_approx(xv[q]), e);
     }
     S2 += rv[q];
   }
-  long long E2, T2;
-  const int L2 = warp_find_i64(S2, rem2, &E2, &T2);
-  if (L2 < 0) return -1;
+  long long E2;
+  const int L2 = warp_find_i64(S2, rem2, &E2);
+  if (L2 < 0) return kRejected;  // in the slack of the line's bound
   long long site = -1, mg = 0;
   float xs = 0.f;
   if (lane == L2) {
-    long long hb, ha;
-    const int h = chunk_find<KL>(rv, E2, T2, &hb, &ha);
-    site = h < 0 ? -1 : base + a2 + h;
-    mg = min(T2 - hb, ha - T2);
+    long long hb;
+    const int h = chunk_find<KL>(rv, E2, rem2, &hb);
+    long long ha = hb;
 #pragma unroll
     for (int q = 0; q < KL; q++)
-      if (q == h) xs = xv[q];
+      if (q == h) {
+        xs = xv[q];
+        ha = hb + rv[q];
+      }
+    site = base + a2 + h;
+    mg = min(rem2 - hb, ha - rem2);
   }
   site = (long long)__shfl_sync(FULL, (unsigned long long)site, L2);
   *margin = (long long)__shfl_sync(FULL, (unsigned long long)mg, L2);
@@ -1954,23 +1996,26 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   const unsigned long long t_tail = gtimer();
   __shared__ Ctl sc;
   __shared__ int sh_kind;
-  __shared__ double sh_R;
   __shared__ long long sh_site;
   __shared__ int sh_mode;
-  __shared__ double sh_margin;
+  __shared__ long long sh_margin;
   __shared__ float sh_x;
-  __shared__ long long sh_p1, sh_rem1, sh_Tint, sh_Rint;
+  __shared__ long long sh_p1, sh_rem1, sh_T, sh_RB;
+  __shared__ int sh_draws;
   __shared__ long long sh_inc_i[TH];
+  __shared__ long long sh_wclk[TH / 32];
   __shared__ unsigned long long sh_tl[2];  // search clock: level 1 done, level 2 done
-  // total rate: the FP64 plane sums q = m n0 + i0 in per-thread contiguous
-  // chunks (loaded before the control-block copy so that the two overlap),
-  // turned into the event's fixed point
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // the plane bounds q = m n0 + i0 in per-thread contiguous chunks (loaded
+  // before the control-block copy so that the two overlap), and the clock row
   const long long P = (long long)STZ_MODES * kp.n0;
   const int ch = (int)((P + TH - 1) / TH);
   const long long q0 = (long long)threadIdx.x * ch, q1 = min(q0 + ch, P);
-  double pv[kLaneChunk];
+  long long iv[kLaneChunk];
 #pragma unroll
-  for (int k = 0; k < kLaneChunk; k++) pv[k] = (q0 + k < q1) ? f.psum[q0 + k] : 0.0;
+  for (int k = 0; k < kLaneChunk; k++) iv[k] = (q0 + k < q1) ? f.psum[q0 + k] : 0;
+  long long vc = 0;
+  for (int i = threadIdx.x; i < kp.n0; i += TH) vc += f.psum[P + i];
   // the generator word the dice will take, unless the state is refilled first
   int mti0 = 624;
   uint32_t w0 = 0;
@@ -1983,43 +2028,40 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
     for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
   }
-  if (threadIdx.x == 0) { sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; }
+  if (threadIdx.x == 0) { sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; sh_draws = 1; }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) vc += shfl_xor_i64(vc, off);
+  if (lane == 0) sh_wclk[wid] = vc;
   __syncthreads();
-  // largest biased exponent of the plane sums, gathered by the plane blocks
-  // (the bit patterns of non-negative doubles order like the values; 0x7ff
-  // marks a non-finite sum); every value < 2^(emax - 1022), so P of them sum
-  // below 2^62
-  const int emax = (int)sc.plane_emax;
-  const int e = 1084 - clog2(P) - emax;
-  long long iv[kLaneChunk];
+  // the event's fixed point, from the largest line-sum exponent the main pass
+  // gathered (0xff: a non-finite sum)
+  const int emax = (int)sc.line_emax;
+  const int e = fix_scale(kp, emax);
   long long S = 0;
 #pragma unroll
-  for (int k = 0; k < kLaneChunk; k++) {
-    iv[k] = fix_d(pv[k], e);
-    S += iv[k];
-  }
-  for (long long q = q0 + kLaneChunk; q < q1; q++) S += fix_d(f.psum[q], e);
+  for (int k = 0; k < kLaneChunk; k++) S += iv[k];
+  for (long long q = q0 + kLaneChunk; q < q1; q++) S += f.psum[q];
   const long long Iq = block_incl_scan_i64(S, sh_inc_i);
   const unsigned long long t_sums = gtimer();
   block_twist_if_needed(&g->rng);
   Ctl* c = &sc;
   if (threadIdx.x == 0) {
     c->step++;
-    c->plane_emax = 0;  // read by every thread before the scan's barriers
+    c->line_emax = 0;  // read by every thread before the scan's barriers
     c->has_pend = 0;
     for (int k = 0; k < 6; k++) c->U[k] = 0;
-    const long long Rint = sh_inc_i[TH - 1];
-    sh_Rint = Rint;
-    const double Rraw = ldexp((double)Rint, -e);
-    const double R = Rraw * kp.rate_scale;
-    sh_R = Rraw;
+    long long RL = 0;  // the exact sum of the quantised FP32 line sums
+    for (int k = 0; k < TH / 32; k++) RL += sh_wclk[k];
+    const long long RB = sh_inc_i[TH - 1];
+    sh_RB = RB;
+    const double R = ldexp((double)RL, -e) * kp.rate_scale;
     c->total_rate = R;
     int kind;
     if (c->neg_count > 0) {
       kind = kAthermal;
       c->halt = 1;
       c->halt_reason = kHaltAthermal;
-    } else if (emax == 0x7ff || Rint <= 0) {
+    } else if (emax == 0xff || RL <= 0 || RB <= 0) {
       kind = kNone;
       c->status = STZ_ERR_NAN;
       c->halt = 1;
@@ -2031,13 +2073,10 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       const int i = mti0 < 624 ? mti0 : g->rng.mti;
       uint32_t y = mti0 < 624 ? w0 : g->rng.mt[i];
       g->rng.mti = i + 1;
-      y ^= (y >> 11);
-      y ^= (y << 7) & 0x9d2c5680u;
-      y ^= (y << 15) & 0xefc60000u;
-      y ^= (y >> 18);
-      // T = dice R with dice = y / 2^32, in the fixed point
-      sh_Tint = (long long)__umul64hi((unsigned long long)Rint, (unsigned long long)y << 32);
-      if (y == 0) {
+      y = mt_temper(y);
+      // T = dice RB with dice = y / 2^32: uniform on [0, RB) at the dice's resolution
+      sh_T = (long long)__umul64hi((unsigned long long)RB, (unsigned long long)y << 32);
+      if (y == 0) {  // dice 0 locates no event in the reference (evolution.c:171-224)
         kind = kNone;
         c->status = STZ_ERR_NO_EVENT;
         c->halt = 1;
@@ -2054,75 +2093,108 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   const unsigned long long t_dec = gtimer();
   const int kind = sh_kind;
   if (kind == kThermal) {
-    // level 1: (mode, plane), by the thread whose chunk holds the target
-    const long long Tq = sh_Tint < 1 ? 1 : sh_Tint;
-    const long long E = threadIdx.x > 0 ? sh_inc_i[threadIdx.x - 1] : 0;
-    if (E < Tq && Tq <= Iq) {
-      long long hb, ha;
-      int h = -1;
-      if (q0 + kLaneChunk >= q1) {
-        h = chunk_find<kLaneChunk>(iv, E, Tq, &hb, &ha);
-      } else {
-        // long chunks (more than kLaneChunk planes per thread): walk in memory
-        long long run = E, lastbefore = E;
-        int lastpos = -1;
-        hb = E;
-        for (long long q = q0; q < q1; q++) {
-          const long long v = fix_d(f.psum[q], e);
-          const long long b0 = run;
-          run += v;
-          if (v > 0) { lastpos = (int)(q - q0); lastbefore = b0; }
-          if (h < 0 && v > 0 && run >= Tq) { h = (int)(q - q0); hb = b0; }
+    // warp 1's lanes 0..5 keep the components the mode-only commit changes,
+    // to put them back when a draw is rejected
+    double keep[6] = {0, 0, 0, 0, 0, 0};
+    if (wid == 1 && lane < 6) {
+      keep[0] = c->eps0_sum[lane];
+      keep[1] = c->eps_avg[lane];
+      keep[2] = c->eps_avg_applied[lane];
+      keep[3] = c->u[lane];
+      keep[4] = c->stress[lane];
+      keep[5] = c->U[lane];
+    }
+    for (;;) {
+      // level 1: (mode, plane), by the thread whose chunk holds the target
+      const long long T = sh_T;
+      const long long E = threadIdx.x > 0 ? sh_inc_i[threadIdx.x - 1] : 0;
+      if (E <= T && T < Iq) {
+        long long hb = E;
+        int h = -1;
+        if (q0 + kLaneChunk >= q1) {
+          h = chunk_find<kLaneChunk>(iv, E, T, &hb);
+        } else {
+          // long chunks (more than kLaneChunk planes per thread): walk in memory
+          long long run = E;
+          for (long long q = q0; q < q1 && h < 0; q++) {
+            const long long v = f.psum[q];
+            if (T < run + v) {
+              h = (int)(q - q0);
+              hb = run;
+            }
+            run += v;
+          }
         }
-        if (h < 0) { h = lastpos; hb = lastbefore; }
+        sh_p1 = q0 + h;
+        sh_rem1 = T - hb;
       }
-      sh_p1 = h < 0 ? -1 : q0 + h;
-      sh_rem1 = Tq - hb;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      // levels 2 and 3: warp 0
-      const long long pg = sh_p1;
-      long long site = -1, mg = 0;
-      float xs = 0.f;
-      int m = -1;
-      if (threadIdx.x == 0) sh_tl[0] = gtimer();
-      if (pg >= 0) {
-        m = (int)(pg / kp.n0);
-        const int i0 = (int)(pg - (long long)m * kp.n0);
-        const int nl = max(kp.n1, kp.n2);
-        if (nl <= 128) site = search_line_site<4>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
-        else if (nl <= 256) site = search_line_site<8>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
-        else site = search_line_site<16>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+      __syncthreads();
+      if (wid == 0) {
+        // levels 2 and 3: warp 0
+        const long long pg = sh_p1;
+        long long site = -1, mg = 0;
+        float xs = 0.f;
+        int m = -1;
+        if (lane == 0) sh_tl[0] = gtimer();
+        if (pg >= 0) {
+          m = (int)(pg / kp.n0);
+          const int i0 = (int)(pg - (long long)m * kp.n0);
+          const int nl = max(kp.n1, kp.n2);
+          if (nl <= 128) site = search_line_site<4>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+          else if (nl <= 256) site = search_line_site<8>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+          else site = search_line_site<16>(kp, f, m, i0, sh_rem1, e, &mg, &sh_tl[1], &xs);
+        }
+        if (lane == 0) {
+          sh_site = site;
+          sh_mode = m;
+          sh_margin = mg;
+          sh_x = xs;
+        }
+      } else if (wid == 1) {
+        // warp 1, while warp 0 searches: the clock advance and the parts of the
+        // commit that need only the mode (level 1 chose it). If the search then
+        // finds no site the step ends in an error and this state is not used.
+        const long long pg = sh_p1;
+        if (pg >= 0) {
+          if (lane == 0) c->t_kmc = 1.0 / c->total_rate;
+          __syncwarp();
+          mixed_commit_lanes(kp, c, (int)(pg / kp.n0));
+        }
       }
+      __syncthreads();
+      if (sh_site != kRejected) break;
+      // rejected: undo warp 1's commit and draw a new target
+      if (wid == 1 && lane < 6) {
+        c->eps0_sum[lane] = keep[0];
+        c->eps_avg[lane] = keep[1];
+        c->eps_avg_applied[lane] = keep[2];
+        c->u[lane] = keep[3];
+        c->stress[lane] = keep[4];
+        c->U[lane] = keep[5];
+      }
+      block_twist_if_needed(&g->rng);
       if (threadIdx.x == 0) {
-        sh_site = site;
-        sh_mode = m;
-        sh_margin = (double)mg;
-        sh_x = xs;
+        c->rejections++;
+        sh_draws++;
+        const int i = g->rng.mti;
+        const uint32_t y = mt_temper(g->rng.mt[i]);
+        g->rng.mti = i + 1;
+        sh_T = (long long)__umul64hi((unsigned long long)sh_RB, (unsigned long long)y << 32);
+        sh_p1 = -1;
+        sh_site = -1;
       }
-    } else if (threadIdx.x < 64) {
-      // warp 1, while warp 0 searches: the clock advance and the parts of the
-      // commit that need only the mode (level 1 chose it). If the search then
-      // finds no site the step ends in an error and this state is not used.
-      const long long pg = sh_p1;
-      if (pg >= 0) {
-        if (threadIdx.x == 32) c->t_kmc = 1.0 / c->total_rate;
-        __syncwarp();
-        mixed_commit_lanes(kp, c, (int)(pg / kp.n0));
-      }
+      __syncthreads();
     }
-    __syncthreads();
   }
   const unsigned long long t_search = gtimer();
-  if (threadIdx.x >= 64 && threadIdx.x < 96) {
+  if (wid == 2) {
     // warp 2: the site's eigenstrain, while thread 0 logs the event
     if (kind == kThermal && sh_site >= 0) mixed_commit_site_lanes(kp, f, sh_site, sh_mode);
-  } else if (threadIdx.x < 32) {
+  } else if (wid == 0) {
     const long long s = sh_site;
     const int m = sh_mode;
     if (threadIdx.x == 0) {
-      const double Rtrue = sh_R * kp.rate_scale;
+      const double Rtrue = c->total_rate;
       if (kind == kThermal) {
         if (s < 0) {
           c->status = STZ_ERR_NO_EVENT;
@@ -2130,7 +2202,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
           c->halt_reason = kHaltError;
           c->step_kind = kNone;
         } else {
-          if (sh_margin < (double)(sh_Rint >> 40)) c->near_ties++;  // within 2^-40 R of an edge
+          if (sh_margin < (sh_RB >> 24)) c->near_ties++;  // within 2^-24 R of an edge
           // Q of the chosen (site, mode) from the argument the search computed
           const double q = (double)kp.q_ref - (double)sh_x * kp.inv_a_scale;
           c->sel_site = s;
@@ -2140,7 +2212,8 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
           c->pend_site = s;
           c->pend_mode = m;
           c->totime += c->t_kmc;
-          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime, c->t_kmc, q, Rtrue);
+          log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime, c->t_kmc, q, Rtrue,
+                    (double)sh_margin / (double)sh_RB, sh_draws);
           if (kp.resolve_period > 0 && c->kstep >= c->next_resolve) {
             c->halt = 1;
             c->halt_reason = kHaltResolve;
@@ -2180,7 +2253,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       c->prof_n++;
     }
   }
-  if (threadIdx.x < 32) {
+  if (wid == 0) {
     __syncwarp();
     set_mixed_head_warp(kp, c);
   }
@@ -2220,7 +2293,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select(KParams kp, Fields f) {
   pdl_wait();
   pdl_release();
   if (f.ctl->halt) return;
-  plane_sums(kp.n0, kp.n1, f.lsum, f.psum, blockIdx.x, &f.ctl->plane_emax);
+  plane_sums(kp, f.lsum, f.psum, blockIdx.x, f.ctl->line_emax);
   if (!last_of(&f.ctl->ticket, gridDim.x)) return;
   mixed_tail_body(kp, f, 0);
 }
@@ -2279,7 +2352,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __
   const int n0 = e.kp.n0;
   Ctl* ctl = e.f.ctl;
   if ((int)blockIdx.x >= n0 || ctl->halt) return;
-  plane_sums(n0, e.kp.n1, e.f.lsum, e.f.psum, blockIdx.x, &ctl->plane_emax);
+  plane_sums(e.kp, e.f.lsum, e.f.psum, blockIdx.x, ctl->line_emax);
   if (!last_of(&ctl->ticket, (unsigned)n0)) return;
   load_desc(d, r, &skp, &sf);
   mixed_tail_body(skp, sf, 0);
@@ -2575,6 +2648,7 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
   mixed_smem_init();
   if (update_only) k_mixed<1><<<kp.nblk, TH, mix_smem_bytes(kp.n2), st>>>(kp, f);
+  else if (kp.general_pass) launch_pdl(k_mixed<0>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 256) launch_pdl(k_mixed<0, 256>, dim3(kp.nblk), mix_smem_main_bytes(256), st, kp, f);
   else if (kp.n2 == 128) launch_pdl(k_mixed<0, 128>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);
   else if (kp.n2 == 96) launch_pdl(k_mixed<0, 96>, dim3(kp.nblk), mix_smem_bytes(kp.n2), st, kp, f);

@@ -48,14 +48,18 @@ STZ_HD void mt_twist(MT* r) {
   r->mti = 0;
 }
 
-STZ_HD uint32_t mt_next(MT* r) {
-  if (r->mti >= 624) mt_twist(r);
-  uint32_t k = r->mt[r->mti++];
+// The output tempering of one state word.
+STZ_HD uint32_t mt_temper(uint32_t k) {
   k ^= (k >> 11);
   k ^= (k << 7) & 0x9d2c5680u;
   k ^= (k << 15) & 0xefc60000u;
   k ^= (k >> 18);
   return k;
+}
+
+STZ_HD uint32_t mt_next(MT* r) {
+  if (r->mti >= 624) mt_twist(r);
+  return mt_temper(r->mt[r->mti++]);
 }
 
 STZ_HD double mt_uniform(MT* r) { return mt_next(r) / 4294967296.0; }

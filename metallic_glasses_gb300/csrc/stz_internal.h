@@ -86,7 +86,9 @@ struct Ctl {
   int sel_mode;
   long long sel_site;
   int ath_count;
-  unsigned int plane_emax;   // mixed: largest biased exponent of this event's plane sums
+  unsigned int line_emax;    // mixed: largest biased FP32 exponent of this event's line sums
+                             // (atomic maximum of the main pass; 0xff: a non-finite sum)
+  long long rejections;      // mixed: selection draws rejected (dice in a line's slack)
   // device-clock phase times of the mixed-form kernel (globaltimer, ns)
   unsigned long long prof_t0, prof_main_ns, prof_tail_ns, prof_n;
   unsigned long long prof_part_ns[8];  // tail: copy-in+sums, twist+decision, search, commit,
@@ -114,7 +116,9 @@ struct Fields {
   double* gsum = nullptr;    // [MODES][ngroups] per (mode, group of blocks) sums
   unsigned* gticket = nullptr;  // [ngroups] last-block counters of the groups
   float* lsum = nullptr;     // mixed: [n0 n1][MODES] per-line rate sums
-  double* psum = nullptr;    // mixed: [MODES][n0] per-plane rate sums
+  long long* psum = nullptr; // mixed: [MODES + 1][n0] per-(mode, plane) sums of the line
+                             // bounds in the event's fixed point; row MODES: each plane's
+                             // fixed-point sum of its line sums over all modes (the clock)
   void* spec = nullptr;      // [nc][Nk] complex FP64 spectrum
   float* ktab = nullptr;     // mixed: [kt0][kt1][kt2][16] response table (15 used)
   stz_event* log = nullptr;  // event ring
@@ -159,6 +163,9 @@ struct KParams {
   double rate_scale;               // vt * exp(-q_ref/kT): true rate per scaled unit
   float mdev_raw[STZ_MODES][5];    // mode deviatoric coords (unscaled)
   int kt0, kt1, kt2;               // response-table extents (n/2+1)
+  int sel_slack;                   // a line's selection bound exceeds its fixed-point FP32 sum
+                                   // by 2^-sel_slack of it (plus 3 quanta)
+  int general_pass;                // the per-event pass runs its general code for every n2
   long long log_cap;
   int resolve_period;
   int c2r_blocks;                  // blocks of the FFT's C2R pass (msum row length)

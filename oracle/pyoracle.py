@@ -45,6 +45,13 @@ def lib():
         L.or_rng_uniform.restype = C.c_double
         L.or_ran_gaussian.argtypes = [vp, C.c_double]
         L.or_ran_gaussian.restype = C.c_double
+        L.or_set_mean_strain.argtypes = [vp, C.POINTER(C.c_double)]
+        L.or_force_path.argtypes = [vp, vp, vp, vp, C.c_int64]
+        L.or_get_checks.argtypes = [vp, vp, C.c_int64]
+        L.or_get_checks.restype = C.c_int64
+        L.or_set_bounded_selection.argtypes = [vp, C.c_int]
+        L.or_params_default.argtypes = [C.POINTER(Params), C.c_int]
+        L.or_params_from_input_file.argtypes = [C.POINTER(Params), C.c_char_p]
         L.or_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         L.or_set_threads.restype = None
@@ -67,6 +74,24 @@ class Rng:
 
     def gaussian(self, sigma=1.0):
         return lib().or_ran_gaussian(self.buf, sigma)
+
+
+def default_params(model):
+    """Parameters of a model from the oracle's own defaults (no engine library)."""
+    p = Params()
+    st = lib().or_params_default(C.byref(p), model)
+    if st != 0:
+        raise ValueError("oracle: no defaults for model %d" % model)
+    return p
+
+
+def params_from_input(path, base=None):
+    """A reference-format input file through the oracle's parser (no engine library)."""
+    p = base if base is not None else default_params(0)
+    st = lib().or_params_from_input_file(C.byref(p), path.encode())
+    if st != 0:
+        raise ValueError("oracle: cannot read input file %s (status %d)" % (path, st))
+    return p
 
 
 def fft3(a, sign):
@@ -129,6 +154,35 @@ class Model:
         v = np.ascontiguousarray(values, dtype=np.float64)
         if lib().or_set_field(self.h, which, comp, v.ctypes.data, self.N) != 0:
             raise ValueError("bad field %d/%d" % (which, comp))
+
+    def set_mean_strain(self, eps_avg):
+        v = (C.c_double * 6)(*([float(x) for x in eps_avg] + [0.0] * (6 - len(eps_avg))))
+        lib().or_set_mean_strain(self.h, v)
+
+    def force_path(self, sites, modes, draws=None):
+        """The next len(sites) thermal events take these (site, mode) pairs,
+        each after discarding draws[k] - 1 generator words."""
+        s = np.ascontiguousarray(sites, dtype=np.int64)
+        mo = np.ascontiguousarray(modes, dtype=np.int32)
+        d = np.ones(len(s), np.int32) if draws is None else np.ascontiguousarray(draws, dtype=np.int32)
+        self._force = (s, mo, d)
+        st = lib().or_force_path(self.h, s.ctypes.data, mo.ctypes.data, d.ctypes.data, len(s))
+        if st != 0:
+            raise ValueError("oracle: bad forced path (status %d)" % st)
+
+    def checks(self):
+        """Per forced event: own site, own mode, dice, the forced element's
+        cumulative interval [lo, hi] (fractions of R), R and the words the
+        own choice took."""
+        n = len(self._force[0]) if getattr(self, "_force", None) else 0
+        out = np.zeros((max(n, 1), 7))
+        k = lib().or_get_checks(self.h, out.ctypes.data, n)
+        return out[:k]
+
+    def set_bounded_selection(self, slack):
+        """Own choices by line bounds of slack 2^-slack with rejection."""
+        if lib().or_set_bounded_selection(self.h, int(slack)) != 0:
+            raise ValueError("oracle: bad slack %r" % slack)
 
     def elastic_energy(self):
         e = C.c_double()

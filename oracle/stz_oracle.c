@@ -256,6 +256,17 @@ struct or_model {
   /* log */
   stz_event* log;
   int64_t nlog, caplog;
+  /* forced path (or_force_path): the thermal events to take instead of the
+   * oracle's own choices, and what the oracle would have chosen */
+  int64_t* force_site;
+  int32_t* force_mode;
+  int32_t* force_draws;
+  int64_t force_n, force_i;
+  double* force_check;   /* [force_n][7]: own site, own mode, dice, forced element's
+                            cumulative interval (lower, upper), total rate, own draws */
+  int sel_slack;         /* 0: the reference's selection; > 0: the line-bound rule
+                            (or_set_bounded_selection) */
+  double* line_cb;       /* bounded rule: cumulative line bounds */
 };
 
 static int is2d(const or_model* m) { return m->dim == 2; }
@@ -267,14 +278,17 @@ static double voigt_weight(const or_model* m, int c) {
   return c >= 3 ? 2.0 : 1.0;
 }
 
-static void log_event(or_model* m, int kind, long site, int mode, double dt, double q, double R) {
+static void log_event(or_model* m, int kind, long site, int mode, double dt, double q, double R, double margin,
+                      int draws) {
   if (m->nlog == m->caplog) {
     m->caplog = m->caplog ? m->caplog * 2 : 1024;
     m->log = (stz_event*)realloc(m->log, sizeof(stz_event) * (size_t)m->caplog);
   }
   stz_event* e = &m->log[m->nlog++];
+  memset(e, 0, sizeof(*e));
   e->step = m->step; e->site = site; e->kind = kind; e->mode = mode;
   e->time = m->totime; e->dt = dt; e->q = q; e->total_rate = R;
+  e->margin = margin; e->draws = draws;
 }
 
 /* isotropicinv (elastic.c:522-531) generalised to DIM dimensions:
@@ -792,7 +806,7 @@ static int athermal(or_model* m) {
       if (minQ > m->Q[(size_t)mo * N + s]) { mm = mo; minQ = m->Q[(size_t)mo * N + s]; }
     if (minQ < 0 || fabs(minQ) < 0.33) {
       voxel_transform(m, mm, s);
-      log_event(m, STZ_EV_ATHERMAL, s, mm, 0.0, minQ, 0.0);
+      log_event(m, STZ_EV_ATHERMAL, s, mm, 0.0, minQ, 0.0, 0.0, 0);
     }
   }
   or_solve(m);
@@ -804,6 +818,48 @@ static int athermal(or_model* m) {
 }
 
 /* -------------------------------------------------------------------- KMC */
+/* The bounded selection rule (or_set_bounded_selection), for checking another
+ * implementation's rejection path: the normalised cumulative rates c[] of the
+ * mode-major elements, grouped in lines of n2 consecutive elements; each line
+ * j gets the bound B_j = L_j (1 + 2^-slack) of its sum L_j; a dice u picks
+ * the line whose bound interval holds T = u sum(B); the rest of T within the
+ * line picks the element by the cumulative rates, unless it lies beyond L_j,
+ * when the draw is rejected and the next generator word is drawn. Returns
+ * the element and the words used in *draws, drawn from g (a copy of the
+ * generator as it was before the event's first word). */
+static long bounded_select(or_model* m, const double* c, long M, or_rng g, double* dice_used, int* draws) {
+  const long n2 = m->n2, nl = M / n2;
+  const double f = 1.0 + ldexp(1.0, -m->sel_slack);
+  double* cb = m->line_cb;
+  double run = 0;
+  for (long j = 0; j < nl; j++) {
+    const double base = j ? c[j * n2 - 1] : 0.0;
+    cb[j] = run;
+    run += (c[(j + 1) * n2 - 1] - base) * f;
+  }
+  const double RB = run;
+  for (int d = 1; d < 1000; d++) {
+    const double u = or_rng_uniform(&g);
+    const double T = u * RB;
+    long lo = 0, hi = nl - 1;  /* last line with cb <= T */
+    while (lo < hi) {
+      long mid = lo + (hi - lo + 1) / 2;
+      if (cb[mid] <= T) lo = mid; else hi = mid - 1;
+    }
+    const long j = lo;
+    const double base = j ? c[j * n2 - 1] : 0.0;
+    const double rem = T - cb[j];
+    if (rem >= c[(j + 1) * n2 - 1] - base) continue;  /* in the line's slack */
+    long i = j * n2;
+    while (i < (j + 1) * n2 - 1 && c[i] - base <= rem) i++;
+    *draws = d;
+    *dice_used = u;
+    return i;
+  }
+  *draws = 0;
+  return -1;
+}
+
 static int kmc(or_model* m) {
   long N = m->N, M = (long)STZ_MODES * N;
   double t_kmc = 0;
@@ -817,6 +873,10 @@ static int kmc(or_model* m) {
   t_kmc = 1 / t_kmc;
   if (t_kmc < m->dt) {
     m->kstep++;
+    const int forced = m->force_i < m->force_n;
+    const int draws = forced ? m->force_draws[m->force_i] : 1;
+    const or_rng g0 = m->rng;  /* before this event's words */
+    for (int k = 1; k < draws; k++) (void)or_rng_get(&m->rng);  /* draws the forced path rejected */
     double dice = or_rng_uniform(&m->rng);
     for (long i = 0; i < M; i++) rate[i] *= t_kmc;
     for (long i = 1; i < M; i++) rate[i] += rate[i - 1];
@@ -833,19 +893,47 @@ static int kmc(or_model* m) {
       event = 0;
     }
     if (event < 0) return STZ_ERR_NO_EVENT;
+    int own_draws = 1;
+    if (m->sel_slack > 0) {
+      /* the bounded rule: own choice from the same words (a copy of the
+       * generator from before this event's draws) */
+      double u;
+      const long e2 = bounded_select(m, rate, M, g0, &u, &own_draws);
+      if (e2 < 0) return STZ_ERR_NO_EVENT;
+      event = e2;
+      if (!forced)
+        for (int k = 1; k < own_draws; k++) (void)or_rng_get(&m->rng);  /* the rejected words */
+    }
+    if (forced) {
+      /* take the forced element; record the oracle's own choice and where the
+       * dice lies against the forced element's cumulative interval */
+      const long fe = (long)m->force_mode[m->force_i] * N + m->force_site[m->force_i];
+      double* ck = m->force_check + 7 * m->force_i;
+      ck[0] = (double)(event - (event / N) * N);
+      ck[1] = (double)(event / N);
+      ck[2] = dice;
+      ck[3] = fe > 0 ? rate[fe - 1] : 0.0;
+      ck[4] = rate[fe];
+      ck[5] = R;
+      ck[6] = (double)own_draws;
+      m->force_i++;
+      event = fe;
+    }
     int mo = (int)(event / N);
     long s = event - (long)mo * N;
     double q = m->Q[event];
+    const double lo = event > 0 ? rate[event - 1] : 0.0, hi = rate[event];
+    const double margin = fmin(dice - lo, hi - dice);
     voxel_transform(m, mo, s);
     or_solve(m);
     load_after_event(m, t_kmc);
     m->totime += t_kmc;
-    log_event(m, STZ_EV_THERMAL, s, mo, t_kmc, q, R);
+    log_event(m, STZ_EV_THERMAL, s, mo, t_kmc, q, R, margin, forced ? draws : own_draws);
   } else {
     m->estep++;
     m->totime += m->dt;
     elastic_step(m);
-    log_event(m, STZ_EV_ELASTIC, -1, -1, m->dt, 0.0, R);
+    log_event(m, STZ_EV_ELASTIC, -1, -1, m->dt, 0.0, R, 0.0, 0);
   }
   return STZ_OK;
 }
@@ -944,7 +1032,54 @@ void or_destroy(or_model* m) {
   free(m->Q); free(m->rate); free(m->work); free(m->perm_soft); free(m->temp_soft);
   free(m->softening); free(m->tlast); free(m->Q0); free(m->Q1); free(m->deps); free(m->dF);
   free(m->log);
+  free(m->force_site); free(m->force_mode); free(m->force_draws); free(m->force_check);
+  free(m->line_cb);
   free(m);
+}
+
+/* Selection by line bounds with rejection (see bounded_select); slack 0
+ * restores the reference's rule. The generator must stay in step with the
+ * implementation under test: use it with or_force_path, whose draws give the
+ * words each event takes. */
+int or_set_bounded_selection(or_model* m, int slack) {
+  if (slack < 0 || slack > 60) return STZ_ERR_INVALID;
+  m->sel_slack = slack;
+  free(m->line_cb);
+  m->line_cb = slack ? (double*)xcalloc((size_t)(STZ_MODES * m->N / m->n2 + 1), sizeof(double)) : NULL;
+  return STZ_OK;
+}
+
+/* The next n thermal events take the given (site, mode) instead of the
+ * oracle's own choice, after discarding draws[k] - 1 generator words (the
+ * draws another implementation rejected); each records in or_get_checks what
+ * the oracle would have chosen with the same dice. The rest of the step (the
+ * FP64 rates, clock, solve and loading) is the oracle's own. */
+int or_force_path(or_model* m, const int64_t* sites, const int32_t* modes, const int32_t* draws, int64_t n) {
+  free(m->force_site); free(m->force_mode); free(m->force_draws); free(m->force_check);
+  m->force_site = (int64_t*)xcalloc((size_t)n, sizeof(int64_t));
+  m->force_mode = (int32_t*)xcalloc((size_t)n, sizeof(int32_t));
+  m->force_draws = (int32_t*)xcalloc((size_t)n, sizeof(int32_t));
+  m->force_check = (double*)xcalloc((size_t)n * 7, sizeof(double));
+  for (int64_t k = 0; k < n; k++) {
+    if (sites[k] < 0 || sites[k] >= m->N || modes[k] < 0 || modes[k] >= STZ_MODES || draws[k] < 1)
+      return STZ_ERR_INVALID;
+    m->force_site[k] = sites[k];
+    m->force_mode[k] = modes[k];
+    m->force_draws[k] = draws[k];
+  }
+  m->force_n = n;
+  m->force_i = 0;
+  return STZ_OK;
+}
+
+/* Checks of the forced events taken so far: [k][7] = own site, own mode,
+ * dice, the forced element's cumulative interval [lower, upper] (fractions of
+ * the total rate), the total rate and the words the own choice took. Returns
+ * the number of records. */
+int64_t or_get_checks(or_model* m, double* out, int64_t cap) {
+  int64_t k = m->force_i < cap ? m->force_i : cap;
+  memcpy(out, m->force_check, sizeof(double) * 7 * (size_t)k);
+  return k;
 }
 
 int or_get_scalars(or_model* m, stz_scalars* o) {
@@ -1015,5 +1150,155 @@ int or_elastic_energy(or_model* m, double* out) {
     e += 0.5 * acc;
   }
   *out = e;
+  return STZ_OK;
+}
+
+/* Mean strain EpsAvg that the next or_solve applies (the host assignment of
+ * EpsAvg before the solve of bmg.c:114-124). */
+int or_set_mean_strain(or_model* m, const double* eps_avg) {
+  for (int c = 0; c < m->nc; c++) m->eps_avg[c] = eps_avg[c];
+  return STZ_OK;
+}
+
+/* ============================================================ parameters */
+/* The oracle's own derivation of a run's parameters, so that CPU runs of the
+ * oracle need nothing from the engine library. */
+static double or_kt(double T) { return T * OR_BOLZ * OR_J_IN_EV; }
+
+/* tTemp of Init() (init.c:60): the relaxation time of the temporary softening */
+static double or_t_temp(const stz_params* p) {
+  return 1 / (p->trial_frequency * exp(-0.37 / or_kt(p->temperature)));
+}
+
+int or_params_default(stz_params* p, int model) {
+  if (!p || (model != STZ_MODEL_REF2D && model != STZ_MODEL_GLOBAL3D)) return STZ_ERR_INVALID;
+  memset(p, 0, sizeof(*p));
+  p->model = model;
+  p->trial_frequency = 1e13;               /* TRIAL_FREQUENCY, bmg.h:42 */
+  p->precision = STZ_PREC_FP64;
+  p->solver = STZ_SOLVER_FFT;
+  p->resolve_period = 1000;
+  p->sf_scheme = STZ_SF_SQUARE_FWD;        /* bmgFlags.h as shipped */
+  p->perm_soft = 13;                       /* PermSoft, TempSoft, cap: init.c:62-68 */
+  p->temp_soft = 39;
+  p->perm_soft_cap = -log(0.6);
+  p->print_period = 5;
+  if (model == STZ_MODEL_REF2D) {
+    /* bmg.h:23-94 and the shipped input file, through Init() under LOW_T */
+    double E = 69.46, nu = 2 * 0.365;
+    p->n[0] = 1;
+    p->n[1] = p->n[2] = 512;
+    p->temperature = 300;
+    p->voxel_volume = 0.7 * 0.7 * 1.0;
+    p->gamma0 = 0.14;
+    p->q0_mean = 2.0;
+    p->q0_sd = 0.25;
+    p->loading = STZ_LOAD_TENSION;
+    p->shear_elastic_quirk = 1;
+    p->young = E;
+    p->poisson = nu;
+    p->mu = E / (2 + 2 * nu);
+    p->lambda = E * nu / (1 - nu * nu);
+    p->strain_rate = 1e-4;
+    p->strain_increment = 1e-4;
+    p->end_strain = 0.06;
+    p->softening = 1;
+    p->seed = 123;
+    p->random_ratio = 0.2;
+    p->xq0amp = 2.0;
+  } else {
+    /* the 3D study: mu = 35 GPa, nu = 0.35, 455 K, Omega0 = 1 nm^3 */
+    double mu = 35.0, nu = 0.35;
+    p->n[0] = p->n[1] = p->n[2] = 64;
+    p->mu = mu;
+    p->poisson = nu;
+    p->lambda = 2 * mu * nu / (1 - 2 * nu);
+    p->young = 2 * mu * (1 + nu);
+    p->temperature = 455;
+    p->voxel_volume = 1.0;
+    p->gamma0 = 0.1;
+    p->df_kind = STZ_DF_TRUNC_NORMAL;
+    p->q0_mean = 1.2;
+    p->q0_sd = 0.1;
+    p->q0_trunc = 3.0;
+    p->q0_corr_len = 4.0;
+    p->loading = STZ_LOAD_SHEAR;
+    p->strain_rate = 0.5e-4;
+    p->strain_increment = 1e-4;
+    p->end_strain = 0.025;
+  }
+  p->t_temp = or_t_temp(p);
+  return STZ_OK;
+}
+
+/* One labelled entry of the reference's input file (io.c:4-101): the label
+ * on its own line, its value(s) on the next line, then a blank line. */
+typedef struct or_entry { const char* label; const char* fmt; int want; void* a; void* b; } or_entry;
+
+static int or_next_line(FILE* f, char* buf, int cap) {
+  while (fgets(buf, cap, f)) {
+    size_t n = strlen(buf);
+    while (n && (buf[n - 1] == '\n' || buf[n - 1] == '\r')) buf[--n] = 0;
+    if (n) return 1;                       /* blank lines separate entries */
+  }
+  return 0;
+}
+
+int or_params_from_input_file(stz_params* p, const char* path) {
+  FILE* f = path ? fopen(path, "r") : NULL;
+  if (!p || !f) return f ? (fclose(f), STZ_ERR_INVALID) : STZ_ERR_IO;
+  double E = 0, nu = 0, q0 = 0, rate = 0, inc = 0, rr = 0, end = 0, relx = 0, xs = 0, xq = 0, resi = 0,
+         xfrac = 0, xq0 = 0;
+  int seed = 0, period = 0, soft = 0, initmro = 0;
+  char resfile[256];
+  or_entry e[] = {
+      {"Moduli(E, nu):", "%lf %lf", 2, &E, &nu},
+      {"Stress-free energy barrier:", "%lf", 1, &q0, NULL},
+      {"Applied strain rate:", "%lf", 1, &rate, NULL},
+      {"Strain increment:", "%lf", 1, &inc, NULL},
+      {"Random seed:", "%d", 1, &seed, NULL},
+      {"Random ratio of fluctuation in energy barrier:", "%lf", 1, &rr, NULL},
+      {"Print period:", "%d", 1, &period, NULL},
+      {"End Strain:", "%lf", 1, &end, NULL},
+      {"Softening Flag:", "%d", 1, &soft, NULL},
+      {"Relaxation Time:", "%lf", 1, &relx, NULL},
+      {"Characteristic Xtal shear:", "%lf", 1, &xs, NULL},
+      {"Barrier for Xtal shear:", "%lf", 1, &xq, NULL},
+      {"Ratio for generating residual stress:", "%lf", 1, &resi, NULL},
+      {"Residual stress data file:", "%255s", 1, resfile, NULL},
+      {"Volume fraction of crystal-like MRO:", "%lf", 1, &xfrac, NULL},
+      {"Initialization condition for MRO:", "%d", 1, &initmro, NULL},
+      {"Stress-free energy barrier for crystal-like MRO:", "%lf", 1, &xq0, NULL},
+  };
+  const int ne = (int)(sizeof(e) / sizeof(e[0]));
+  int matched = 0;
+  char line[512];
+  for (int i = 0; i < ne; i++) {
+    if (!or_next_line(f, line, sizeof line)) break;
+    if (strcmp(line, e[i].label) != 0) continue;
+    if (!or_next_line(f, line, sizeof line)) break;
+    if (sscanf(line, e[i].fmt, e[i].a, e[i].b) == e[i].want) matched++;
+  }
+  fclose(f);
+  if (matched == 0) return STZ_ERR_IO;
+  /* Init() with LOW_T (init.c:26-27, 44) */
+  nu *= 2;
+  p->young = E;
+  p->poisson = nu;
+  p->mu = E / (2 + 2 * nu);
+  p->lambda = E * nu / (1 - nu * nu);
+  p->q0_mean = q0;
+  p->strain_rate = rate;
+  p->strain_increment = inc;
+  p->seed = (uint64_t)(uint32_t)seed;
+  p->random_ratio = rr;
+  p->print_period = period;
+  p->end_strain = end;
+  p->softening = soft;
+  p->xmro_frac = xfrac;
+  p->init_mro = initmro;
+  p->xq0amp = xq0;
+  p->t_temp = or_t_temp(p);
+  (void)relx; (void)xs; (void)xq; (void)resi;
   return STZ_OK;
 }

@@ -57,6 +57,23 @@ int  or_get_events(or_model* m, int64_t first, stz_event* out, int64_t cap, int6
 int  or_get_field(or_model* m, int which, int comp, double* out, int64_t count);
 int  or_set_field(or_model* m, int which, int comp, const double* in, int64_t count);
 int  or_elastic_energy(or_model* m, double* out);
+int  or_set_mean_strain(or_model* m, const double* eps_avg);
+/* Forced path: the next n thermal events take (sites[k], modes[k]) after
+ * discarding draws[k] - 1 generator words; or_get_checks returns per event
+ * the oracle's own choice with the same words, the dice, the forced element's
+ * cumulative interval (fractions of the total rate), the total rate and the
+ * words the own choice took. */
+int  or_force_path(or_model* m, const int64_t* sites, const int32_t* modes, const int32_t* draws, int64_t n);
+int64_t or_get_checks(or_model* m, double* out, int64_t cap);
+/* Own choices by line bounds of slack 2^-slack with rejection (slack > 0), the
+ * rule of the engine's mixed form, instead of the reference's (slack 0). For
+ * tests of the engine's rejection path only. */
+int  or_set_bounded_selection(or_model* m, int slack);
+/* Parameters without the engine library: defaults per model (the reference's
+ * constants for REF2D, the 3D study's for GLOBAL3D) and the reference's
+ * labelled input file through Init() under LOW_T (io.c:4-101, init.c:6-75). */
+int  or_params_default(stz_params* p, int model);
+int  or_params_from_input_file(stz_params* p, const char* path);
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int  or_threads(void);
 void or_set_threads(int n);

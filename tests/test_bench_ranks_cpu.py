@@ -53,3 +53,21 @@ def test_reference_arm_under_torchrun(oracle_lib):
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "events/s"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.headline_config(12, 1000, 2)
+    assert line["ms_per_step"] > 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_loads_no_engine_code(oracle_lib):
+    """The reference arm times the CPU oracle with parameters from the
+    oracle's own derivation: the engine library is never mapped."""
+    code = ("import runpy, sys\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', '--grid', '12']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\nexcept SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('ENGINE_MAPPED' if 'libstz_gb300' in maps else 'ENGINE_NOT_MAPPED')\n"
+            "print('ORACLE_MAPPED' if 'liboracle' in maps else 'ORACLE_NOT_MAPPED')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ENGINE_NOT_MAPPED" in r.stdout and "ORACLE_MAPPED" in r.stdout, r.stdout[-2000:]

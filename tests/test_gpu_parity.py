@@ -162,10 +162,13 @@ def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib):
 def test_ensemble_stress_strain_curves_agree():
     """Ensemble-mean stress-strain curves of the mixed form and the FP64 plain
     form (shear loading at 250 K to 3 % shear strain through the elastic rise,
-    thermal yield and softening; 16^3, seeds 0..5, the same seeds in both
-    forms) within 1 % of the plain curve's peak."""
+    thermal yield and softening; 16^3, seeds 0..15, the same seeds in both
+    forms) within 1 % of the plain curve's peak. The two forms' trajectories
+    part after some events, so the difference of the means is mostly the
+    sampling noise of 16 realisations per form."""
     from metallic_glasses_gb300 import timing
-    out = timing.ensemble(16, 6)
+    out = timing.ensemble(16, 16)
+    print("ensemble 16^3: %s" % {k: out[k] for k in ("rel_diff_max", "rel_diff_mean", "forms")})
     assert out["strain_xy_max"] > 0.029
     assert out["forms"]["plain"]["thermal_events"] > 1000
     assert out["rel_diff_max"] < 0.01, out["rel_diff_max"]
