@@ -662,6 +662,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   if ((st = dalloc(&f.amark, (size_t)N))) return fail(st);
   if (mixed) {
     if ((st = dalloc(&f.lsum, (size_t)STZ_MODES * kp.n0 * kp.n1))) return fail(st);
+    if ((st = dalloc(&f.lbnd, (size_t)STZ_MODES * kp.n0 * kp.n1))) return fail(st);
     if ((st = dalloc(&f.psum, (size_t)(STZ_MODES + 1) * kp.n0))) return fail(st);
   } else {
     if ((st = dalloc(&f.part, (size_t)STZ_MODES * kp.nblk))) return fail(st);
@@ -757,7 +758,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
   void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.dnorm, f.prev_deps, f.perm_soft, f.temp_soft,
-                  f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.psum, f.spec, f.ktab, f.log,
+                  f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.lbnd, f.psum, f.spec, f.ktab, f.log,
                   f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf, f.lam_site, f.mu_site,
                   f.inh_tau0, f.inh_eeff, f.inh_last, f.inh_part};
   for (void* p : ptrs)

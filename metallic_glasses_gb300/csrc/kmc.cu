@@ -514,12 +514,17 @@ __device__ bool last_block(Ctl* ctl, int nblk) {
 // MT19937 recurrence in four phases, each of which only reads words that no
 // thread of the same phase writes (old words k, k+1 and either old k+397 or
 // new k-227). Bit-identical to the sequential twist.
+__device__ void block_twist(MT* g);
 __device__ void block_twist_if_needed(MT* g) {
   __shared__ int need;
   __syncthreads();
   if (threadIdx.x == 0) need = g->mti >= 624;
   __syncthreads();
-  if (!need) return;
+  if (need) block_twist(g);
+}
+
+// The refill itself (whole block, unconditional).
+__device__ void block_twist(MT* g) {
   const uint32_t UP = 0x80000000u, LO = 0x7fffffffu, A = 0x9908b0dfu;
   uint32_t* mt = g->mt;
   const int k0[4] = {0, 227, 454, 623}, k1[4] = {227, 454, 623, 624};
@@ -1521,10 +1526,11 @@ __device__ __forceinline__ long long shfl_xor_i64(long long v, int off) {
 // Plane i0's sums by one block, in the event's fixed point (scale from the
 // main pass's largest line-sum exponent): psum[m][i0] = the sum of the line
 // bounds of mode m over the plane's lines, and psum[MODES][i0] = the sum over
-// modes and lines of floor(L 2^e) (the clock). 8 threads per mode take lines
-// g, g + 8, ...; integer sums, so the result does not depend on the order.
-__device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum, long long* psum, int i0,
-                                           unsigned emax) {
+// modes and lines of floor(L 2^e) (the clock); each line's bound also goes to
+// lbnd[i0][m][i1] for the search. 8 threads per mode take lines g, g + 8, ...;
+// integer sums, so the result does not depend on the order.
+__device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum, long long* psum, long long* lbnd,
+                                           int i0, unsigned emax) {
   constexpr int kG = 8;       // threads per mode
   constexpr int kBatch = 16;  // loads in flight per thread
   __shared__ long long wv[TH / 32];
@@ -1532,6 +1538,7 @@ __device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum,
   const int e = fix_scale(kp, emax), slack = kp.sel_slack;
   const int m = threadIdx.x / kG, g = threadIdx.x % kG;
   const float* ls = lsum + (long long)i0 * n1 * STZ_MODES + m;
+  long long* lb = lbnd + ((long long)i0 * STZ_MODES + m) * n1;
   long long bs = 0, vs = 0;
   if (m < STZ_MODES) {
     for (int i1 = g; i1 < n1; i1 += kG * kBatch) {
@@ -1541,8 +1548,10 @@ __device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum,
 #pragma unroll
       for (int q = 0; q < kBatch; q++) {
         const long long v = fix_f(x[q], e);
+        const long long b = line_bound(x[q], v, slack);
         vs += v;
-        bs += line_bound(x[q], v, slack);
+        bs += b;
+        if (i1 + q * kG < n1) lb[i1 + q * kG] = b;
       }
     }
   }
@@ -1906,16 +1915,12 @@ __device__ long long search_line_site(const KParams& kp, const Fields& f, int m,
   const int n1 = kp.n1;
   const int c2 = (n1 + 31) / 32;
   const int a1 = lane * c2;
-  const float* lp = f.lsum + (long long)i0 * n1 * STZ_MODES + m;
+  const long long* lp = f.lbnd + ((long long)i0 * STZ_MODES + m) * n1;
   long long lv[KL];
   long long S1 = 0;
 #pragma unroll
   for (int q = 0; q < KL; q++) {
-    lv[q] = 0;
-    if (q < c2 && a1 + q < n1) {
-      const float L = lp[(a1 + q) * STZ_MODES];
-      lv[q] = line_bound(L, fix_f(L, e), kp.sel_slack);
-    }
+    lv[q] = (q < c2 && a1 + q < n1) ? lp[a1 + q] : 0;
     S1 += lv[q];
   }
   long long E1;
@@ -2001,7 +2006,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   __shared__ long long sh_margin;
   __shared__ float sh_x;
   __shared__ long long sh_p1, sh_rem1, sh_T, sh_RB;
-  __shared__ int sh_draws;
+  __shared__ int sh_draws, sh_twist;
   __shared__ long long sh_inc_i[TH];
   __shared__ long long sh_wclk[TH / 32];
   __shared__ unsigned long long sh_tl[2];  // search clock: level 1 done, level 2 done
@@ -2028,7 +2033,10 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     uint32_t* d = reinterpret_cast<uint32_t*>(&sc);
     for (int i = threadIdx.x; i < kCtlScalarWords; i += blockDim.x) d[i] = a[i];
   }
-  if (threadIdx.x == 0) { sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; sh_draws = 1; }
+  if (threadIdx.x == 0) {
+    sh_p1 = -1; sh_site = -1; sh_margin = 0; sh_mode = -1; sh_draws = 1;
+    sh_twist = mti0 >= 624;  // the generator needs a refill before the dice
+  }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) vc += shfl_xor_i64(vc, off);
   if (lane == 0) sh_wclk[wid] = vc;
@@ -2043,7 +2051,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   for (long long q = q0 + kLaneChunk; q < q1; q++) S += f.psum[q];
   const long long Iq = block_incl_scan_i64(S, sh_inc_i);
   const unsigned long long t_sums = gtimer();
-  block_twist_if_needed(&g->rng);
+  if (sh_twist) block_twist(&g->rng);  // (every thread read sh_twist after the scan's barriers)
   Ctl* c = &sc;
   if (threadIdx.x == 0) {
     c->step++;
@@ -2293,7 +2301,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select(KParams kp, Fields f) {
   pdl_wait();
   pdl_release();
   if (f.ctl->halt) return;
-  plane_sums(kp, f.lsum, f.psum, blockIdx.x, f.ctl->line_emax);
+  plane_sums(kp, f.lsum, f.psum, f.lbnd, blockIdx.x, f.ctl->line_emax);
   if (!last_of(&f.ctl->ticket, gridDim.x)) return;
   mixed_tail_body(kp, f, 0);
 }
@@ -2352,7 +2360,7 @@ __global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __
   const int n0 = e.kp.n0;
   Ctl* ctl = e.f.ctl;
   if ((int)blockIdx.x >= n0 || ctl->halt) return;
-  plane_sums(e.kp, e.f.lsum, e.f.psum, blockIdx.x, ctl->line_emax);
+  plane_sums(e.kp, e.f.lsum, e.f.psum, e.f.lbnd, blockIdx.x, ctl->line_emax);
   if (!last_of(&ctl->ticket, (unsigned)n0)) return;
   load_desc(d, r, &skp, &sf);
   mixed_tail_body(skp, sf, 0);

@@ -116,6 +116,9 @@ struct Fields {
   double* gsum = nullptr;    // [MODES][ngroups] per (mode, group of blocks) sums
   unsigned* gticket = nullptr;  // [ngroups] last-block counters of the groups
   float* lsum = nullptr;     // mixed: [n0 n1][MODES] per-line rate sums
+  long long* lbnd = nullptr; // mixed: [n0][MODES][n1] the lines' selection bounds in the event's
+                             // fixed point, written by the plane sums (mode-major per plane,
+                             // so the search reads one contiguous run)
   long long* psum = nullptr; // mixed: [MODES + 1][n0] per-(mode, plane) sums of the line
                              // bounds in the event's fixed point; row MODES: each plane's
                              // fixed-point sum of its line sums over all modes (the clock)

@@ -44,11 +44,13 @@ def dev5(sig):
     return np.stack([(xx - yy) * r2, (2 * zz - xx - yy) * r6, q2 * yz, q2 * xz, q2 * xy])
 
 
-def replay(oracle_lib, eng, p_oracle, events, bounded=0):
-    """Run the engine, replay its thermal events in the oracle; returns
-    (engine events, oracle events, oracle checks, oracle model). bounded > 0:
-    the oracle's own choices follow the line-bound rule of that slack."""
-    eng.run(max_events=events)
+def replay(oracle_lib, eng, p_oracle, events, bounded=0, run=True):
+    """Run the engine (unless run is False: a batch replica that has run),
+    replay its thermal events in the oracle; returns (engine events, oracle
+    events, oracle checks, oracle model). bounded > 0: the oracle's own
+    choices follow the line-bound rule of that slack."""
+    if run:
+        eng.run(max_events=events)
     ev = eng.events()
     assert (ev["kind"] != api.EV_ATHERMAL).all()
     th = ev[ev["kind"] == api.EV_THERMAL]
@@ -143,6 +145,34 @@ def test_mixed_rejected_draws_follow_the_oracle(engine_lib, oracle_lib):
     check_state(stats)
     eng.close()
     ora.close()
+
+
+def test_batch_replicas_follow_the_oracle(engine_lib, oracle_lib):
+    """Replicas of one batch (uneven grids, temperatures and strain rates,
+    the shared seed-0 mode set, one launch per line-length class) replayed
+    in the oracle: the same bars as a single grid."""
+    ps = configs.replicas(count=4, sizes=(16, 24, 32))
+    for p in ps:
+        p.resolve_period = 100
+        p.resolve_fp64 = 1
+    events = 300
+    batch = api.Batch(ps)
+    batch.run(events)
+    checked = 0
+    for i, p in enumerate(ps):
+        r = batch.replicas[i]
+        if r.scalars()["kstep"] != events or (r.events()["kind"] == api.EV_ATHERMAL).any():
+            continue  # stopped early or avalanched: not a pure thermal path to replay
+        ev, oe, ck, ora = replay(oracle_lib, r, p, events, run=False)
+        stats, own_same, flagged, dist = replay_stats(r, ev, oe, ck, ora)
+        print("batch replica %d (%d^3, %.0f K): %s" % (i, p.n[0], p.temperature, stats))
+        assert dist.max() <= CUM_TOL, stats
+        assert (own_same | flagged).all(), np.nonzero(~(own_same | flagged))[0][:5]
+        check_state(stats)
+        checked += 1
+        ora.close()
+    assert checked >= 2
+    batch.close()
 
 
 def test_default_slack_rejects_rarely(engine_lib):
