@@ -417,7 +417,18 @@ def main():
         # per event) next to the CPU oracle on the same grid, in the same run
         from metallic_glasses_gb300 import timing
         pl = timing.run("plain64", events=2000, warmup=100)
+        rp = pl["rate_pass"]
         pl = {k: pl[k] for k in ("grid", "sites", "events", "athermal_steps", "ms", "events_per_s", "us_per_event")}
+        if rp and rp["achieved_gbs"]:
+            # the FP64 rate kernel against HBM: far below it, the kernel is
+            # bound by the FP64 pipe (ncu: profiles/k_rate64_64.md)
+            pl["roofline"] = {"kernel": "k_rate64<1> (FP64 rates of 20 modes, per-block sums, selection and commit "
+                                        "in the last block)", "bound": "fp64 pipe (HBM shown for scale)",
+                              "achieved": rp["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                              "frac": rp["achieved_gbs"] / peak, "alg_bytes_per_launch": rp["alg_bytes"],
+                              "launch_ms": rp["launch_ms"], "launches_timed": rp["launches"],
+                              "peak_kind": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                              else peak_kind}
         if not args.no_cpu:
             pl["cpu_baseline"] = cpu_baseline(seconds=8.0, grid=64)
             pl["gpu_over_cpu"] = pl["events_per_s"] / pl["cpu_baseline"]["value"]

@@ -341,12 +341,13 @@ int stz_phase_times(stz_ctx* ctx, double* main_us, double* tail_us, int64_t* n);
 int stz_selftest_wait(int32_t device, int32_t tries, int32_t* status, double* ms, int32_t* kernel_tries);
 /* sizeof the ABI structs, for bindings: 0 stz_params, 1 stz_event, 2 stz_scalars */
 int64_t stz_sizeof(int32_t which);
-/* Mixed form, timed with CUDA events on the ctx stream over *launches events
- * launched one by one: which = 0 the grid-wide stress-update/rate kernel,
+/* Timed with CUDA events on the ctx stream over *launches events launched
+ * one by one. Mixed form: which = 0 the grid-wide stress-update/rate kernel,
  * 2 the whole event (that kernel and the selection kernel: one block per plane
  * for the plane sums, the last of them running the tail), 1 the update-only
- * variant (the stress-field streaming floor). Returns the average ms;
- * *launches receives the number of events timed. */
+ * variant (the stress-field streaming floor). FP64 forms: which = 0 the rate
+ * kernel of *launches driver steps (rates, sums, selection and commit).
+ * Returns the average ms; *launches receives the number of launches timed. */
 int stz_kernel_time(stz_ctx* ctx, int32_t which, double* ms_avg, int64_t* launches);
 
 #ifdef __cplusplus

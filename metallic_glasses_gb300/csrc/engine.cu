@@ -378,12 +378,16 @@ int build_response_table(stz_ctx* c) {
 
 // ------------------------------------------------------------- stepping
 // One driver-loop iteration of the FP64 forms, as a fixed kernel sequence.
-void enqueue_plain_step(stz_ctx* c) {
+// One driver step of the FP64 forms; t0/t1 (optional) are recorded around the
+// rate kernel.
+void enqueue_plain_step(stz_ctx* c, cudaEvent_t t0 = nullptr, cudaEvent_t t1 = nullptr) {
   const KParams& kp = c->kp;
   const Fields& f = c->f;
   const int* gate = &f.ctl->solve_req;
   const double* ebar = f.ctl->eps_avg;
+  if (t0) cudaEventRecord(t0, c->stream);
   launch_rate_fp64(kp, f, c->stream);
+  if (t1) cudaEventRecord(t1, c->stream);
   launch_athermal(kp, f, 0, c->stream);
   solve_plain(c, gate, ebar);
   launch_post_a(kp, f, c->stream);
@@ -1219,8 +1223,28 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
   const int steps = launches && *launches > 0 ? (int)*launches : 64;
   const bool mixed = c->f.sdev != nullptr;
   if (!mixed) {
+    // FP64 forms: the rate kernel (rates, sums, selection and commit of the
+    // step in its last block) of `steps` driver steps, each launched alone
     *ms_avg = 0;
-    return STZ_ERR_UNSUPPORTED;
+    if (which != 0) return STZ_ERR_UNSUPPORTED;
+    Ctl& h = c->host_ctl;
+    if ((st = set_targets(c, -1, h.step + steps))) return st;
+    double tot = 0;
+    int n = 0;
+    for (int i = 0; i < steps && !h.halt && !h.stopped; i++) {
+      enqueue_plain_step(c, c->kev0, c->kev1);
+      CK(cudaStreamSynchronize(c->stream));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, c->kev0, c->kev1));
+      tot += ms;
+      n++;
+      if ((st = sync_ctl(c))) return st;
+      if ((st = drain_log(c))) return st;
+      if (h.status) return h.status;
+    }
+    *ms_avg = n ? tot / n : 0;
+    if (launches) *launches = n;
+    return STZ_OK;
   }
   if (which == 1) {
     // update-only variant: streams the stress field (read + write) and the

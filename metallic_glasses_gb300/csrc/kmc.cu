@@ -2101,29 +2101,39 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
   const unsigned long long t_dec = gtimer();
   const int kind = sh_kind;
   if (kind == kThermal) {
-    // warp 1's lanes 0..5 keep the components the mode-only commit changes,
-    // to put them back when a draw is rejected
-    double keep[6] = {0, 0, 0, 0, 0, 0};
+    // warp 1's lanes 0..5 keep the components the mode-only commit changes
+    // (in shared memory, not registers), to put them back when a draw is
+    // rejected
+    __shared__ double sh_keep[6][6];
     if (wid == 1 && lane < 6) {
-      keep[0] = c->eps0_sum[lane];
-      keep[1] = c->eps_avg[lane];
-      keep[2] = c->eps_avg_applied[lane];
-      keep[3] = c->u[lane];
-      keep[4] = c->stress[lane];
-      keep[5] = c->U[lane];
+      sh_keep[0][lane] = c->eps0_sum[lane];
+      sh_keep[1][lane] = c->eps_avg[lane];
+      sh_keep[2][lane] = c->eps_avg_applied[lane];
+      sh_keep[3][lane] = c->u[lane];
+      sh_keep[4][lane] = c->stress[lane];
+      sh_keep[5][lane] = c->U[lane];
     }
-    for (;;) {
-      // level 1: (mode, plane), by the thread whose chunk holds the target
+    // level 1 of the first draw: (mode, plane), by the thread whose chunk
+    // holds the target, from the sums it holds in registers (dead after this:
+    // a redraw walks its chunk in memory)
+    {
       const long long T = sh_T;
       const long long E = threadIdx.x > 0 ? sh_inc_i[threadIdx.x - 1] : 0;
-      if (E <= T && T < Iq) {
+      if (E <= T && T < Iq && q0 + kLaneChunk >= q1) {
         long long hb = E;
-        int h = -1;
-        if (q0 + kLaneChunk >= q1) {
-          h = chunk_find<kLaneChunk>(iv, E, T, &hb);
-        } else {
-          // long chunks (more than kLaneChunk planes per thread): walk in memory
-          long long run = E;
+        const int h = chunk_find<kLaneChunk>(iv, E, T, &hb);
+        sh_p1 = q0 + h;
+        sh_rem1 = T - hb;
+      }
+    }
+    for (int draw = 0;; draw++) {
+      // level 1 from memory: redraws, and chunks of more than kLaneChunk planes
+      {
+        const long long T = sh_T;
+        const long long E = threadIdx.x > 0 ? sh_inc_i[threadIdx.x - 1] : 0;
+        if (E <= T && T < Iq && (draw > 0 || q0 + kLaneChunk < q1)) {
+          long long run = E, hb = E;
+          int h = -1;
           for (long long q = q0; q < q1 && h < 0; q++) {
             const long long v = f.psum[q];
             if (T < run + v) {
@@ -2132,9 +2142,9 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
             }
             run += v;
           }
+          sh_p1 = q0 + h;
+          sh_rem1 = T - hb;
         }
-        sh_p1 = q0 + h;
-        sh_rem1 = T - hb;
       }
       __syncthreads();
       if (wid == 0) {
@@ -2173,12 +2183,12 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
       if (sh_site != kRejected) break;
       // rejected: undo warp 1's commit and draw a new target
       if (wid == 1 && lane < 6) {
-        c->eps0_sum[lane] = keep[0];
-        c->eps_avg[lane] = keep[1];
-        c->eps_avg_applied[lane] = keep[2];
-        c->u[lane] = keep[3];
-        c->stress[lane] = keep[4];
-        c->U[lane] = keep[5];
+        c->eps0_sum[lane] = sh_keep[0][lane];
+        c->eps_avg[lane] = sh_keep[1][lane];
+        c->eps_avg_applied[lane] = sh_keep[2][lane];
+        c->u[lane] = sh_keep[3][lane];
+        c->stress[lane] = sh_keep[4][lane];
+        c->U[lane] = sh_keep[5][lane];
       }
       block_twist_if_needed(&g->rng);
       if (threadIdx.x == 0) {

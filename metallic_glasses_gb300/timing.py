@@ -143,7 +143,14 @@ def run(config, events, warmup=1000, grid=None):
     eng.run(max_events=events)
     ms = eng.timer_stop()
     s1 = eng.scalars()
-    main = None
+    main = rate = None
+    if p.precision != api.PREC_MIXED:
+        # the FP64 rate kernel of single driver steps (algorithmic bytes: the
+        # six FP64 stress components and the FP64 barrier read, 56 B per site)
+        kms, kn = eng.kernel_time(steps=16, which=0)
+        n_sites = p.n[0] * p.n[1] * p.n[2]
+        rate = {"launch_ms": kms, "launches": kn, "alg_bytes": 56 * n_sites,
+                "achieved_gbs": 56 * n_sites / (kms / 1e3) / 1e9 if kms > 0 else None}
     if p.precision == api.PREC_MIXED:
         # the per-event pass alone, launch by launch (algorithmic bytes: read
         # and write of 5 FP32 stress coordinates and the FP32 barrier, 44 B
@@ -159,7 +166,7 @@ def run(config, events, warmup=1000, grid=None):
             "events_per_s": k / (ms / 1e3), "us_per_event": ms * 1e3 / max(k, 1),
             "resolves": s1["n_resolves"] - s0["n_resolves"],
             "stress_err_rms_worst": s1["stress_err_rms_worst"], "stress_err_max_worst": s1["stress_err_max_worst"],
-            "strain": s1["eps_avg"], "stopped": s1["stopped"], "main_pass": main}
+            "strain": s1["eps_avg"], "stopped": s1["stopped"], "main_pass": main, "rate_pass": rate}
 
 
 def _ensemble_params(grid, seed, mixed, temperature, eng_rate, eng_end):
