@@ -1529,8 +1529,10 @@ __device__ __forceinline__ long long shfl_xor_i64(long long v, int off) {
 // modes and lines of floor(L 2^e) (the clock); each line's bound also goes to
 // lbnd[i0][m][i1] for the search. 8 threads per mode take lines g, g + 8, ...;
 // integer sums, so the result does not depend on the order.
+// halted: the event does not run (the loads are issued anyway, next to the
+// halt flag's, so that the flag's round trip is not paid before them).
 __device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum, long long* psum, long long* lbnd,
-                                           int i0, unsigned emax) {
+                                           int i0, unsigned emax, int halted) {
   constexpr int kG = 8;       // threads per mode
   constexpr int kBatch = 16;  // loads in flight per thread
   __shared__ long long wv[TH / 32];
@@ -1540,11 +1542,15 @@ __device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum,
   const float* ls = lsum + (long long)i0 * n1 * STZ_MODES + m;
   long long* lb = lbnd + ((long long)i0 * STZ_MODES + m) * n1;
   long long bs = 0, vs = 0;
+  float x[kBatch];
+  int i1 = g;
   if (m < STZ_MODES) {
-    for (int i1 = g; i1 < n1; i1 += kG * kBatch) {
-      float x[kBatch];
 #pragma unroll
-      for (int q = 0; q < kBatch; q++) x[q] = i1 + q * kG < n1 ? ls[(i1 + q * kG) * STZ_MODES] : 0.f;
+    for (int q = 0; q < kBatch; q++) x[q] = i1 + q * kG < n1 ? ls[(i1 + q * kG) * STZ_MODES] : 0.f;
+  }
+  if (halted) return;  // the same in every thread of the block, before any barrier
+  if (m < STZ_MODES) {
+    for (;;) {
 #pragma unroll
       for (int q = 0; q < kBatch; q++) {
         const long long v = fix_f(x[q], e);
@@ -1553,6 +1559,10 @@ __device__ __forceinline__ void plane_sums(const KParams& kp, const float* lsum,
         bs += b;
         if (i1 + q * kG < n1) lb[i1 + q * kG] = b;
       }
+      i1 += kG * kBatch;
+      if (i1 >= n1) break;
+#pragma unroll
+      for (int q = 0; q < kBatch; q++) x[q] = i1 + q * kG < n1 ? ls[(i1 + q * kG) * STZ_MODES] : 0.f;
     }
   }
   // the 8 threads of a mode are consecutive lanes of one warp
@@ -1987,7 +1997,10 @@ constexpr int kCtlScalarWords = (int)(offsetof(Ctl, rng) / 4);
 
 // One block after the grid of k_mixed: total rate, step kind, dice, search,
 // commit, log and the halt conditions of the mixed form.
-__device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields& f, int update_only) {
+// check_halt: read the halt flag first (the selection kernel's blocks have
+// read it already; nothing sets it between their read and the tail).
+__device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields& f, int update_only,
+                                                int check_halt = 1) {
   Ctl* const g = f.ctl;
   if (update_only) {
     if (threadIdx.x == 0) {
@@ -1997,7 +2010,7 @@ __device__ __forceinline__ void mixed_tail_body(const KParams& kp, const Fields&
     }
     return;
   }
-  if (g->halt) return;
+  if (check_halt && g->halt) return;
   const unsigned long long t_tail = gtimer();
   __shared__ Ctl sc;
   __shared__ int sh_kind;
@@ -2310,10 +2323,11 @@ __device__ bool last_of(unsigned* counter, unsigned count) {
 __global__ void __launch_bounds__(TH) k_mixed_select(KParams kp, Fields f) {
   pdl_wait();
   pdl_release();
-  if (f.ctl->halt) return;
-  plane_sums(kp, f.lsum, f.psum, f.lbnd, blockIdx.x, f.ctl->line_emax);
+  const int halted = f.ctl->halt;
+  plane_sums(kp, f.lsum, f.psum, f.lbnd, blockIdx.x, f.ctl->line_emax, halted);
+  if (halted) return;
   if (!last_of(&f.ctl->ticket, gridDim.x)) return;
-  mixed_tail_body(kp, f, 0);
+  mixed_tail_body(kp, f, 0, 0);
 }
 
 // ------------------------------------------------------------ batches
@@ -2357,23 +2371,29 @@ __global__ void __launch_bounds__(TH, 3) k_mixed_batched(const BatchDesc* __rest
     mixed_main_body<0, LV, N2>(skp, sf, blk - rep_first[r], &skp.mdev2[0][0], skp.mdev_raw, mix_smem);
 }
 
-// Plane sums and selection of a batch: block (x, r) sums plane x of replica
-// r; the last of replica r's blocks runs its selection and reports its state.
-__global__ void __launch_bounds__(TH) k_mixed_select_batched(const BatchDesc* __restrict__ d,
-                                                             BatchStatus* __restrict__ st) {
-  __shared__ KParams skp;
-  __shared__ Fields sf;
+// Plane sums of a batch: block (x, r) sums plane x of replica r. A kernel of
+// its own (about 40 registers, six blocks per SM) so that the thousands of
+// plane blocks of a batch are not held to the tail's register count.
+__global__ void __launch_bounds__(TH, 6) k_plane_sums_batched(const BatchDesc* __restrict__ d) {
   pdl_wait();
   pdl_release();
   const int r = blockIdx.y;
   const BatchDesc& e = d[r];
-  const int n0 = e.kp.n0;
+  if ((int)blockIdx.x >= e.kp.n0) return;
   Ctl* ctl = e.f.ctl;
-  if ((int)blockIdx.x >= n0 || ctl->halt) return;
-  plane_sums(e.kp, e.f.lsum, e.f.psum, e.f.lbnd, blockIdx.x, ctl->line_emax);
-  if (!last_of(&ctl->ticket, (unsigned)n0)) return;
+  const int halted = ctl->halt;
+  plane_sums(e.kp, e.f.lsum, e.f.psum, e.f.lbnd, blockIdx.x, ctl->line_emax, halted);
+}
+
+// The tail of each replica of a batch (block r, after every plane sum of the
+// round), which then reports the replica's state.
+__global__ void __launch_bounds__(TH) k_mixed_tail_batched(const BatchDesc* __restrict__ d,
+                                                           BatchStatus* __restrict__ st) {
+  __shared__ KParams skp;
+  __shared__ Fields sf;
+  const int r = blockIdx.x;
   load_desc(d, r, &skp, &sf);
-  mixed_tail_body(skp, sf, 0);
+  mixed_tail_body(skp, sf, 0, 1);
   __syncthreads();
   if (threadIdx.x == 0) {
     const Ctl* c = sf.ctl;
@@ -2660,7 +2680,8 @@ void launch_mixed_batched(const BatchDesc* d, const int* blk_rep, const int* rep
       cudaStreamWaitEvent(st, bl.join[c], 0);
     }
   }
-  k_mixed_select_batched<<<dim3(max_n0, nrep), TH, 0, st>>>(d, status);
+  k_plane_sums_batched<<<dim3(max_n0, nrep), TH, 0, st>>>(d);
+  k_mixed_tail_batched<<<nrep, TH, 0, st>>>(d, status);
 }
 
 void launch_mixed_main(const KParams& kp, const Fields& f, int update_only, cudaStream_t st) {
