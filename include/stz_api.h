@@ -347,6 +347,8 @@ int64_t stz_sizeof(int32_t which);
  * for the plane sums, the last of them running the tail), 1 the update-only
  * variant (the stress-field streaming floor). FP64 forms: which = 0 the rate
  * kernel of *launches driver steps (rates, sums, selection and commit).
+ * In the mixed form a 40 us one-warp hold kernel runs before each timed
+ * launch, so the start event is not stamped ahead of the host's launch.
  * Returns the average ms; *launches receives the number of launches timed. */
 int stz_kernel_time(stz_ctx* ctx, int32_t which, double* ms_avg, int64_t* launches);
 

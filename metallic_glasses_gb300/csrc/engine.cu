@@ -1215,6 +1215,10 @@ extern "C" int stz_transfer_bytes(stz_ctx* c, int64_t* h2d, int64_t* d2h) {
 // Average device time of the per-step kernel: runs `steps` steps launching
 // that kernel directly between CUDA events (no graph), on the context's
 // stream. which = 0: the per-step rate/update kernel.
+// Lead of the hold kernel queued before each timed mixed-form launch: long
+// enough for the host to queue the event and the launches behind it.
+constexpr unsigned long long kHoldNs = 40000;
+
 extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_t* launches) {
   if (!c || !ms_avg) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
@@ -1251,6 +1255,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
     // response table; state is unchanged after its first launch
     double tot = 0;
     for (int i = 0; i < steps; i++) {
+      launch_hold(kHoldNs, c->stream);
       CK(cudaEventRecord(c->kev0, c->stream));
       launch_mixed_main(c->kp, c->f, 1, c->stream);
       CK(cudaEventRecord(c->kev1, c->stream));
@@ -1261,7 +1266,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
       tot += ms;
     }
     CK(cudaStreamSynchronize(c->stream));
-    c->launches += 2 * steps;
+    c->launches += 3 * steps;
     *ms_avg = tot / steps;
     if (launches) *launches = steps;
     return STZ_OK;
@@ -1274,6 +1279,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
   for (int i = 0; i < steps; i++) {
     // which 0: the grid-wide update/rate kernel alone; 2: the whole event
     // (that kernel plus the selection/commit kernel)
+    launch_hold(kHoldNs, c->stream);
     CK(cudaEventRecord(c->kev0, c->stream));
     launch_mixed_main(c->kp, c->f, 0, c->stream);
     if (which == 0) CK(cudaEventRecord(c->kev1, c->stream));
@@ -1294,7 +1300,7 @@ extern "C" int stz_kernel_time(stz_ctx* c, int32_t which, double* ms_avg, int64_
     tot += ms;
     n++;
   }
-  c->launches += kMixedLaunches * steps;
+  c->launches += (kMixedLaunches + 1) * steps;
   *ms_avg = n ? tot / n : 0;
   if (launches) *launches = n;
   return STZ_OK;

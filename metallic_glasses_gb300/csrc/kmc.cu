@@ -2557,6 +2557,20 @@ __global__ void k_l2_flush(uint4* buf, long long n, unsigned v) {
     buf[i] = make_uint4(v, v + 1, v + 2, (unsigned)i);
 }
 
+// Keeps the stream busy for about `ns` nanoseconds of the global timer: the
+// host has queued the launches behind it by the time it ends, so an event
+// recorded after it stamps the next kernel's start rather than the host's
+// launch latency. The loop is bounded by an iteration limit as well.
+__global__ void k_hold(unsigned long long ns) {
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (int i = 0; i < (1 << 20); i++) {
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 >= ns) break;
+    __nanosleep(256);
+  }
+}
+
 }  // namespace
 
 void launch_rate_fp64(const KParams& kp, const Fields& f, cudaStream_t st) {
@@ -2776,6 +2790,8 @@ void launch_fill_f32(const double* in, float* out, long long n, cudaStream_t st)
   const long long nb = std::min<long long>((n + 255) / 256, 4096);
   k_fill_f32<<<(unsigned)nb, 256, 0, st>>>(in, out, n);
 }
+
+void launch_hold(unsigned long long ns, cudaStream_t st) { k_hold<<<1, 32, 0, st>>>(ns); }
 
 void launch_l2_flush(void* buf, size_t bytes, cudaStream_t st) {
   const long long n = (long long)(bytes / sizeof(uint4));

@@ -73,5 +73,8 @@ constexpr int kInhomBlocks = 608;
 void launch_inhom_init(const KParams& kp, const Fields& f, const double* ebar, cudaStream_t st);
 void launch_inhom_update(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_l2_flush(void* buf, size_t bytes, cudaStream_t st);
+// One-warp kernel that keeps the stream busy for about ns nanoseconds, so the
+// launches queued behind it start back to back (kernel timing).
+void launch_hold(unsigned long long ns, cudaStream_t st);
 
 }  // namespace stz
