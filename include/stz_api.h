@@ -136,9 +136,22 @@ typedef struct stz_params {
   int32_t softening;         /* input "Softening Flag" */
   int32_t sf_scheme;         /* STZ_SF_* */
   double  perm_soft, temp_soft, perm_soft_cap, t_temp;
-  /* crystal-like MRO inputs (init.c:345-437). Only an all-glass map is run. */
-  double  xmro_frac, xq0amp, random_ratio;
-  int32_t init_mro;
+  /* crystal-like MRO sites of STZ_MODEL_REF2D (init.c:345-437, elastic.c:61-137 and
+   * 361-520, ActEnergy under NO_SF_XTAL_MRO init.c:645-660) */
+  double  xmro_frac;         /* init_mro 0: share of six-fold sites ("Volume fraction of
+                                crystal-like MRO") */
+  double  xq0amp;            /* barrier of a crystal-like site after it transforms */
+  double  random_ratio;      /* "Random ratio of fluctuation in energy barrier" */
+  int32_t init_mro;          /* 0: the map is drawn; 1: the map is mro_type/mro_theta
+                                (the reference's MROstructure.ms) */
+  int32_t no_sf_xtal_mro;    /* bmgFlags.h NO_SF_XTAL_MRO (on as shipped): the barriers of a
+                                crystal-like site soften less (init.c:645-660) */
+  double  perm_soft_mro, temp_soft_mro; /* a six-fold site's PermSoftmro, TempSoftmro
+                                (init.c:61-63) */
+  const int32_t* mro_type;   /* init_mro 1: host array of N types (0 glass, 1 six-fold,
+                                2 two-fold, 3 ten-fold) in site order, read by stz_create
+                                only; NULL otherwise */
+  const double*  mro_theta;  /* init_mro 1: host array of N angles (MROthe0), as above */
   /* bookkeeping */
   int32_t print_period;      /* reference "Print period" */
   uint64_t seed;             /* MT19937 seed; 0 maps to 4357 as GSL does */
@@ -228,10 +241,13 @@ enum {
                                 (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, sqrt2 yz,
                                 sqrt2 xz, sqrt2 xy (pending update applied first) */
   STZ_FIELD_LAMBDA = 10,     /* plain forms: the Lame moduli of each site (Lambda, Mu of   */
-  STZ_FIELD_MU = 11          /* init.c:456-465; the params' lambda, mu until set). Once either
+  STZ_FIELD_MU = 11,         /* init.c:456-465; the params' lambda, mu until set). Once either
                                 varies, every stress solve is the reference's polarisation
                                 fixed point (InhomogeneousStressSolver, elastic.c:977-1066)
                                 with the params' moduli as the reference medium */
+  STZ_FIELD_MRO = 12         /* REF2D crystal-like MRO map (read only): comp 0 the type of
+                                each site (0 glass, 1 six-fold, 2 two-fold, 3 ten-fold),
+                                comp 1 its angle MROthe0 */
 };
 
 typedef struct stz_ctx stz_ctx;

@@ -24,7 +24,7 @@ DF_TRUNC_NORMAL, DF_CORRELATED = 0, 1
 XX, YY, ZZ, YZ, XZ, XY = range(6)
 EV_THERMAL, EV_ATHERMAL, EV_ELASTIC = 0, 1, 2
 FIELD_SIGMA, FIELD_EPS0, FIELD_DF, FIELD_DEPS, FIELD_TLAST, FIELD_PERM_SOFT, FIELD_TEMP_SOFT, \
-    FIELD_PREV_DEPS, FIELD_Q, FIELD_SDEV, FIELD_LAMBDA, FIELD_MU = range(12)
+    FIELD_PREV_DEPS, FIELD_Q, FIELD_SDEV, FIELD_LAMBDA, FIELD_MU, FIELD_MRO = range(13)
 
 
 class Params(C.Structure):
@@ -41,12 +41,30 @@ class Params(C.Structure):
         ("softening", C.c_int32), ("sf_scheme", C.c_int32),
         ("perm_soft", C.c_double), ("temp_soft", C.c_double), ("perm_soft_cap", C.c_double), ("t_temp", C.c_double),
         ("xmro_frac", C.c_double), ("xq0amp", C.c_double), ("random_ratio", C.c_double),
-        ("init_mro", C.c_int32), ("print_period", C.c_int32), ("seed", C.c_uint64),
+        ("init_mro", C.c_int32), ("no_sf_xtal_mro", C.c_int32), ("perm_soft_mro", C.c_double), ("temp_soft_mro", C.c_double),
+        ("mro_type", C.POINTER(C.c_int32)), ("mro_theta", C.POINTER(C.c_double)),
+        ("print_period", C.c_int32), ("seed", C.c_uint64),
         ("precision", C.c_int32), ("solver", C.c_int32), ("resolve_period", C.c_int32), ("device", C.c_int32),
         ("log_capacity", C.c_int32), ("mode_seed_set", C.c_int32), ("mode_seed", C.c_int32),
         ("resolve_fp64", C.c_int32), ("sel_slack_shift", C.c_int32),
         ("main_pass_general", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
+
+
+def set_mro_map(p, types, theta):
+    """Give a REF2D Params the crystal-like MRO map of the reference's
+    MROstructure.ms (init_mro 1): a type (0 glass, 1 six-fold, 2 two-fold,
+    3 ten-fold) and an angle per site in site order. The arrays stay referenced
+    by the Params object; the context reads them when it is created."""
+    t = np.ascontiguousarray(types, dtype=np.int32)
+    th = np.ascontiguousarray(theta, dtype=np.float64)
+    if t.shape != th.shape or t.ndim != 1:
+        raise ValueError("types and angles must be 1-D arrays of one length")
+    p._mro_keep = (t, th)
+    p.init_mro = 1
+    p.mro_type = t.ctypes.data_as(C.POINTER(C.c_int32))
+    p.mro_theta = th.ctypes.data_as(C.POINTER(C.c_double))
+    return p
 
 
 class Event(C.Structure):

@@ -1,7 +1,8 @@
 """Workload configurations.
 
 ref2d(...)      the reference's own 2D model, built from a reference-format
-                input file (labels of io.c:4-101) at a chosen grid
+                input file (labels of io.c:4-101) at a chosen grid, with the
+                text of an MROstructure.ms file when its input reads one
 stress32()      32^3, FP64, constant applied pure shear stress 1 GPa, seed 0
 shear64(seed)   64^3, FP64, shear strain rate, seeds 0-3
 mixed128()      128^3, mixed form, periodic full re-solve every 1000 events
@@ -64,8 +65,28 @@ def write_input(path, **overrides):
     return path
 
 
+def read_mro_structure(text, nx, ny):
+    """The crystal-like MRO map of a structure file in the reference's
+    MROstructure.ms layout (init.c:398-420): one line per site in site order,
+    "i j type angle" with 1-based i (slow axis) and j. Returns (types, angles);
+    a line whose indices do not match its position raises ValueError, as the
+    reference aborts."""
+    rows = [ln.split() for ln in text.splitlines() if ln.strip()]
+    if len(rows) < nx * ny:
+        raise ValueError("structure file has %d lines for %d sites" % (len(rows), nx * ny))
+    types = np.zeros(nx * ny, np.int32)
+    theta = np.zeros(nx * ny, np.float64)
+    for m in range(nx * ny):
+        ii, jj, t, th = rows[m][:4]
+        if (int(ii) - 1) * ny + int(jj) - 1 != m:
+            raise ValueError("structure file line %d: inconsistent index" % (m + 1))
+        types[m] = int(t)
+        theta[m] = float(th)
+    return types, theta
+
+
 def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None, from_input=None,
-          **overrides):
+          mro_structure=None, **overrides):
     p = (defaults or api.default_params)(api.MODEL_REF2D)
     if input_path is None:
         import tempfile
@@ -74,6 +95,8 @@ def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None
     (from_input or api.params_from_input)(input_path, p)
     p.n[0], p.n[1], p.n[2] = 1, nx, ny
     p.loading = loading
+    if mro_structure is not None:
+        api.set_mro_map(p, *read_mro_structure(mro_structure, nx, ny))
     return p
 
 

@@ -109,26 +109,61 @@ int upload(void* d, const void* h, size_t bytes, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------- initial state
+// Crystal-like MRO types 0 glass, 1 six-fold, 2 two-fold, 3 ten-fold: the
+// amplitude of mode 0 in units of gamma0 (elastic.c:68-112) and the number of
+// slip modes (XMODES_SIX/TWO/TEN, bmg.h:30-32; the site's other modes carry no
+// eigenstrain). The reference's PI (bmg.h:74) sets the angles.
+constexpr double kMroAmp[4] = {0.0, 0.5, 0.8, 0.5};
+constexpr int kMroModes[4] = {0, 6, 2, 12};
+constexpr double kRefPi = 3.14159265359;
+
+// the rotation jitter 1 + 0.2 (2u - 1) of a crystal-like site's modes
+double mro_jitter(MT* rng) { return 1. + 0.2 * (2 * mt_uniform(rng) - 1.); }
+
 int init_ref2d(stz_ctx* c, MT* rng) {
   const stz_params& p = c->p;
   const long long N = c->kp.N;
-  // Alloc(): MRO map (init.c:350-397), Energy_Init (init.c:181-198),
-  // DStrain glass branch (elastic.c:126-130); draw order is the reference's.
-  if (p.init_mro != 0) {
-    set_error("MRO initialisation from a structure file is not supported");
-    return STZ_ERR_UNSUPPORTED;
-  }
+  // Alloc(): the MRO map (init.c:350-437). InitMRO 0: one uniform per site,
+  // at or below xMROFrac a six-fold site with a second uniform for its angle
+  // in [-PI/2, PI/2). InitMRO 1: the caller's types and angles (the
+  // structure file), then one uniform per ten-fold site, below 0.5 making it
+  // two-fold. Then Energy_Init (init.c:181-198) and DStrain (elastic.c:61-137);
+  // the draw order is the reference's.
+  std::vector<int8_t> ty((size_t)N, 0);
+  std::vector<double> th((size_t)N, 0.0);
   bool any_mro = false;
-  for (long long s = 0; s < N; s++) {
-    const double tmp = mt_uniform(rng);
-    if (tmp <= p.xmro_frac) {
-      any_mro = true;
-      (void)mt_uniform(rng);
+  if (p.init_mro == 0) {
+    for (long long s = 0; s < N; s++) {
+      const double tmp = mt_uniform(rng);
+      if (tmp <= p.xmro_frac) {
+        any_mro = true;
+        ty[s] = 1;
+        th[s] = mt_uniform(rng) * kRefPi - kRefPi / 2.0;
+      }
     }
-  }
-  if (any_mro) {
-    set_error("crystal-like MRO sites were drawn; only all-glass maps are supported");
-    return STZ_ERR_UNSUPPORTED;
+  } else if (p.init_mro == 1) {
+    if (!p.mro_type || !p.mro_theta) {
+      set_error("init_mro 1 needs the map (mro_type, mro_theta)");
+      return STZ_ERR_INVALID;
+    }
+    for (long long s = 0; s < N; s++) {
+      const int32_t v = p.mro_type[s];
+      if (v < 0 || v > 3) {
+        set_error("MRO type %d at site %lld (only 0..3 are allowed)", (int)v, s);
+        return STZ_ERR_INVALID;
+      }
+      ty[s] = (int8_t)v;
+      th[s] = p.mro_theta[s];
+      any_mro = any_mro || v != 0;
+    }
+    for (long long s = 0; s < N; s++)
+      if (ty[s] == 3) {
+        const double tmp = mt_uniform(rng);
+        if (tmp < 0.5) ty[s] = 2;
+      }
+  } else {
+    set_error("init_mro %d (0: drawn map, 1: given map)", (int)p.init_mro);
+    return STZ_ERR_INVALID;
   }
   std::vector<double> Q0((size_t)STZ_MODES * N), deps((size_t)STZ_MODES * 3 * N);
   for (int m = 0; m < STZ_MODES; m++)
@@ -136,11 +171,40 @@ int init_ref2d(stz_ctx* c, MT* rng) {
   for (int m = 0; m < STZ_MODES; m++)
     for (long long s = 0; s < N; s++) {
       double* d = deps.data() + (size_t)m * 3 * N;
-      d[s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
-      d[N + s] = -d[s];
-      d[2 * N + s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
+      const int t = ty[s];
+      if (t == 0) {
+        d[s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
+        d[N + s] = -d[s];
+        d[2 * N + s] = 0.5 * p.gamma0 * mt_gaussian(rng, 1.0);
+      } else if (m == 0) {
+        d[s] = kMroAmp[t] * p.gamma0 * std::cos(th[s]);
+        d[N + s] = -d[s];
+        d[2 * N + s] = kMroAmp[t] * p.gamma0 * std::sin(th[s]);
+      } else if (m < kMroModes[t]) {
+        // mode 0 rotated by m 2PI/X; angle and the two terms of each
+        // component jittered, the left term's draw first
+        const double a0 = deps[s], a2 = deps[2 * N + s];
+        const double tt = m * 2. * kRefPi / kMroModes[t] * mro_jitter(rng);
+        const double j1 = mro_jitter(rng), j2 = mro_jitter(rng);
+        d[s] = a0 * j1 * std::cos(2 * tt) + a2 * j2 * std::sin(2 * tt);
+        d[N + s] = -d[s];
+        const double j3 = mro_jitter(rng), j4 = mro_jitter(rng);
+        d[2 * N + s] = -a0 * j3 * std::sin(2 * tt) + a2 * j4 * std::cos(2 * tt);
+      } else {
+        d[s] = d[N + s] = d[2 * N + s] = 0.0;
+      }
     }
   int st;
+  c->mro_h = ty;
+  c->mro_theta_h = th;
+  if (any_mro) {
+    if ((st = dalloc(&c->f.mro, (size_t)N))) return st;
+    if ((st = upload(c->f.mro, ty.data(), (size_t)N, c->stream))) return st;
+    // crystal-like sites draw new barriers when they transform; each print
+    // restores the initial ones
+    if ((st = dalloc(&c->f.Q1, Q0.size()))) return st;
+    if ((st = upload(c->f.Q1, Q0.data(), sizeof(double) * Q0.size(), c->stream))) return st;
+  }
   if ((st = upload(c->f.Q0, Q0.data(), sizeof(double) * Q0.size(), c->stream))) return st;
   if ((st = upload(c->f.deps, deps.data(), sizeof(double) * deps.size(), c->stream))) return st;
   launch_mode_norms(c->kp, c->f, c->stream);
@@ -392,6 +456,10 @@ void enqueue_plain_step(stz_ctx* c, cudaEvent_t t0 = nullptr, cudaEvent_t t1 = n
   solve_plain(c, gate, ebar);
   launch_post_a(kp, f, c->stream);
   solve_plain(c, gate, ebar);
+  if (f.Q1) {
+    launch_q0_reset(kp, f, c->stream);
+    c->launches += 1;
+  }
   launch_post_b(kp, f, c->stream);
   c->launches += 1 + 2 + 2 + 1;
 }
@@ -560,6 +628,10 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   }
   if (!(p.mu > 0) || !(p.temperature > 0)) { set_error("mu and temperature must be positive"); return STZ_ERR_INVALID; }
   if (!ref2d && p.softening) { set_error("softening is implemented for the reference 2D model only"); return STZ_ERR_UNSUPPORTED; }
+  if (!ref2d && (p.xmro_frac > 0 || p.init_mro != 0)) {
+    set_error("crystal-like MRO sites belong to the reference 2D model");
+    return STZ_ERR_UNSUPPORTED;
+  }
   const bool mixed = p.precision == STZ_PREC_MIXED;
   if (mixed && ref2d) { set_error("the mixed form is implemented for the 3D model"); return STZ_ERR_UNSUPPORTED; }
   if (mixed && (p.n[2] % 4 || p.n[2] > 512 || p.n[1] > 512)) {
@@ -639,6 +711,9 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   kp.dt = p.strain_rate > 0 ? p.strain_increment / p.strain_rate : INFINITY;
   kp.gamma0 = p.gamma0;
   kp.perm_soft = p.perm_soft; kp.temp_soft = p.temp_soft; kp.perm_soft_cap = p.perm_soft_cap; kp.t_temp = p.t_temp;
+  kp.perm_soft_mro = p.perm_soft_mro; kp.temp_soft_mro = p.temp_soft_mro;
+  kp.no_sf_xtal_mro = p.no_sf_xtal_mro;
+  kp.xq0amp = p.xq0amp; kp.random_ratio = p.random_ratio;
   kp.end_strain = p.end_strain;
   kp.strain_rate = p.strain_rate;
   kp.strain_increment = p.strain_increment;
@@ -761,7 +836,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   cudaSetDevice(c->p.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
-  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.deps, f.dnorm, f.prev_deps, f.perm_soft, f.temp_soft,
+  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.Q1, f.deps, f.dnorm, f.mro, f.prev_deps, f.perm_soft, f.temp_soft,
                   f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.lbnd, f.psum, f.spec, f.ktab, f.log,
                   f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf, f.lam_site, f.mu_site,
                   f.inh_tau0, f.inh_eeff, f.inh_last, f.inh_part};
@@ -927,6 +1002,12 @@ extern "C" int stz_get_field(stz_ctx* c, int32_t which, int32_t comp, double* ho
   if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
   const long long N = c->kp.N;
+  if (which == STZ_FIELD_MRO) {
+    if (c->kp.model != STZ_MODEL_REF2D || comp < 0 || comp > 1 || (long long)c->mro_h.size() != N)
+      return STZ_ERR_INVALID;
+    for (long long s = 0; s < N; s++) host[s] = comp == 0 ? (double)c->mro_h[(size_t)s] : c->mro_theta_h[(size_t)s];
+    return STZ_OK;
+  }
   if (which == STZ_FIELD_LAMBDA || which == STZ_FIELD_MU) {
     if (comp != 0) return STZ_ERR_INVALID;
     const std::vector<double>& h = which == STZ_FIELD_LAMBDA ? c->lam_h : c->mu_h;
@@ -1061,7 +1142,7 @@ static int ensure_moduli(stz_ctx* c) {
 }
 
 extern "C" int stz_set_field(stz_ctx* c, int32_t which, int32_t comp, const double* host, int64_t count) {
-  if (!c || !host || count != c->kp.N) return STZ_ERR_INVALID;
+  if (!c || !host || count != c->kp.N || which == STZ_FIELD_MRO) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
   if (which == STZ_FIELD_LAMBDA || which == STZ_FIELD_MU) {
     // the mixed form's response table assumes one uniform medium

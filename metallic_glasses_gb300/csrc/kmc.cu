@@ -319,10 +319,14 @@ __device__ __forceinline__ double dire_modifier(int scheme, double dot, double n
   }
 }
 
-// REF2D: site data shared by the 20 modes
+// REF2D: site data shared by the 20 modes; ft is the factor NO_SF_XTAL_MRO
+// applies at a crystal-like site (init.c:645-660), 0 at a glass site
 struct R2Site {
-  double sg[3], pd[3], n2, soft;
+  double sg[3], pd[3], n2, soft, ft;
 };
+
+// the factor of MRO type 1 (six-fold), 2 (two-fold), 3 (ten-fold)
+__device__ __forceinline__ double mro_factor(int t) { return t == 1 ? 0.1 : (t == 2 ? 0.01 : 0.9); }
 
 __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, const double* u, double totime,
                                           long long s) {
@@ -339,6 +343,8 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
   d.soft = kp.softening ? (ts != 0.0 ? f.perm_soft[s] + ts * exp((f.tlast[s] - totime) / kp.t_temp)
                                      : f.perm_soft[s])
                         : 0.0;
+  const int t = (f.mro && kp.no_sf_xtal_mro) ? f.mro[s] : 0;
+  d.ft = t ? mro_factor(t) : 0.0;
   return d;
 }
 
@@ -363,8 +369,16 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
   if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
   const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
   const double n1 = f.dnorm[(long long)m * N + s];
-  const double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
-  return f.Q0[(long long)m * N + s] * exp(-DM * d.soft) - DWork / 2;
+  double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
+  double soft = d.soft;
+  if (d.ft != 0.0) {
+    // a crystal-like site: the reference scales the direction modifier and,
+    // in place, the site's softening by the factor for every mode in turn,
+    // so mode m sees the softening times the factor m + 1 times
+    DM = __dmul_rn(DM, d.ft);
+    for (int k = 0; k <= m; k++) soft = __dmul_rn(soft, d.ft);
+  }
+  return f.Q0[(long long)m * N + s] * exp(-DM * soft) - DWork / 2;
 }
 
 // GLOBAL3D FP64: Q = dF - W/2 with W = sigma:deps_m
@@ -752,12 +766,23 @@ __device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, 
     ctl->eps0_sum[c] += d[c];
   }
   if (MODEL == 0) {
+    const int ty = f.mro ? f.mro[s] : 0;
     const double ds = d[0] * d[0] + d[1] * d[1] + 2 * d[2] * d[2];
-    double ps = f.perm_soft[s] + ds * kp.perm_soft;
+    double ps = f.perm_soft[s] + ds * (ty == 1 ? kp.perm_soft_mro : kp.perm_soft);
     if (ps > kp.perm_soft_cap) ps = kp.perm_soft_cap;
     f.perm_soft[s] = ps;
-    f.temp_soft[s] = ds * kp.temp_soft;
+    f.temp_soft[s] = ds * (ty == 1 ? kp.temp_soft_mro : kp.temp_soft);
     f.tlast[s] = ctl->totime;
+    if (ty) {
+      // a crystal-like site keeps its modes and draws new barriers
+      // xQ0amp (1 - RandomRatio + RandomRatio u) (elastic.c:451-500)
+      for (int i = 0; i < STZ_MODES; i++) {
+        const double u = mt_uniform(rng);
+        f.Q0[(long long)i * N + s] =
+            __dmul_rn(kp.xq0amp, __dadd_rn(1.0 - kp.random_ratio, __dmul_rn(kp.random_ratio, u)));
+      }
+      return;
+    }
     // re-draw the site's modes, glass branch (elastic.c:508-512)
     for (int i = 0; i < STZ_MODES; i++) {
       double* dd = f.deps + (long long)i * 3 * N;
@@ -1043,6 +1068,15 @@ __global__ void k_post_print(KParams kp, Fields f) {
   if (ctl->step_kind == kNone) return;
   ctl->print_done = print_check(kp, ctl);
   ctl->solve_req = ctl->print_done;
+}
+
+// The print's reset of the barriers to their initial copy (bmg.c:214-221),
+// when this step printed. Only REF2D grids with crystal-like sites have Q1.
+__global__ void k_q0_reset(KParams kp, Fields f) {
+  if (!f.ctl->print_done || f.ctl->step_kind == kNone) return;
+  const long long total = (long long)STZ_MODES * kp.N;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x)
+    f.Q0[i] = f.Q1[i];
 }
 
 // One block of TH threads, as k_post_a.
@@ -2755,6 +2789,12 @@ void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st) {
 }
 
 void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st) { k_post_b<<<1, TH, 0, st>>>(kp, f); }
+
+void launch_q0_reset(const KParams& kp, const Fields& f, cudaStream_t st) {
+  const long long total = (long long)STZ_MODES * kp.N;
+  const unsigned nb = (unsigned)std::min<long long>((total + TH - 1) / TH, 152LL * 8);
+  k_q0_reset<<<nb, TH, 0, st>>>(kp, f);
+}
 
 void launch_mixed_after_resolve(const KParams& kp, const Fields& f, int kind, cudaStream_t st) {
   k_mixed_after_resolve<<<1, 1, 0, st>>>(kp, f, kind);

@@ -55,6 +55,8 @@ void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t
 // after the optional print re-solve (stop checks, targets).
 void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st);
+// REF2D with crystal-like sites: restore the initial barriers when the step printed
+void launch_q0_reset(const KParams& kp, const Fields& f, cudaStream_t st);
 // Reset of the incremental state after a full re-solve (mixed form).
 // kind 0: field solved with the current mean strain (print / athermal);
 // kind 1: periodic re-solve with the applied mean strain (field unchanged).

@@ -31,6 +31,9 @@ extern "C" int stz_params_default(stz_params* p, int32_t model) {
   p->perm_soft = 13;
   p->temp_soft = 39;
   p->perm_soft_cap = -std::log(0.6);
+  p->perm_soft_mro = 20;  // PermSoftmro, TempSoftmro (init.c:61-63)
+  p->temp_soft_mro = 60;
+  p->no_sf_xtal_mro = 1;  // bmgFlags.h as shipped
   p->sf_scheme = STZ_SF_SQUARE_FWD;
   if (model == STZ_MODEL_REF2D) {
     // the reference's compile-time constants (bmg.h:23-94) and shipped input

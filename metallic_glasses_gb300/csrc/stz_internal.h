@@ -107,6 +107,9 @@ struct Fields {
   double* Q0 = nullptr;      // [MODES][N] (REF2D)
   double* deps = nullptr;    // [MODES][3][N] (REF2D)
   double* dnorm = nullptr;   // [MODES][N] |deps| of each mode (REF2D), kept with deps
+  int8_t* mro = nullptr;     // [N] crystal-like MRO type 0..3 (REF2D); null for an all-glass map
+  double* Q1 = nullptr;      // [MODES][N] the initial Q0, restored at every print (bmg.c:214-221);
+                             // only with crystal-like sites (glass sites never change Q0)
   double* prev_deps = nullptr;  // [nc][N]
   double* perm_soft = nullptr;
   double* temp_soft = nullptr;
@@ -148,10 +151,11 @@ struct KParams {
   int adv_q2, adv_r2;        // kRateThreads sites = adv_q2 rows of n2 plus adv_r2 sites
   int fast_inv;              // mixed form: precomputed compliance coefficients
   double inv_2mu, inv_lam_coef, invN, inv_a_scale;
-  int loading, softening, sf_scheme, no_subtract_error, shear_quirk;
+  int loading, softening, sf_scheme, no_subtract_error, shear_quirk, no_sf_xtal_mro;
   double lambda, mu, young, poisson;
   double kT, vt, V0, dt, gamma0;
   double perm_soft, temp_soft, perm_soft_cap, t_temp;
+  double perm_soft_mro, temp_soft_mro, xq0amp, random_ratio;  // crystal-like MRO sites (REF2D)
   double end_strain, strain_rate, strain_increment, print_thr;
   double applied[6];
   double modes[STZ_MODES][6];      // GLOBAL3D mode table (Voigt, tensor shear)
@@ -213,6 +217,8 @@ struct stz_ctx {
   int use_graph = 1;
   int inhom = 0;                      // some site's moduli differ from the params' (plain forms)
   std::vector<double> lam_h, mu_h;    // host copies of the site moduli (empty until set)
+  std::vector<int8_t> mro_h;          // REF2D crystal-like MRO map (types) and its angles
+  std::vector<double> mro_theta_h;
   cudaGraphExec_t graph = nullptr;
   int graph_batch = 0;
   int64_t graph_launches = 0;        // kernels per graph launch

@@ -33,8 +33,13 @@
  * engine, whose solves (those of the steps too) then run the reference's
  * polarisation fixed point.
  *
+ * Crystal-like MRO sites (init.c:350-437): the engine draws the map (InitMRO
+ * 0) or takes the one Alloc reads from MROstructure.ms (InitMRO 1); Alloc
+ * fills MRO/MROthe0 from it and writes Initial_MROstructure, and actQ.out
+ * records the chosen site's MRO type, as the reference does.
+ *
  * Not provided: SOC counters (UpdateSOC leaves main's arrays as they are),
- * MRO maps, residual-stress generation.
+ * residual-stress generation.
  */
 #include <math.h>
 #include <stdio.h>
@@ -76,6 +81,9 @@
 static stz_ctx* g_ctx = NULL;
 static stz_params g_p;
 static int64_t g_events_seen = 0;  /* events already written to fq */
+static int g_any_mro = 0;          /* the map holds crystal-like sites */
+static real* g_q0_seen[MODES];     /* Q0 as RecordPrep read it from the device */
+static int g_q0_check = 0;         /* compare the Q0 mirror before the next step */
 static double g_epsavg_dev[3];     /* EpsAvg as last read from the device */
 
 static void fail(const char* what, int code) {
@@ -237,6 +245,44 @@ void Alloc(void) {
   g_p.xmro_frac = xMROFrac;
   g_p.init_mro = InitMRO;
   g_p.xq0amp = xQ0amp;
+  g_p.perm_soft_mro = PermSoftmro;
+  g_p.temp_soft_mro = TempSoftmro;
+#if defined(NO_SF_XTAL_MRO)
+  g_p.no_sf_xtal_mro = 1;
+#else
+  g_p.no_sf_xtal_mro = 0;
+#endif
+  MRO = (int*)calloc((size_t)NXY, sizeof(int));
+  MROthe0 = alloc_field();
+  int32_t* mro_in = NULL;
+  if (!MRO) fail("allocation", STZ_ERR_NOMEM);
+  if (InitMRO == 1) {
+    /* init.c:398-420: one "i j type angle" line per site of this rank's slab */
+    FILE* fp = fopen("MROstructure.ms", "r");
+    if (!fp) {
+      perror("MROstructure.ms");
+      MPI_Abort(MPI_COMM_WORLD, -1);
+    }
+    mro_in = (int32_t*)calloc((size_t)NXY, sizeof(int32_t));
+    if (!mro_in) fail("allocation", STZ_ERR_NOMEM);
+    char buffer[80] = {0};
+    for (int i = 0; i < lnx; i++)
+      for (int j = 0; j < NY; j++) {
+        const int m = i * NY + j;
+        int ii = 0, jj = 0, t = 0;
+        double th = 0;
+        if (!fgets(buffer, 80, fp) || sscanf(buffer, "%d %d %d %lf", &ii, &jj, &t, &th) != 4 ||
+            (ii - 1 - lxs) * NY + jj - 1 != m) {
+          perror("Error in reading MROstructure.ms file (inconsistent index system)!!\n");
+          MPI_Abort(MPI_COMM_WORLD, -1);
+        }
+        mro_in[m] = t;
+        MROthe0[m] = th;
+      }
+    fclose(fp);
+    g_p.mro_type = mro_in;
+    g_p.mro_theta = MROthe0;
+  }
 #if defined(TENSION)
   g_p.loading = STZ_LOAD_TENSION;
 #elif defined(SHEAR)
@@ -263,7 +309,23 @@ void Alloc(void) {
   g_p.log_capacity = 1 << 16;
   int st = stz_create(&g_p, &g_ctx);
   if (st) fail("stz_create", st);
+  free(mro_in);
+  g_p.mro_type = NULL;
+  g_p.mro_theta = NULL;
   g_events_seen = 0;
+  /* the map the engine holds (ten-fold sites of a structure file may have
+   * become two-fold), as init.c:437 writes it */
+  real* tmp = alloc_field();
+  pull_field(STZ_FIELD_MRO, 0, tmp);
+  for (int s = 0; s < NXY; s++) {
+    MRO[s] = (int)tmp[s];
+    g_any_mro |= MRO[s] != 0;
+  }
+  free(tmp);
+  if (g_any_mro)
+    for (int m = 0; m < MODES; m++) g_q0_seen[m] = alloc_field();
+  pull_field(STZ_FIELD_MRO, 1, MROthe0);
+  WriteMROMPI_INT(MRO, "Initial_MROstructure", 0);
 }
 
 /* init.c:181-198: the barriers the engine drew, and their initial copy Q1 */
@@ -385,9 +447,21 @@ void ActEnergy(int step_) {
   for (int m = 0; m < MODES; m++) pull_field(STZ_FIELD_Q, m, Q[m]);
 }
 
+/* Q0 modes that main changed since RecordPrep go to the device */
+static void sync_q0(void) {
+  if (!g_q0_check) return;
+  g_q0_check = 0;
+  for (int m = 0; m < MODES; m++)
+    if (memcmp(g_q0_seen[m], Q0[m], sizeof(real) * NXY) != 0) {
+      int st = stz_set_field(g_ctx, STZ_FIELD_DF, m, Q0[m], (int64_t)NXY);
+      if (st) fail("stz_set_field", st);
+    }
+}
+
 /* one driver step on the device, then the globals and the actQ.out records
  * of evolution.c:243 */
 static void one_step(void) {
+  sync_q0();
   int st = stz_run(g_ctx, 1, 0);
   if (st) fail("stz_run", st);
   pull_scalars();
@@ -399,7 +473,8 @@ static void one_step(void) {
     if (n <= 0) break;
     for (int64_t i = 0; i < n; i++)
       if (ev[i].kind == STZ_EV_THERMAL && rank == 0 && fq) {
-        fprintf(fq, "%d\t%.6e\n", ev[i].mode, ev[i].q);
+        /* evolution.c:206,243: the chosen site's MRO type and its Q */
+        fprintf(fq, "%d\t%.6e\n", MRO[ev[i].site], ev[i].q);
         fflush(fq);
       }
     g_events_seen += n;
@@ -427,6 +502,17 @@ void RecordPrep(void) {
   for (int c = 0; c < DE; c++) {
     pull_field(STZ_FIELD_EPS0, c, Eps0[c]);
     pull_field(STZ_FIELD_SIGMA, c, Sigma[c]);
+  }
+  /* the reference's main resets Q0 to Q1 right after RecordPrep in its print
+   * block (bmg.c:214-221). Crystal-like sites change Q0 when they transform,
+   * so the mirror is brought up to date here and what main writes to it is
+   * passed to the device before the next step (sync_q0). */
+  if (g_any_mro) {
+    for (int m = 0; m < MODES; m++) {
+      pull_field(STZ_FIELD_DF, m, Q0[m]);
+      memcpy(g_q0_seen[m], Q0[m], sizeof(real) * NXY);
+    }
+    g_q0_check = 1;
   }
   EqStrain = (real*)malloc((size_t)lsize * sizeof(real));
   EqStress = (real*)malloc((size_t)lsize * sizeof(real));
@@ -523,6 +609,16 @@ void Free(void) {
   free(PermSoftening);
   free(TempSoftening);
   free(Softening);
+  free(MRO);
+  free(MROthe0);
+  MRO = NULL;
+  MROthe0 = NULL;
+  for (int m = 0; m < MODES; m++) {
+    free(g_q0_seen[m]);
+    g_q0_seen[m] = NULL;
+  }
+  g_any_mro = 0;
+  g_q0_check = 0;
 #ifdef INHOM_ELAST
   free(Lambda);
   free(Mu);

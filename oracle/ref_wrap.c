@@ -11,7 +11,8 @@
  *                       per driver step (kind 0 thermal, 1 athermal, 2 elastic)
  *   STZ_REF_MAX_EVENTS  stop once this many thermal events are done
  *   STZ_REF_MAX_STEPS   stop once this many driver steps are done
- *   STZ_REF_DUMP        binary dump of the final state, written at the start of
+ *   STZ_REF_DUMP        binary dump of the final state (fields, then the MRO
+ *                       map's types and angles), written at the start of
  *                       the step after the stop condition (i.e. after the
  *                       previous step's print/re-solve), or at Free() when the
  *                       reference stops on its own end condition
@@ -98,6 +99,12 @@ static void dump_state(long long steps_done) {
         double v = PreDEps0[PreSelectMode[s]][c][s];
         fwrite(&v, sizeof(double), 1, f);
       }
+    /* the crystal-like MRO map: types (as doubles) and angles */
+    for (int s = 0; s < lsize; s++) {
+      double v = (double)MRO[s];
+      fwrite(&v, sizeof(double), 1, f);
+    }
+    wr(f, MROthe0, sizeof(double), (size_t)lsize);
     fclose(f);
   }
   if (g_log) fflush(g_log);

@@ -236,6 +236,8 @@ struct or_model {
   double* Q0;            /* [MODES][N] */
   double* Q1;            /* [MODES][N] initial copy (bmg.c:221 reset) */
   double* deps;          /* [MODES][3][N] */
+  int8_t* mro;           /* [N] crystal-like MRO type 0..3, NULL for an all-glass map */
+  double* mro_theta;     /* [N] MROthe0 */
   /* GLOBAL3D */
   double* dF;            /* [N] */
   double modes[STZ_MODES][6];
@@ -309,34 +311,98 @@ static void iso_inv(const or_model* m, const double* s, double* e) {
 }
 
 /* ------------------------------------------------------------- initialise */
+/* Crystal-like MRO types: 0 glass, 1 six-fold, 2 two-fold, 3 ten-fold. Per
+ * type: the amplitude of mode 0 in units of gamma0 (elastic.c:68-112), the
+ * number of slip modes (XMODES_SIX/TWO/TEN, bmg.h:30-32; the other modes have
+ * no eigenstrain) and the factor NO_SF_XTAL_MRO applies to the direction
+ * modifier and to the softening in ActEnergy (init.c:645-660). */
+static const double kMroAmp[4] = {0.0, 0.5, 0.8, 0.5};
+static const int kMroModes[4] = {0, 6, 2, 12};
+static const double kMroFactor[4] = {1.0, 0.1, 0.01, 0.9};
+#define OR_PI 3.14159265359 /* the reference's PI, bmg.h:74 */
+
+/* a factor 1 + 0.2 (2u - 1) of the MRO mode rotation (elastic.c:72-79) */
+static double mro_jitter(or_model* m) { return 1. + 0.2 * (2 * or_rng_uniform(&m->rng) - 1.); }
+
 static int init_ref2d(or_model* m) {
   long N = m->N;
-  /* Alloc(): MRO map, one uniform per site, plus one for the angle of a
-   * crystal-like site (init.c:350-397). Only all-glass maps are run. */
-  if (m->p.init_mro != 0) return STZ_ERR_UNSUPPORTED;
+  /* Alloc(): the MRO map (init.c:350-437). InitMRO 0: one uniform per site;
+   * a site at or below xMROFrac is six-fold with an angle uniform on
+   * [-PI/2, PI/2) (a second uniform). InitMRO 1: the types and angles of a
+   * structure file, then one uniform per ten-fold site, below 0.5 making it
+   * two-fold. */
   int any_mro = 0;
-  for (long s = 0; s < N; s++) {
-    double tmp = or_rng_uniform(&m->rng);
-    if (tmp <= m->p.xmro_frac) {
-      any_mro = 1;
-      (void)or_rng_uniform(&m->rng);
+  int8_t* t = (int8_t*)calloc((size_t)N, 1);
+  double* th = (double*)calloc((size_t)N, sizeof(double));
+  if (m->p.init_mro == 0) {
+    for (long s = 0; s < N; s++) {
+      double tmp = or_rng_uniform(&m->rng);
+      if (tmp <= m->p.xmro_frac) {
+        any_mro = 1;
+        t[s] = 1;
+        th[s] = or_rng_uniform(&m->rng) * OR_PI - OR_PI / 2.0;
+      }
     }
+  } else if (m->p.init_mro == 1) {
+    if (!m->p.mro_type || !m->p.mro_theta) { free(t); free(th); return STZ_ERR_INVALID; }
+    for (long s = 0; s < N; s++) {
+      int32_t v = m->p.mro_type[s];
+      if (v < 0 || v > 3) { free(t); free(th); return STZ_ERR_INVALID; }
+      t[s] = (int8_t)v;
+      th[s] = m->p.mro_theta[s];
+      any_mro |= v != 0;
+    }
+    for (long s = 0; s < N; s++)
+      if (t[s] == 3) {
+        double tmp = or_rng_uniform(&m->rng);
+        if (tmp < 0.5) t[s] = 2;
+      }
+  } else {
+    free(t); free(th);
+    return STZ_ERR_INVALID;
   }
-  if (any_mro) return STZ_ERR_UNSUPPORTED;
-  /* Energy_Init (init.c:181-198): Q0 = N(0, 0.25) + Q0amp, mode-major. */
+  m->mro_theta = th;
+  if (any_mro) m->mro = t;
+  else free(t);
+  /* Energy_Init (init.c:181-198): Q0 = N(0, 0.25) + Q0amp, mode-major, every
+   * site (its MRO branch is commented out in the reference). */
   for (int mo = 0; mo < STZ_MODES; mo++)
     for (long s = 0; s < N; s++) {
       double q = or_ran_gaussian(&m->rng, m->p.q0_sd) + m->p.q0_mean;
       m->Q0[mo * N + s] = q;
       m->Q1[mo * N + s] = q;
     }
-  /* DStrain, glass branch (elastic.c:126-130), mode-major. */
+  /* DStrain (elastic.c:61-137), mode-major. Glass: two normal draws. MRO:
+   * mode 0 along the site's angle; modes 1..X-1 that increment rotated by
+   * m 2PI/X, angle and the two terms of each component jittered by
+   * 1 + 0.2 (2u - 1) (five uniforms, taken in the order the reference's
+   * expressions evaluate them when built with gcc: left term first); the
+   * other modes zero. */
   for (int mo = 0; mo < STZ_MODES; mo++)
     for (long s = 0; s < N; s++) {
       double* d = m->deps + (size_t)mo * 3 * N;
-      d[0 * N + s] = 0.5 * m->p.gamma0 * or_ran_gaussian(&m->rng, 1.0);
-      d[1 * N + s] = -d[0 * N + s];
-      d[2 * N + s] = 0.5 * m->p.gamma0 * or_ran_gaussian(&m->rng, 1.0);
+      int ty = m->mro ? m->mro[s] : 0;
+      if (ty == 0) {
+        d[0 * N + s] = 0.5 * m->p.gamma0 * or_ran_gaussian(&m->rng, 1.0);
+        d[1 * N + s] = -d[0 * N + s];
+        d[2 * N + s] = 0.5 * m->p.gamma0 * or_ran_gaussian(&m->rng, 1.0);
+      } else if (mo == 0) {
+        d[0 * N + s] = kMroAmp[ty] * m->p.gamma0 * cos(th[s]);
+        d[1 * N + s] = -d[0 * N + s];
+        d[2 * N + s] = kMroAmp[ty] * m->p.gamma0 * sin(th[s]);
+      } else if (mo < kMroModes[ty]) {
+        const double a0 = m->deps[s], a2 = m->deps[2 * N + s];  /* mode 0 of the site */
+        double tt = mo * 2. * OR_PI / kMroModes[ty] * mro_jitter(m);
+        double j1 = mro_jitter(m), j2 = mro_jitter(m);
+        d[0 * N + s] = a0 * j1 * cos(2 * tt) + a2 * j2 * sin(2 * tt);
+        d[1 * N + s] = -d[0 * N + s];
+        double j3 = mro_jitter(m), j4 = mro_jitter(m);
+        d[2 * N + s] = -a0 * j3 * sin(2 * tt) + a2 * j4 * cos(2 * tt);
+      } else {
+        d[0 * N + s] = 0.0;
+        d[1 * N + s] = 0.0;
+        d[2 * N + s] = 0.0;
+      }
     }
   return STZ_OK;
 }
@@ -598,7 +664,10 @@ static double dire_modifier(int scheme, double dot, double n1, double n2) {
 }
 
 /* SofteningFactor (init.c:711-739, default branch) and ActEnergy
- * (init.c:561-690) with MICRO_MEMORY and NO_SF_XTAL_MRO on an all-glass map.
+ * (init.c:561-690) with MICRO_MEMORY and NO_SF_XTAL_MRO. At a crystal-like
+ * site the reference multiplies the direction modifier and, in place, the
+ * site's Softening by the type's factor for every mode in turn, so mode m sees
+ * the softening times the factor m + 1 times (each product rounded).
  * PreDEps0[PreSelectMode[s]][:][s] is kept as prev_deps[:][s]: VoxelShearTransform
  * copies every mode's DEps0 into PreDEps0 (elastic.c:369-374) and KMC then sets
  * PreSelectMode to the transformed mode (evolution.c:208), so ActEnergy only
@@ -618,6 +687,8 @@ static long act_energy(or_model* m) {
     for (int c = 0; c < nc; c++) { sg[c] = m->sigma[c][s]; pd[c] = m->prev_deps[c][s]; }
     double n2 = 0;
     if (is2d(m)) n2 = sqrt(pd[0] * pd[0] + pd[1] * pd[1] + 2 * pd[2] * pd[2]);
+    const int ty = (m->mro && m->p.no_sf_xtal_mro) ? m->mro[s] : 0;
+    double soft = m->softening[s];
     for (int mo = 0; mo < STZ_MODES; mo++) {
       double d[6], q0;
       if (is2d(m)) {
@@ -634,7 +705,11 @@ static long act_energy(or_model* m) {
         double dot = pd[0] * d[0] + pd[1] * d[1] + 2 * pd[2] * d[2];
         double n1 = sqrt(d[0] * d[0] + d[1] * d[1] + 2 * d[2] * d[2]);
         double DM = dire_modifier(m->p.sf_scheme, dot, n1, n2);
-        Q = q0 * exp(-DM * m->softening[s]) - DWork / 2;
+        if (ty) {
+          DM *= kMroFactor[ty];
+          soft *= kMroFactor[ty];
+        }
+        Q = q0 * exp(-DM * soft) - DWork / 2;
       } else {
         double w = 0;
         for (int c = 0; c < 6; c++) w += voigt_weight(m, c) * sg[c] * d[c];
@@ -649,7 +724,10 @@ static long act_energy(or_model* m) {
 }
 
 /* --------------------------------------------------------- transformation */
-/* VoxelShearTransform (elastic.c:361-520), glass sites. */
+/* VoxelShearTransform (elastic.c:361-520). Glass sites draw new mode
+ * eigenstrains; crystal-like sites keep theirs and draw new barriers
+ * xQ0amp (1 - RandomRatio + RandomRatio u), and a six-fold site softens with
+ * PermSoftmro and TempSoftmro. */
 static void voxel_transform(or_model* m, int mm, long s) {
   long N = m->N;
   int nc = m->nc;
@@ -667,11 +745,15 @@ static void voxel_transform(or_model* m, int mm, long s) {
   double ds = 0;
   for (int c = 0; c < nc; c++) ds += voigt_weight(m, c) * d[c] * d[c];
   if (is2d(m)) ds = d[0] * d[0] + d[1] * d[1] + 2 * d[2] * d[2];
-  m->perm_soft[s] += ds * m->p.perm_soft;
+  const int ty = m->mro ? m->mro[s] : 0;
+  m->perm_soft[s] += ds * (ty == 1 ? m->p.perm_soft_mro : m->p.perm_soft);
   if (m->perm_soft[s] > m->p.perm_soft_cap) m->perm_soft[s] = m->p.perm_soft_cap;
-  m->temp_soft[s] = ds * m->p.temp_soft;
+  m->temp_soft[s] = ds * (ty == 1 ? m->p.temp_soft_mro : m->p.temp_soft);
   m->tlast[s] = m->totime;
-  if (is2d(m)) {
+  if (ty) {
+    for (int i = 0; i < STZ_MODES; i++)
+      m->Q0[(size_t)i * N + s] = m->p.xq0amp * (1 - m->p.random_ratio + m->p.random_ratio * or_rng_uniform(&m->rng));
+  } else if (is2d(m)) {
     for (int i = 0; i < STZ_MODES; i++) {
       double* dd = m->deps + (size_t)i * 3 * N;
       dd[s] = 0.5 * m->p.gamma0 * or_ran_gaussian(&m->rng, 1.0);
@@ -1031,6 +1113,7 @@ void or_destroy(or_model* m) {
   for (int c = 0; c < 6; c++) { free(m->eps0[c]); free(m->sigma[c]); free(m->prev_deps[c]); }
   free(m->Q); free(m->rate); free(m->work); free(m->perm_soft); free(m->temp_soft);
   free(m->softening); free(m->tlast); free(m->Q0); free(m->Q1); free(m->deps); free(m->dF);
+  free(m->mro); free(m->mro_theta);
   free(m->log);
   free(m->force_site); free(m->force_mode); free(m->force_draws); free(m->force_check);
   free(m->line_cb);
@@ -1124,6 +1207,12 @@ static double* field_ptr(or_model* m, int which, int comp) {
 }
 
 int or_get_field(or_model* m, int which, int comp, double* out, int64_t count) {
+  if (which == STZ_FIELD_MRO) {
+    if (!is2d(m) || comp < 0 || comp > 1 || count != m->N) return STZ_ERR_INVALID;
+    for (long s = 0; s < m->N; s++)
+      out[s] = comp == 0 ? (m->mro ? (double)m->mro[s] : 0.0) : m->mro_theta[s];
+    return STZ_OK;
+  }
   if (which == STZ_FIELD_Q) act_energy(m);
   double* f = field_ptr(m, which, comp);
   if (!f || count != m->N) return STZ_ERR_INVALID;
@@ -1182,6 +1271,9 @@ int or_params_default(stz_params* p, int model) {
   p->perm_soft = 13;                       /* PermSoft, TempSoft, cap: init.c:62-68 */
   p->temp_soft = 39;
   p->perm_soft_cap = -log(0.6);
+  p->perm_soft_mro = 20;                   /* PermSoftmro, TempSoftmro: init.c:61-63 */
+  p->temp_soft_mro = 60;
+  p->no_sf_xtal_mro = 1;                   /* bmgFlags.h as shipped */
   p->print_period = 5;
   if (model == STZ_MODEL_REF2D) {
     /* bmg.h:23-94 and the shipped input file, through Init() under LOW_T */

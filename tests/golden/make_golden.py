@@ -20,6 +20,16 @@ directory and stores, per case:
                                    Sigma of the same prints as the reference's
                                    main writes them with FULL_TENSOR_RECORD
                                    (Strain_0c/Stress_0c_S%03d.iout, raw FP64)
+             cases with crystal-like MRO sites (MRO_CASES) also:
+               mro        int8 [N]   the MRO map (0 glass, 1 six-, 2 two-, 3 ten-fold)
+               theta      float64 [N] its angles MROthe0
+               mro_iout   int32 [N]  the reference's Initial_MROstructure_S000.iout
+               deps_mro   float64 [20, 3, M] the mode eigenstrains of the M
+                                   crystal-like sites (kept through transformations)
+               q0_mro     float64 [20, M] their barriers at the end
+               actq       float64 [K, 2] the reference's actQ.out (MRO type of
+                                   the chosen site, its Q), one row per thermal event
+               structure  (InitMRO 1 cases) the MROstructure.ms the run read
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
@@ -54,12 +64,35 @@ CASES = {
 # cases whose reference build also writes the .iout records of its prints
 IOUT_CASES = {"ref2d_32_tension_nosoft_s5"}
 
+# cases with crystal-like MRO sites: (nx, ny, loading, input overrides, thermal
+# events); initmro 1 cases read a structure file drawn by mro_structure()
+MRO_CASES = {
+    "ref2d_32_mro_s11": (32, 32, "TENSION", {"end": "0.5", "seed": "11", "xfrac": "0.15", "xq0": "1.8"}, 3000),
+    "ref2d_32_mrofile_s13": (32, 32, "TENSION", {"end": "0.5", "seed": "13", "initmro": "1", "xq0": "2.2"}, 3000),
+}
 
-def run_case(name, nx, ny, loading, overrides, events):
+
+def mro_structure(nx, ny, seed=2024):
+    """A structure file in the reference's MROstructure.ms layout (one line
+    per site in site order: 1-based i, 1-based j, type, angle): types 0/1/2/3
+    with probabilities 0.6/0.15/0.1/0.15, angles uniform on [-pi/2, pi/2)."""
+    rs = np.random.default_rng(seed)
+    t = rs.choice(4, size=nx * ny, p=[0.6, 0.15, 0.1, 0.15])
+    th = rs.uniform(-np.pi / 2, np.pi / 2, size=nx * ny)
+    lines = ["%d %d %d %.17g" % (i + 1, j + 1, t[i * ny + j], th[i * ny + j]) for i in range(nx) for j in range(ny)]
+    return "\n".join(lines) + "\n"
+
+
+def run_case(name, nx, ny, loading, overrides, events, mro=False):
     ftr = name in IOUT_CASES
     exe = build_ref2d(nx, ny, loading, full_tensor=ftr)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
+    structure = None
+    if overrides.get("initmro") == "1":
+        structure = mro_structure(nx, ny)
+        with open(os.path.join(d, "MROstructure.ms"), "w") as f:
+            f.write(structure)
     env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS=str(events),
                STZ_REF_DUMP=os.path.join(d, "dump.bin"))
     subprocess.run([exe], cwd=d, env=env, stdout=subprocess.DEVNULL, check=True)
@@ -86,10 +119,13 @@ def run_case(name, nx, ny, loading, overrides, events):
     sigma = take(3 * N).reshape(3, N)
     eps0 = take(3 * N).reshape(3, N)
     deps = take(60 * N).reshape(20, 3, N)
-    take(20 * N)  # Q0
+    q0 = take(20 * N).reshape(20, N)
     tlast = take(N)
     perm = take(N)
     temp = take(N)
+    take(3 * N)  # PreDEps0 of the last transformations
+    mro_map = take(N).astype(np.int8)
+    theta = take(N)
     # the reference main's print files X1R%03d_P00.out / X2R%03d_P00.out:
     # four prints spread over the run
     n_prints = 0
@@ -102,6 +138,13 @@ def run_case(name, nx, ny, loading, overrides, events):
     if ftr:
         extra["iout"] = np.array([[[np.fromfile(os.path.join(d, "%s_%02d_S%03d.iout" % (w, c + 1, k)), np.float64)
                                     for c in range(3)] for w in ("Strain", "Stress")] for k in xr_k])
+    if mro:
+        sel = np.nonzero(mro_map)[0]
+        extra.update(mro=mro_map, theta=theta, deps_mro=deps[:, :, sel], q0_mro=q0[:, sel],
+                     mro_iout=np.fromfile(os.path.join(d, "Initial_MROstructure_S000.iout"), np.int32),
+                     actq=np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2))
+        if structure is not None:
+            extra["structure"] = structure
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
@@ -173,3 +216,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev) in CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev)
+    for name, (nx, ny, loading, ov, ev) in MRO_CASES.items():
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev, mro=True)

@@ -1,12 +1,35 @@
 """Shared description of the reference-pinned 2D parity cases (tests/golden)."""
 import ast
 
+import numpy as np
+
 from metallic_glasses_gb300 import api, configs
 
 CASES = ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5", "ref2d_32_shear_stop_s7"]
 
 
-def params_for(g):
+MRO_CASES = ["ref2d_32_mro_s11", "ref2d_32_mrofile_s13"]
+
+
+def params_for(g, **kw):
     ov = ast.literal_eval(str(g["overrides"]))
     loading = api.LOAD_SHEAR if str(g["loading"]) == "SHEAR" else api.LOAD_TENSION
-    return configs.ref2d(int(g["nx"]), int(g["ny"]), loading=loading, **ov)
+    structure = str(g["structure"]) if "structure" in g.files else None
+    return configs.ref2d(int(g["nx"]), int(g["ny"]), loading=loading, mro_structure=structure, **kw, **ov)
+
+
+def check_mro_state(m, g, exact=True):
+    """The crystal-like sites of an MRO fixture: the map and angles, their
+    mode eigenstrains (drawn at the start and kept) and their barriers at the
+    end (new ones drawn at each of their transformations)."""
+    assert np.array_equal(m.field(api.FIELD_MRO, 0).astype(np.int8), g["mro"])
+    assert np.array_equal(m.field(api.FIELD_MRO, 1), g["theta"])
+    sel = np.nonzero(g["mro"])[0]
+    deps = np.stack([m.field(api.FIELD_DEPS, k) for k in range(60)]).reshape(20, 3, -1)[:, :, sel]
+    q0 = np.stack([m.field(api.FIELD_DF, k) for k in range(20)])[:, sel]
+    if exact:
+        assert np.array_equal(deps, g["deps_mro"])
+        assert np.array_equal(q0, g["q0_mro"])
+    else:
+        assert np.abs(deps - g["deps_mro"]).max() <= 1e-15
+        assert np.abs(q0 - g["q0_mro"]).max() <= 1e-14

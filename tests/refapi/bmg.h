@@ -54,6 +54,7 @@ G(real PermSoft, 0); G(real PermSoftmro, 0); G(real TempSoft, 0); G(real TempSof
 G(real PermSofteningCap, 0);
 G(real* PermSoftening, 0); G(real* TempSoftening, 0); G(real* Softening, 0);
 G(real xQ0amp, 0); G(real xMROFrac, 0); G(int InitMRO, 0); G(real tTemp, 0); G(real tResi, 0);
+G(int* MRO, 0); G(real* MROthe0, 0);
 G(real strainrate, 0); G(real strainincrement, 0); G(real totime, 0); G(real dt, 0);
 G(real RandomRatio, 0); G(int printperiod, 0); G(real EndStrain, 0); G(real elEnergy, 0);
 G(real RelxTime, 0);

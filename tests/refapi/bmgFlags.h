@@ -1,7 +1,8 @@
 /* Test build flags for the reference-API driver: the configuration of the
  * 2D fixtures (tension loading, square-forward softening directions, the
  * low-temperature material branch, micro memory, the inhomogeneous-solver
- * entry point). Written for the tests; the names are the reference's. */
+ * entry point, the reduced softening of crystal-like sites). Written for the
+ * tests; the names are the reference's. */
 #ifndef H_BMGFLAGS
 #define H_BMGFLAGS
 #ifdef REFAPI_TEST_SHEAR
@@ -15,4 +16,5 @@
 #define MICRO_MEMORY
 #endif
 #define INHOM_ELAST
+#define NO_SF_XTAL_MRO
 #endif

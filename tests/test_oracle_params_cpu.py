@@ -17,10 +17,14 @@ from metallic_glasses_gb300 import api, configs
 
 
 def _fields(p):
+    import ctypes as C
     out = {}
     for name, ctype in api.Params._fields_:
         v = getattr(p, name)
-        out[name] = list(v) if hasattr(v, "__len__") else v
+        if isinstance(v, C._Pointer):
+            out[name] = C.cast(v, C.c_void_p).value  # the address (None: no map)
+        else:
+            out[name] = list(v) if hasattr(v, "__len__") else v
     return out
 
 

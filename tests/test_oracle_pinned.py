@@ -5,10 +5,10 @@ import pytest
 
 from conftest import golden
 from metallic_glasses_gb300 import api
-from ref2d_cases import CASES, params_for
+from ref2d_cases import CASES, MRO_CASES, check_mro_state, params_for
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + MRO_CASES)
 def test_oracle_matches_reference_bitwise(oracle_lib, engine_lib, case):
     g = golden(case)
     p = params_for(g)
@@ -47,6 +47,33 @@ def test_oracle_matches_reference_bitwise(oracle_lib, engine_lib, case):
     assert np.allclose(deps.sum(axis=(0, 2)), g["deps_sum"], rtol=0, atol=1e-12)
     assert sc["eps_avg"][:3] == list(g["sc"][1:4])
     assert sc["stress"][:3] == list(g["sc"][4:7])
+    if case in MRO_CASES:
+        check_mro_state(m, g)
+
+
+def test_mro_fixtures_take_crystal_like_transformations():
+    """The MRO fixtures exercise what they are for: crystal-like sites of
+    every type the map holds transform (the reference's actQ.out records the
+    chosen site's type), and their barriers were re-drawn."""
+    for case, types in (("ref2d_32_mro_s11", {1}), ("ref2d_32_mrofile_s13", {1, 2, 3})):
+        g = golden(case)
+        assert set(np.unique(g["mro"])) == types | {0}
+        chosen = set(np.unique(g["actq"][:, 0].astype(int)))
+        assert types <= chosen
+        X = g["X"]
+        thermal = X[X[:, 1] == 0]
+        assert np.array_equal(g["actq"][:, 0].astype(np.int8), g["mro"][thermal[:, 2]])
+        assert (g["mro_iout"] == g["mro"]).all()
+
+
+def test_mro_structure_file_is_checked():
+    """A structure line whose indices do not match its position is refused,
+    as the reference aborts (init.c:412-416)."""
+    from metallic_glasses_gb300 import configs
+    t, th = configs.read_mro_structure("1 1 0 0.5\n1 2 3 -0.25\n", 1, 2)
+    assert t.tolist() == [0, 3] and th.tolist() == [0.5, -0.25]
+    with pytest.raises(ValueError):
+        configs.read_mro_structure("1 1 0 0.5\n1 3 3 -0.25\n", 1, 2)
 
 
 def test_shear_instability_stop(oracle_lib, engine_lib):

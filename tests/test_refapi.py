@@ -103,10 +103,11 @@ def test_driver_reproduces_reference_events(engine_lib):
     for r10 in S10:
         got = steps[rows[int(r10[0])]]
         assert np.allclose(got[3:9], r10[3:9], rtol=1e-9, atol=1e-12)
-    # actQ.out: one record per thermal event, the chosen mode
+    # actQ.out: one record per thermal event, the chosen site's MRO type (all
+    # glass here) and its Q
     thermal = X[X[:, 1] == 0]
     assert len(actq) == len(thermal)
-    assert np.array_equal(actq[:, 0].astype(np.int64), thermal[:, 3])
+    assert (actq[:, 0] == 0).all()
     # the print files' positions: supercell position plus the displacement
     # field (up to ~1 nm here), both written with 6 decimals
     ref_xr = g["xr"]
@@ -119,6 +120,41 @@ def test_driver_reproduces_reference_events(engine_lib):
     assert iout.shape == ref_io.shape
     assert np.abs(iout[:, 0] - ref_io[:, 0]).max() <= 1e-12 * np.abs(ref_io[:, 0]).max()
     assert np.abs(iout[:, 1] - ref_io[:, 1]).max() <= 1e-9 * np.abs(ref_io[:, 1]).max()
+
+
+@pytest.mark.gpu
+def test_driver_reproduces_reference_with_mro_structure(engine_lib):
+    """InitMRO 1: the drop-in's Alloc reads the reference's MROstructure.ms
+    (six-, two- and ten-fold sites), the run takes the reference's
+    transformations, writes its Initial_MROstructure record (ten-fold sites
+    turned two-fold by the same draws) and its actQ.out (the chosen site's MRO
+    type and Q)."""
+    import ast
+    g = golden("ref2d_32_mrofile_s13")
+    hdr = g["hdr"]
+    ov = ast.literal_eval(str(g["overrides"]))
+    with tempfile.TemporaryDirectory() as d:
+        exe = build_driver(os.path.join(d, "driver"))
+        configs.write_input(os.path.join(d, "input"), **ov)
+        with open(os.path.join(d, "MROstructure.ms"), "w") as f:
+            f.write(str(g["structure"]))
+        env = dict(os.environ, REFAPI_MAX_EVENTS=str(int(hdr[2])), REFAPI_XR_PRINTS="1")
+        r = subprocess.run([exe], cwd=d, env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
+        ev = np.loadtxt(os.path.join(d, "events.txt"), dtype=np.int64, ndmin=2)
+        actq = np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2)
+        mro = np.fromfile(os.path.join(d, "Initial_MROstructure_S000.iout"), np.int32)
+    X = g["X"]
+    assert ev.shape == X.shape
+    for col, name in enumerate(("step", "kind", "site", "mode")):
+        bad = np.nonzero(ev[:, col] != X[:, col])[0]
+        assert bad.size == 0, "first mismatch in %s at row %d" % (name, bad[0])
+    assert np.array_equal(mro, g["mro_iout"])
+    ref = g["actq"]
+    assert actq.shape == ref.shape
+    assert np.array_equal(actq[:, 0], ref[:, 0])
+    # Q printed with 7 significant digits
+    assert np.abs(actq[:, 1] - ref[:, 1]).max() <= 1e-6 * np.abs(ref[:, 1]).max()
 
 
 def test_iout_records_are_the_raw_fields(engine_lib):
