@@ -361,7 +361,18 @@ def main():
     pe.run(max_events=plain_events)
     pms = pe.timer_stop()
     plain = plain_events / (pms / 1e3)
+    # its FP64 rate pass alone (rates of all sites and modes, sums, selection
+    # and commit): an FP64 form with the mixed form's incremental update would
+    # still run it once per event, so it bounds such a form's event rate
+    rate64_ms, rate64_n = pe.kernel_time(steps=8, which=0)
     pe.close()
+    precision_gain = {
+        "fp64_rate_pass_ms": rate64_ms, "launches_timed": rate64_n,
+        "fp64_incremental_events_per_s_at_most": 1e3 / rate64_ms,
+        "mixed_over_fp64_incremental_at_least": (value / world) / (1e3 / rate64_ms),
+        "note": "an FP64 form with the incremental update runs this FP64 rate pass once per event; "
+                "the ratio compares FP32 with FP64 arithmetic under the same method (mixed_over_plain "
+                "also compares the incremental update with the full re-solve per event)"}
 
     if rank != 0:
         if dist:
@@ -373,6 +384,7 @@ def main():
             "data": "synthetic (seeded barriers, modes)",
             "config": headline_config(n, B, world),
             "plain_fp64_events_per_s": plain, "mixed_over_plain": value / world / plain,
+            "precision_gain": precision_gain,
             "stress_err": stress_err,
             "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
             "wall_s": t_wall}
