@@ -302,8 +302,8 @@ int stz_solve(stz_ctx* ctx);
  * with <eps> = eps_avg. Scratch is one fixed device array (about 13 MB, held
  * by every GPU that loads the library until exit) that fits at most six
  * components of 64^3 (2D up to 512^2); larger grids return STZ_ERR_INVALID.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture. All calls share the array: calls
+ * The first call on a device looks up the array's device address. All calls
+ * share the array: calls
  * that overlap on the GPU race. Each call copies its twiddle tables and the
  * mean strain from host memory to the array and synchronises the stream
  * before returning. */
