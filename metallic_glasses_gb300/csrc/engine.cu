@@ -706,8 +706,10 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   kp.shear_quirk = p.shear_elastic_quirk;
   kp.lambda = p.lambda; kp.mu = p.mu; kp.young = p.young; kp.poisson = p.poisson;
   kp.kT = p.temperature * kBoltz * kJInEv;
+  kp.inv_kT = 1.0 / kp.kT;
   kp.vt = p.voxel_volume * p.trial_frequency;
   kp.V0 = p.voxel_volume;
+  kp.w_scale = kp.V0 * 1e-18 * kJInEv / (2 * kp.kT);
   kp.dt = p.strain_rate > 0 ? p.strain_increment / p.strain_rate : INFINITY;
   kp.gamma0 = p.gamma0;
   kp.perm_soft = p.perm_soft; kp.temp_soft = p.temp_soft; kp.perm_soft_cap = p.perm_soft_cap; kp.t_temp = p.t_temp;

@@ -319,6 +319,51 @@ __device__ __forceinline__ double dire_modifier(int scheme, double dot, double n
   }
 }
 
+// ---------------------------------------------------------- FP64 rates
+// exp(x) of the FP64 rate kernels by Tang's table-driven method (P. T. P. Tang,
+// "Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (64 m + j) ln2/64 + r
+// with |r| <= ln2/128, exp(x) = 2^m 2^(j/64) e^r; ln2/64 in a 32-bit head (k
+// times it is exact for |k| < 2^21) and a tail; e^r - 1 by its Taylor
+// polynomial of degree 5 (truncation below 2^-54 relative); 2^(j/64) from
+// exp_table.h (generated by exp_table.py) as hi + lo, read through L1 since
+// each lane takes its own entry. Within 1 ulp of the exact value. Arguments
+// outside (-700, 700), and NaN, take the library routine. As written the FP64
+// pipe (the bound of the rate kernels) does the arithmetic only: the range test
+// compares the bit pattern of |x|, 2^m enters as an integer add to the
+// exponent field, and hi + lo rounds to hi (|lo| is below half an ulp of hi),
+// so S(J) of Tang's reconstruction is hi.
+#define STZ_EXP_TABLE_STORAGE __device__ const
+#include "exp_table.h"
+#undef STZ_EXP_TABLE_STORAGE
+
+__device__ __forceinline__ double exp_tang(double x) {
+  if (!((__double_as_longlong(x) & 0x7fffffffffffffffLL) < 0x4085e00000000000LL)) return exp(x);  // |x| < 700
+  const double kd = rint(x * STZ_EXP_INV_STEP);
+  const int k = (int)kd;
+  const double r1 = __fma_rn(-kd, STZ_EXP_STEP_HEAD, x);
+  const double r2 = -kd * STZ_EXP_STEP_TAIL;
+  const double r = r1 + r2;
+  double c = __fma_rn(r, 1.0 / 120, 1.0 / 24);
+  c = __fma_rn(r, c, 1.0 / 6);
+  c = __fma_rn(r, c, 0.5);
+  const double p = r1 + __fma_rn(r * r, c, r2);
+  const int j = k & 63, m = (k - j) / 64;
+  const double hi = __ldg(&kExp2Hi[j]), lo = __ldg(&kExp2Lo[j]);
+  return __longlong_as_double(__double_as_longlong(hi + __fma_rn(hi, p, lo)) + ((long long)m << 52));
+}
+
+// Q/kT correctly rounded: Markstein's refinement of Q times the rounded
+// reciprocal of kT (one correction of the product by its exact residual;
+// checked against the division for 2 10^7 barriers at three temperatures)
+__device__ __forceinline__ double over_kT(const KParams& kp, double Q) {
+  const double q0 = Q * kp.inv_kT;
+  return isfinite(q0) ? __fma_rn(__fma_rn(-q0, kp.kT, Q), kp.inv_kT, q0) : Q / kp.kT;
+}
+
+// vt exp(-Q/kT), the rate of a barrier Q (REF2D)
+__device__ __forceinline__ double rate64(const KParams& kp, double Q) { return kp.vt * exp_tang(-over_kT(kp, Q)); }
+
 // REF2D: site data shared by the 20 modes; ft is the factor NO_SF_XTAL_MRO
 // applies at a crystal-like site (init.c:645-660), 0 at a glass site
 struct R2Site {
@@ -340,7 +385,7 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
   // a site without temporary softening skips the decay's exponential: its
   // term is 0 times a finite positive factor, +0 exactly
   const double ts = kp.softening ? f.temp_soft[s] : 0.0;
-  d.soft = kp.softening ? (ts != 0.0 ? f.perm_soft[s] + ts * exp((f.tlast[s] - totime) / kp.t_temp)
+  d.soft = kp.softening ? (ts != 0.0 ? f.perm_soft[s] + ts * exp_tang((f.tlast[s] - totime) / kp.t_temp)
                                      : f.perm_soft[s])
                         : 0.0;
   const int t = (f.mro && kp.no_sf_xtal_mro) ? f.mro[s] : 0;
@@ -378,7 +423,7 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
     DM = __dmul_rn(DM, d.ft);
     for (int k = 0; k <= m; k++) soft = __dmul_rn(soft, d.ft);
   }
-  return f.Q0[(long long)m * N + s] * exp(-DM * soft) - DWork / 2;
+  return f.Q0[(long long)m * N + s] * exp_tang(-DM * soft) - DWork / 2;
 }
 
 // GLOBAL3D FP64: Q = dF - W/2 with W = sigma:deps_m
@@ -390,6 +435,27 @@ __device__ __forceinline__ double g3_Q(const KParams& kp, const double* sg, doub
 
 __device__ __forceinline__ void g3_load(const KParams& kp, const Fields& f, const double* u, long long s, double* sg) {
   for (int c = 0; c < 6; c++) sg[c] = f.sig[c * kp.N + s] + u[c];
+}
+
+// GLOBAL3D FP64 rate arguments x_m = -Q_m/kT = W_m V0 1e-18 J / (2 kT) - dF/kT,
+// from the site's stresses scaled once by V0 1e-18 J / (2 kT) (Voigt shear
+// weights included): six FMAs per mode in place of the work sum, its four
+// scale factors, the difference and the quotient of -Q/kT, which x matches to
+// a few ulps. x > 0 exactly when Q < 0 (the avalanche trigger) unless |Q| is
+// within a few ulps of zero; the avalanche's own marking keeps g3_Q.
+struct G3Arg {
+  double ws[6], x0;
+};
+__device__ __forceinline__ G3Arg g3_arg_site(const KParams& kp, const double* sg, double dF) {
+  G3Arg a;
+  for (int c = 0; c < 6; c++) a.ws[c] = ((c >= 3 ? 2.0 : 1.0) * sg[c]) * kp.w_scale;
+  a.x0 = -over_kT(kp, dF);
+  return a;
+}
+__device__ __forceinline__ double g3_arg(const KParams& kp, const G3Arg& a, int m) {
+  double x = a.x0;
+  for (int c = 0; c < 6; c++) x = __fma_rn(a.ws[c], kp.modes[m][c], x);
+  return x;
 }
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -594,11 +660,11 @@ __device__ __forceinline__ double site_rate(const KParams& kp, const Fields& f, 
                                             long long s, int m) {
   if (MODEL == 0) {
     const R2Site d = r2_load(kp, f, u, totime, s);
-    return kp.vt * exp(-r2_Q(kp, f, d, s, m) / kp.kT);
+    return rate64(kp, r2_Q(kp, f, d, s, m));
   } else if (MODEL == 1) {
     double sg[6];
     g3_load(kp, f, u, s, sg);
-    return kp.vt * exp(-g3_Q(kp, sg, f.dF[s], m) / kp.kT);
+    return kp.vt * exp_tang(g3_arg(kp, g3_arg_site(kp, sg, f.dF[s]), m));
   } else {
     float sv[5];
     mx_site(kp, f, s, sv);
@@ -934,17 +1000,17 @@ __global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
       for (int m = 0; m < STZ_MODES; m++) {
         const double Q = r2_Q(kp, f, d, s, m);
         neg += Q < 0;
-        acc[m] += kp.vt * exp(-Q / kp.kT);
+        acc[m] += rate64(kp, Q);
       }
     } else {
       double sg[6];
       g3_load(kp, f, u, s, sg);
-      const double dF = f.dF[s];
+      const G3Arg a = g3_arg_site(kp, sg, f.dF[s]);
 #pragma unroll 4
       for (int m = 0; m < STZ_MODES; m++) {
-        const double Q = g3_Q(kp, sg, dF, m);
-        neg += Q < 0;
-        acc[m] += kp.vt * exp(-Q / kp.kT);
+        const double x = g3_arg(kp, a, m);
+        neg += x > 0;
+        acc[m] += kp.vt * exp_tang(x);
       }
     }
   }
