@@ -93,7 +93,11 @@ enum {
   STZ_SOLVER_FFT = 0,       /* full Green's-function re-solve by FFT after every
                                transformation (the reference's method) */
   STZ_SOLVER_KERNEL = 1,    /* incremental: add the precomputed real-space
-                               response of one transformed voxel */
+                               response of one transformed voxel (the mixed form's
+                               FP32 table; in the FP64 forms an FP64 table of the
+                               unit responses of each strain component, avalanches
+                               and prints still re-solving by FFT; homogeneous
+                               moduli only) */
   STZ_SOLVER_AUTO = 2       /* pick per grid size from the tuning table */
 };
 

@@ -4,6 +4,8 @@ ref2d(...)      the reference's own 2D model, built from a reference-format
                 input file (labels of io.c:4-101) at a chosen grid, with the
                 text of an MROstructure.ms file when its input reads one
 stress32()      32^3, FP64, constant applied pure shear stress 1 GPa, seed 0
+plain128()      128^3 (or n^3), FP64, shear strain rate, the re-solve after every event
+incr128()       the same with the FP64 incremental update
 shear64(seed)   64^3, FP64, shear strain rate, seeds 0-3
 mixed128()      128^3, mixed form, periodic full re-solve every 1000 events
 grf256()        256^3, mixed form, correlated barrier field
@@ -134,6 +136,14 @@ def mixed128(seed=0, n=128, resolve_period=1000, defaults=None):
 
 def plain128(seed=0, n=128, defaults=None):
     return shear64(seed, n, defaults=defaults)
+
+
+def incr128(seed=0, n=128, defaults=None):
+    """The FP64 form with the incremental update (the mixed form's method in
+    FP64) in place of the re-solve after every event."""
+    p = shear64(seed, n, defaults=defaults)
+    p.solver = api.SOLVER_KERNEL
+    return p
 
 
 def grf256(seed=0, n=256, defaults=None):

@@ -326,7 +326,48 @@ int solve_plain(stz_ctx* c, const int* gate, const double* ebar) {
   a.msum = c->f.msum;
   a.spec = c->f.spec;
   a.fp32 = 0;
-  return fft_solve(*plan_of(c), a, c->stream, &c->launches);
+  const int st = fft_solve(*plan_of(c), a, c->stream, &c->launches);
+  if (!st && c->kp.incr64) {
+    // the incremental updates start from the mean strain of this solve
+    launch_note_solve(c->f, gate, ebar, c->stream);
+    c->launches += 1;
+  }
+  return st;
+}
+
+// FP64 incremental form: the solve of a unit eigenstrain component k at site
+// 0 with zero mean strain, for each k, as the stress table rtab64 [k][c][N].
+// The solve is linear in the eigenstrain and the mean strain, so a transformed
+// voxel's increment d and a mean-strain change adds sum_k d_k R_k (shifted to
+// the voxel) plus C:(change) to the field.
+int build_response_table64(stz_ctx* c) {
+  const KParams& kp = c->kp;
+  const long long N = kp.N;
+  const int nc = kp.nc;
+  int st;
+  if ((st = dalloc(&c->f.rtab64, (size_t)nc * nc * N))) return st;
+  double *eps = nullptr, *zero = nullptr;
+  if ((st = dalloc(&eps, (size_t)nc * N))) return st;
+  if ((st = dalloc(&zero, 6))) { cudaFree(eps); return st; }
+  const double one = 1.0;
+  for (int k = 0; k < nc; k++) {
+    CK(cudaMemsetAsync(eps, 0, sizeof(double) * nc * N, c->stream));
+    CK(cudaMemcpyAsync(eps + (size_t)k * N, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    SolveArgs a{};
+    a.eps = eps;
+    a.ebar = zero;
+    a.lambda = kp.lambda;
+    a.mu = kp.mu;
+    a.out = kOutSig64;
+    a.sig64 = c->f.rtab64 + (size_t)k * nc * N;
+    a.msum = c->f.msum;
+    a.spec = c->f.spec;
+    if ((st = fft_solve(*plan_of(c), a, c->stream, &c->launches))) break;
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  cudaFree(eps);
+  cudaFree(zero);
+  return st;
 }
 
 // A spatially varying medium (InhomogeneousStressSolver, elastic.c:977-1066):
@@ -454,6 +495,10 @@ void enqueue_plain_step(stz_ctx* c, cudaEvent_t t0 = nullptr, cudaEvent_t t1 = n
   if (t1) cudaEventRecord(t1, c->stream);
   launch_athermal(kp, f, 0, c->stream);
   solve_plain(c, gate, ebar);
+  if (kp.incr64) {
+    launch_incr64(kp, f, c->stream);
+    c->launches += 2;
+  }
   launch_post_a(kp, f, c->stream);
   solve_plain(c, gate, ebar);
   if (f.Q1) {
@@ -644,7 +689,8 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
   int solver = p.solver;
   if (solver == STZ_SOLVER_AUTO) solver = mixed ? STZ_SOLVER_KERNEL : STZ_SOLVER_FFT;
   if (mixed && solver != STZ_SOLVER_KERNEL) { set_error("the mixed form uses the incremental (kernel) solver"); return STZ_ERR_UNSUPPORTED; }
-  if (!mixed && solver != STZ_SOLVER_FFT) { set_error("the FP64 forms use the FFT solver"); return STZ_ERR_UNSUPPORTED; }
+  // FP64 forms: the FFT re-solve after every event (the reference's method) or
+  // the incremental update (the solve's response to one voxel, precomputed)
 
   stz_ctx* c = new stz_ctx();
   c->p = p;
@@ -661,6 +707,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
 
   kp.model = p.model;
   kp.nc = ref2d ? 3 : 6;
+  kp.incr64 = !mixed && solver == STZ_SOLVER_KERNEL;
   kp.n0 = p.n[0]; kp.n1 = p.n[1]; kp.n2 = p.n[2];
   kp.nh = kp.n2 / 2 + 1;
   kp.N = (long long)kp.n0 * kp.n1 * kp.n2;
@@ -822,6 +869,7 @@ int stz::create_ctx(const stz_params* pin, stz_ctx** out, int units_per_block) {
     if ((st = build_response_table(c))) return fail(st);
     solve_dev(c, f.ctl->eps_avg, nullptr, f.scratch);
   } else {
+    if (kp.incr64 && (st = build_response_table64(c))) return fail(st);
     solve_plain(c, nullptr, f.ctl->eps_avg);
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
@@ -838,7 +886,7 @@ extern "C" void stz_destroy(stz_ctx* c) {
   cudaSetDevice(c->p.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   Fields& f = c->f;
-  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.Q1, f.deps, f.dnorm, f.mro, f.prev_deps, f.perm_soft, f.temp_soft,
+  void* ptrs[] = {f.eps0, f.sig, f.sdev, f.dF, f.dF32, f.Q0, f.Q1, f.deps, f.dnorm, f.rtab64, f.mro, f.prev_deps, f.perm_soft, f.temp_soft,
                   f.tlast, f.amark, f.part, f.gsum, f.gticket, f.lsum, f.lbnd, f.psum, f.spec, f.ktab, f.log,
                   f.ctl, f.scratch, f.msum, c->err_dev, c->l2buf, c->qbuf, f.lam_site, f.mu_site,
                   f.inh_tau0, f.inh_eeff, f.inh_last, f.inh_part};
@@ -1147,8 +1195,9 @@ extern "C" int stz_set_field(stz_ctx* c, int32_t which, int32_t comp, const doub
   if (!c || !host || count != c->kp.N || which == STZ_FIELD_MRO) return STZ_ERR_INVALID;
   cudaSetDevice(c->p.device);
   if (which == STZ_FIELD_LAMBDA || which == STZ_FIELD_MU) {
-    // the mixed form's response table assumes one uniform medium
-    if (c->f.sdev) return STZ_ERR_UNSUPPORTED;
+    // the response tables of the mixed and the FP64 incremental form assume
+    // one uniform medium
+    if (c->f.sdev || c->kp.incr64) return STZ_ERR_UNSUPPORTED;
     if (comp != 0) return STZ_ERR_INVALID;
     int st = ensure_moduli(c);
     if (st) return st;

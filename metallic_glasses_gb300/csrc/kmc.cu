@@ -830,6 +830,7 @@ __device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, 
     f.prev_deps[c * N + s] = d[c];
     f.eps0[c * N + s] += d[c];
     ctl->eps0_sum[c] += d[c];
+    ctl->pend_deps[c] = d[c];
   }
   if (MODEL == 0) {
     const int ty = f.mro ? f.mro[s] : 0;
@@ -961,7 +962,12 @@ __device__ void finish_step(const KParams& kp, const Fields& f) {
         c->sel_mode = m;
         c->sel_q = q;
         transform<MODEL>(kp, f, c, m, s, &c->rng);
-        c->solve_req = 1;
+        if (kp.incr64) {
+          c->incr_req = 1;  // the incremental update instead of the re-solve
+          c->pend_site = s;
+        } else {
+          c->solve_req = 1;
+        }
         log_event(kp, f, c, STZ_EV_THERMAL, s, m, c->totime + c->t_kmc, c->t_kmc, q, Rtrue, sh_margin / sh_R, 1);
       }
     } else if (kind == kElastic) {
@@ -1102,7 +1108,9 @@ __global__ void k_post_a(KParams kp, Fields f) {
   Ctl* ctl = f.ctl;
   if (ctl->halt && ctl->step_kind == kNone) return;
   const int kind = ctl->step_kind;
-  const bool fieldmean = f.msum != nullptr;
+  // the mean of the solved field; after an incremental update, C:(ebar - <eps*>)
+  // of the same linear solve
+  const bool fieldmean = f.msum != nullptr && !(kp.incr64 && kind == kThermal);
   if ((kind == kThermal || kind == kAthermal) && fieldmean) field_mean_stress(kp, f, ctl->stress);
   if (threadIdx.x != 0) return;
   if (kind == kThermal) {
@@ -1126,6 +1134,56 @@ __global__ void k_post_a(KParams kp, Fields f) {
   }
   ctl->print_done = 0;
   ctl->solve_req = 0;
+}
+
+// FP64 incremental form, after a thermal event: the field the re-solve would
+// give, from its linearity in the eigenstrain and the mean strain. Each site r
+// gains sum_k d_k R_k(r - s) over the strain components k of the site's
+// increment d (the unit responses of rtab64, shifted to the transformed site
+// s) and C:(ebar - ebar_solved), the mean strain's change since the stored
+// field was solved.
+__global__ void k_incr64(KParams kp, Fields f) {
+  const Ctl* ctl = f.ctl;
+  if (!ctl->incr_req) return;
+  const int nc = kp.nc, nd = nc == 3 ? 2 : 3;
+  const long long N = kp.N;
+  double d[6], dU[6], dE[6];
+  for (int c = 0; c < nc; c++) {
+    d[c] = ctl->pend_deps[c];
+    dE[c] = ctl->eps_avg[c] - ctl->ebar_solved[c];
+  }
+  double tr = 0;
+  for (int c = 0; c < nd; c++) tr += dE[c];
+  for (int c = 0; c < nc; c++) dU[c] = (c < nd ? kp.lambda * tr : 0.0) + 2.0 * kp.mu * dE[c];
+  const long long sp = ctl->pend_site;
+  const int a2 = (int)(sp % kp.n2), a1 = (int)((sp / kp.n2) % kp.n1), a0 = (int)(sp / ((long long)kp.n2 * kp.n1));
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x) {
+    const int r2 = (int)(r % kp.n2), r1 = (int)((r / kp.n2) % kp.n1), r0 = (int)(r / ((long long)kp.n2 * kp.n1));
+    int o0 = r0 - a0, o1 = r1 - a1, o2 = r2 - a2;
+    o0 += o0 < 0 ? kp.n0 : 0;
+    o1 += o1 < 0 ? kp.n1 : 0;
+    o2 += o2 < 0 ? kp.n2 : 0;
+    const long long o = ((long long)o0 * kp.n1 + o1) * kp.n2 + o2;
+    for (int c = 0; c < nc; c++) {
+      double acc = dU[c];
+      for (int k = 0; k < nc; k++) acc = __fma_rn(d[k], __ldg(&f.rtab64[((long long)k * nc + c) * N + o]), acc);
+      f.sig[c * N + r] += acc;
+    }
+  }
+}
+
+// the update is in the field: it now holds the solve at the current mean strain
+__global__ void k_incr64_done(Fields f) {
+  Ctl* ctl = f.ctl;
+  if (!ctl->incr_req) return;
+  for (int c = 0; c < 6; c++) ctl->ebar_solved[c] = ctl->eps_avg[c];
+  ctl->incr_req = 0;
+}
+
+// an FFT solve (when its gate was set) leaves the field at the mean strain ebar
+__global__ void k_note_solve(Fields f, const int* gate, const double* ebar) {
+  if (gate && !*gate) return;
+  for (int c = 0; c < 6; c++) f.ctl->ebar_solved[c] = ebar[c];
 }
 
 // print check after every step kind; requests the print re-solve
@@ -2855,6 +2913,16 @@ void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st) {
 }
 
 void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st) { k_post_b<<<1, TH, 0, st>>>(kp, f); }
+
+void launch_incr64(const KParams& kp, const Fields& f, cudaStream_t st) {
+  const unsigned nb = (unsigned)std::min<long long>((kp.N + TH - 1) / TH, 152LL * 8);
+  k_incr64<<<nb, TH, 0, st>>>(kp, f);
+  k_incr64_done<<<1, 1, 0, st>>>(f);
+}
+
+void launch_note_solve(const Fields& f, const int* gate, const double* ebar, cudaStream_t st) {
+  k_note_solve<<<1, 1, 0, st>>>(f, gate, ebar);
+}
 
 void launch_q0_reset(const KParams& kp, const Fields& f, cudaStream_t st) {
   const long long total = (long long)STZ_MODES * kp.N;

@@ -55,6 +55,11 @@ void launch_athermal(const KParams& kp, const Fields& f, int mixed, cudaStream_t
 // after the optional print re-solve (stop checks, targets).
 void launch_post_a(const KParams& kp, const Fields& f, cudaStream_t st);
 void launch_post_b(const KParams& kp, const Fields& f, cudaStream_t st);
+// FP64 incremental form: the thermal event's update of the field (two kernels,
+// gated on the control block), and the mean strain of an FFT solve (gated as
+// the solve)
+void launch_incr64(const KParams& kp, const Fields& f, cudaStream_t st);
+void launch_note_solve(const Fields& f, const int* gate, const double* ebar, cudaStream_t st);
 // REF2D with crystal-like sites: restore the initial barriers when the step printed
 void launch_q0_reset(const KParams& kp, const Fields& f, cudaStream_t st);
 // Reset of the incremental state after a full re-solve (mixed form).

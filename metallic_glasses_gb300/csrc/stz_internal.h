@@ -82,6 +82,9 @@ struct Ctl {
   int has_pend;              // incremental path: a transformation is pending
   int pend_mode;
   long long pend_site;
+  int incr_req;              // FP64 incremental form: the thermal event's update is due
+  double pend_deps[6];       // FP64 forms: eigenstrain increment of the last transformation
+  double ebar_solved[6];     // FP64 forms: mean strain of the stored field's last solve
   unsigned int ticket;       // last-block-done counter of the rate kernels
   int sel_mode;
   long long sel_site;
@@ -107,6 +110,8 @@ struct Fields {
   double* Q0 = nullptr;      // [MODES][N] (REF2D)
   double* deps = nullptr;    // [MODES][3][N] (REF2D)
   double* dnorm = nullptr;   // [MODES][N] |deps| of each mode (REF2D), kept with deps
+  double* rtab64 = nullptr;  // [nc][nc][N] FP64 incremental form: stress component c of the
+                             // solve of a unit eigenstrain component k at site 0, ebar = 0
   int8_t* mro = nullptr;     // [N] crystal-like MRO type 0..3 (REF2D); null for an all-glass map
   double* Q1 = nullptr;      // [MODES][N] the initial Q0, restored at every print (bmg.c:214-221);
                              // only with crystal-like sites (glass sites never change Q0)
@@ -152,6 +157,7 @@ struct KParams {
   int fast_inv;              // mixed form: precomputed compliance coefficients
   double inv_2mu, inv_lam_coef, invN, inv_a_scale;
   int loading, softening, sf_scheme, no_subtract_error, shear_quirk, no_sf_xtal_mro;
+  int incr64;                      // FP64 forms: thermal events by the incremental update
   double lambda, mu, young, poisson;
   double kT, vt, V0, dt, gamma0;
   double inv_kT;                   // 1/kT rounded to nearest (rate quotients, over_kT)

@@ -117,6 +117,7 @@ def batch(replicas, events, alone=None, seed0=0):
 
 
 RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128, "plain64": configs.plain128,
+               "incr64": configs.incr128,
                # the reference's own 2D model at its shipped grid and input
                "ref2d512": lambda: configs.ref2d(512, 512)}
 

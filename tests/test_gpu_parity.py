@@ -123,9 +123,13 @@ def test_ref2d_deterministic(engine_lib):
 
 
 # ------------------------------------------------------------- 3D vs oracle
+@pytest.mark.parametrize("solver", [api.SOLVER_FFT, api.SOLVER_KERNEL])
 @pytest.mark.parametrize("cfg,events", [("stress32", 400), ("shear16", 400)])
-def test_global3d_plain_matches_oracle(engine_lib, oracle_lib, cfg, events):
+def test_global3d_plain_matches_oracle(engine_lib, oracle_lib, cfg, events, solver):
+    """The FP64 forms against the oracle's full re-solve per event: the FFT
+    re-solve (the reference's method) and the incremental update."""
     p = configs.stress32() if cfg == "stress32" else configs.shear64(seed=5, n=16)
+    p.solver = solver
     eng = api.Engine(p)
     ora = oracle_lib.Model(p)
     eng.run(max_events=events)
@@ -141,12 +145,15 @@ def test_global3d_plain_matches_oracle(engine_lib, oracle_lib, cfg, events):
     assert rel_err(eng.field(api.FIELD_DF), ora.field(api.FIELD_DF)) < 1e-15
 
 
-def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib):
+@pytest.mark.parametrize("solver", [api.SOLVER_FFT, api.SOLVER_KERNEL])
+def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib, solver):
     """The 32^3 stress-controlled configuration (1 GPa of shear, seed 0): the
     plain FP64 form takes the oracle's (step, kind, site, mode) sequence for the
     first 10^4 events, at its times, and ends with its stress and eigenstrain
-    fields within 1e-10 of their size."""
+    fields within 1e-10 of their size; with the FFT re-solve after every event
+    (the reference's method) and with the incremental update."""
     p = configs.stress32()
+    p.solver = solver
     eng = api.Engine(p)
     ora = oracle_lib.Model(p)
     eng.run(max_events=10000)
@@ -162,6 +169,29 @@ def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib):
         assert rel_err(eng.field(api.FIELD_EPS0, c), ora.field(api.FIELD_EPS0, c)) < FIELD_RTOL
     eng.close()
     ora.close()
+
+
+def test_fp64_incremental_form_matches_resolve_form(engine_lib):
+    """The FP64 incremental form against the FFT re-solve after every event
+    (the reference's method) over 2000 events of shear loading at 32^3: the
+    same events at the same times, stress fields within 1e-12 of their size
+    (FP64 rounding of 2000 updates of the linear solve) and the same mean
+    stress (C:(ebar - <eps*>) of the solve against the solved field's mean)."""
+    out = []
+    for solver in (api.SOLVER_FFT, api.SOLVER_KERNEL):
+        p = configs.shear64(seed=3, n=32)
+        p.solver = solver
+        eng = api.Engine(p)
+        eng.run(max_events=2000)
+        out.append((eng.events(), np.stack([eng.field(api.FIELD_SIGMA, c) for c in range(6)]), eng.scalars()))
+        eng.close()
+    (a, fa, sa), (b, fb, sb) = out
+    assert sa["status"] == sb["status"] == 0 and sa["kstep"] == sb["kstep"] == 2000
+    for k in ("step", "kind", "site", "mode"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.abs(a["time"] - b["time"]).max() <= 1e-12 * np.abs(a["time"]).max()
+    assert np.abs(fa - fb).max() <= 1e-12 * np.abs(fa).max()
+    assert np.allclose(sa["stress"], sb["stress"], rtol=0, atol=1e-12 * np.abs(fa).max())
 
 
 def test_ensemble_stress_strain_curves_agree():
