@@ -171,19 +171,23 @@ def test_first_10k_events_match_oracle_32(engine_lib, oracle_lib, solver):
     ora.close()
 
 
-def test_fp64_incremental_form_matches_resolve_form(engine_lib):
+@pytest.mark.parametrize("model", ["shear32", "ref2d64"])
+def test_fp64_incremental_form_matches_resolve_form(engine_lib, model):
     """The FP64 incremental form against the FFT re-solve after every event
-    (the reference's method) over 2000 events of shear loading at 32^3: the
-    same events at the same times, stress fields within 1e-12 of their size
-    (FP64 rounding of 2000 updates of the linear solve) and the same mean
-    stress (C:(ebar - <eps*>) of the solve against the solved field's mean)."""
+    (the reference's method) over 2000 events: shear loading at 32^3, and the
+    reference's 2D model at 64^2 on its shipped input (per-site modes re-drawn
+    at each transformation, softening, prints and their re-solves). The same
+    events at the same times, stress fields within 1e-12 of their size (FP64
+    rounding of 2000 updates of the linear solve) and the same mean stress
+    (C:(ebar - <eps*>) of the solve against the solved field's mean)."""
     out = []
     for solver in (api.SOLVER_FFT, api.SOLVER_KERNEL):
-        p = configs.shear64(seed=3, n=32)
+        p = configs.shear64(seed=3, n=32) if model == "shear32" else configs.ref2d(64, 64)
         p.solver = solver
         eng = api.Engine(p)
         eng.run(max_events=2000)
-        out.append((eng.events(), np.stack([eng.field(api.FIELD_SIGMA, c) for c in range(6)]), eng.scalars()))
+        nc = 6 if model == "shear32" else 3
+        out.append((eng.events(), np.stack([eng.field(api.FIELD_SIGMA, c) for c in range(nc)]), eng.scalars()))
         eng.close()
     (a, fa, sa), (b, fb, sb) = out
     assert sa["status"] == sb["status"] == 0 and sa["kstep"] == sb["kstep"] == 2000
