@@ -479,6 +479,10 @@ def main():
         r2["workload"] = ("the reference's 2D model (per-site barriers and eigenstrains re-drawn after each "
                           "transformation, softening on) at its shipped 512 x 512 grid and input file, TENSION, "
                           "2000 thermal events after 100 warm-up events, every event a full FP64 re-solve")
+        ri = timing.run("ref2d512_incremental", events=2000, warmup=100)
+        r2["incremental"] = {"events_per_s": ri["events_per_s"], "us_per_event": ri["us_per_event"],
+                             "athermal_steps": ri["athermal_steps"],
+                             "workload": "the same with the FP64 incremental update in place of the re-solve"}
         line["ref2d512"] = r2
     if single and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(seconds=15.0, grid=n)

@@ -88,7 +88,7 @@ def read_mro_structure(text, nx, ny):
 
 
 def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None, from_input=None,
-          mro_structure=None, **overrides):
+          mro_structure=None, solver=None, **overrides):
     p = (defaults or api.default_params)(api.MODEL_REF2D)
     if input_path is None:
         import tempfile
@@ -99,6 +99,8 @@ def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None
     p.loading = loading
     if mro_structure is not None:
         api.set_mro_map(p, *read_mro_structure(mro_structure, nx, ny))
+    if solver is not None:
+        p.solver = solver
     return p
 
 

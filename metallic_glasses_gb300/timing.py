@@ -118,8 +118,10 @@ def batch(replicas, events, alone=None, seed0=0):
 
 RUN_CONFIGS = {"grf256": configs.grf256, "mixed128": configs.mixed128, "plain64": configs.plain128,
                "incr64": configs.incr128,
-               # the reference's own 2D model at its shipped grid and input
-               "ref2d512": lambda: configs.ref2d(512, 512)}
+               # the reference's own 2D model at its shipped grid and input,
+               # with the re-solve after every event and with the incremental update
+               "ref2d512": lambda: configs.ref2d(512, 512),
+               "ref2d512_incremental": lambda: configs.ref2d(512, 512, solver=api.SOLVER_KERNEL)}
 
 
 def run(config, events, warmup=1000, grid=None):
