@@ -307,15 +307,19 @@ __device__ void set_mixed_head(const KParams& kp, Ctl* c) {
 }
 
 // Direction modifier of the softening schemes (init.c:590-642)
-__device__ __forceinline__ double dire_modifier(int scheme, double dot, double n1, double n2) {
-  double DM;
+// The direction modifier from DM = dot / (n1 + eps) / (n2 + eps), here formed
+// as dot * r1 * r2 with the reciprocals r = 1 / (n + eps) (the mode's stored,
+// the site's once per site): two multiplications in place of two divisions,
+// within a few ulps of the quotients.
+__device__ __forceinline__ double dire_modifier(int scheme, double dot, double r1, double r2) {
+  const double DM = dot * r1 * r2;
   switch (scheme) {
-    case STZ_SF_LINEAR_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (DM + 1) / 2;
-    case STZ_SF_LINEAR_BWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (-DM + 1) / 2;
+    case STZ_SF_LINEAR_FWD: return (DM + 1) / 2;
+    case STZ_SF_LINEAR_BWD: return (-DM + 1) / 2;
     case STZ_SF_EVEN: return 0.5;
-    case STZ_SF_SQUARE_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (1 + DM) * (1 + DM) / 4;
-    case STZ_SF_CUBIC_FWD: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return (DM + 1) * (DM + 1) * (DM + 1) / 8;
-    default: DM = dot / (n1 + kEpsilon) / (n2 + kEpsilon); return exp(-DM * DM * 9 / 2);
+    case STZ_SF_SQUARE_FWD: return (1 + DM) * (1 + DM) / 4;
+    case STZ_SF_CUBIC_FWD: return (DM + 1) * (DM + 1) * (DM + 1) / 8;
+    default: return exp(-DM * DM * 9 / 2);
   }
 }
 
@@ -367,7 +371,7 @@ __device__ __forceinline__ double rate64(const KParams& kp, double Q) { return k
 // REF2D: site data shared by the 20 modes; ft is the factor NO_SF_XTAL_MRO
 // applies at a crystal-like site (init.c:645-660), 0 at a glass site
 struct R2Site {
-  double sg[3], pd[3], n2, soft, ft;
+  double sg[3], pd[3], r2, soft, ft;  // r2: 1 / (|last increment| + eps)
 };
 
 // the factor of MRO type 1 (six-fold), 2 (two-fold), 3 (ten-fold)
@@ -381,7 +385,7 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
     d.sg[c] = f.sig[c * N + s] + u[c];
     d.pd[c] = f.prev_deps[c * N + s];
   }
-  d.n2 = sqrt(d.pd[0] * d.pd[0] + d.pd[1] * d.pd[1] + 2 * d.pd[2] * d.pd[2]);
+  d.r2 = 1.0 / (sqrt(d.pd[0] * d.pd[0] + d.pd[1] * d.pd[1] + 2 * d.pd[2] * d.pd[2]) + kEpsilon);
   // a site without temporary softening skips the decay's exponential: its
   // term is 0 times a finite positive factor, +0 exactly
   const double ts = kp.softening ? f.temp_soft[s] : 0.0;
@@ -395,10 +399,15 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
 
 // Norm of a 2D mode increment, sqrt(de_xx^2 + de_yy^2 + 2 de_xy^2)
 // (init.c:600-603), every operation rounded on its own as the reference's C
-// evaluates it. Stored per mode and site whenever the modes are drawn, so the
-// rate passes load it instead of taking a square root per mode.
+// evaluates it, and the reciprocal 1 / (norm + eps) of the direction
+// modifier. The reciprocal is stored per mode and site whenever the modes are
+// drawn, so the rate passes load it instead of taking a square root and a
+// division per mode.
 __device__ __forceinline__ double mode_norm(double d0, double d1, double d2) {
   return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(__dmul_rn(2.0, d2), d2)));
+}
+__device__ __forceinline__ double mode_rnorm(double d0, double d1, double d2) {
+  return 1.0 / (mode_norm(d0, d1, d2) + kEpsilon);
 }
 
 // ActEnergy for one (mode, site) of the reference model (init.c:585-686)
@@ -413,8 +422,8 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
   // square root, two divisions and an exponential per mode are skipped
   if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
   const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
-  const double n1 = f.dnorm[(long long)m * N + s];
-  double DM = dire_modifier(kp.sf_scheme, dot, n1, d.n2);
+  const double r1 = f.dnorm[(long long)m * N + s];
+  double DM = dire_modifier(kp.sf_scheme, dot, r1, d.r2);
   double soft = d.soft;
   if (d.ft != 0.0) {
     // a crystal-like site: the reference scales the direction modifier and,
@@ -858,7 +867,7 @@ __device__ void transform(const KParams& kp, const Fields& f, Ctl* ctl, int mm, 
       dd[s] = a;
       dd[N + s] = -a;
       dd[2 * N + s] = c2;
-      f.dnorm[(long long)i * N + s] = mode_norm(a, -a, c2);
+      f.dnorm[(long long)i * N + s] = mode_rnorm(a, -a, c2);
     }
   }
 }
@@ -2880,7 +2889,7 @@ __global__ void k_mode_norms(KParams kp, Fields f) {
        i += (long long)gridDim.x * blockDim.x) {
     const long long m = i / N, s = i - m * N;
     const double* dd = f.deps + m * 3 * N;
-    f.dnorm[i] = mode_norm(dd[s], dd[N + s], dd[2 * N + s]);
+    f.dnorm[i] = mode_rnorm(dd[s], dd[N + s], dd[2 * N + s]);
   }
 }
 

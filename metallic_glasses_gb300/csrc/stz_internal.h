@@ -109,7 +109,7 @@ struct Fields {
   float* dF32 = nullptr;     // [N] barrier (mixed form)
   double* Q0 = nullptr;      // [MODES][N] (REF2D)
   double* deps = nullptr;    // [MODES][3][N] (REF2D)
-  double* dnorm = nullptr;   // [MODES][N] |deps| of each mode (REF2D), kept with deps
+  double* dnorm = nullptr;   // [MODES][N] 1 / (|deps| + eps) of each mode (REF2D), kept with deps
   double* rtab64 = nullptr;  // [nc][nc][N] FP64 incremental form: stress component c of the
                              // solve of a unit eigenstrain component k at site 0, ebar = 0
   int8_t* mro = nullptr;     // [N] crystal-like MRO type 0..3 (REF2D); null for an all-glass map
