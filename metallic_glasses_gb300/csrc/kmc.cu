@@ -365,13 +365,12 @@ __device__ __forceinline__ double over_kT(const KParams& kp, double Q) {
   return isfinite(q0) ? __fma_rn(__fma_rn(-q0, kp.kT, Q), kp.inv_kT, q0) : Q / kp.kT;
 }
 
-// vt exp(-Q/kT), the rate of a barrier Q (REF2D)
-__device__ __forceinline__ double rate64(const KParams& kp, double Q) { return kp.vt * exp_tang(-over_kT(kp, Q)); }
 
 // REF2D: site data shared by the 20 modes; ft is the factor NO_SF_XTAL_MRO
 // applies at a crystal-like site (init.c:645-660), 0 at a glass site
 struct R2Site {
   double sg[3], pd[3], r2, soft, ft;  // r2: 1 / (|last increment| + eps)
+  double sw[3];                       // the stresses times V0 1e-18 J / (2 kT), shear weight 2
 };
 
 // the factor of MRO type 1 (six-fold), 2 (two-fold), 3 (ten-fold)
@@ -384,6 +383,7 @@ __device__ __forceinline__ R2Site r2_load(const KParams& kp, const Fields& f, co
   for (int c = 0; c < 3; c++) {
     d.sg[c] = f.sig[c * N + s] + u[c];
     d.pd[c] = f.prev_deps[c * N + s];
+    d.sw[c] = ((c == 2 ? 2.0 : 1.0) * d.sg[c]) * kp.w_scale;
   }
   d.r2 = 1.0 / (sqrt(d.pd[0] * d.pd[0] + d.pd[1] * d.pd[1] + 2 * d.pd[2] * d.pd[2]) + kEpsilon);
   // a site without temporary softening skips the decay's exponential: its
@@ -411,16 +411,10 @@ __device__ __forceinline__ double mode_rnorm(double d0, double d1, double d2) {
 }
 
 // ActEnergy for one (mode, site) of the reference model (init.c:585-686)
-__device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m) {
+// The softened barrier Q0 exp(-DM soft) of a softened site (init.c:612-684)
+__device__ __forceinline__ double r2_soft_q0(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m,
+                                             double d0, double d1, double d2) {
   const long long N = kp.N;
-  const double* dd = f.deps + (long long)m * 3 * N;
-  const double d0 = dd[s], d1 = dd[N + s], d2 = dd[2 * N + s];
-  const double DWork = (d.sg[0] * d0 + d.sg[1] * d1 + 2 * d.sg[2] * d2) * kp.V0 * 1e-18 * kJInEv;
-  // an unsoftened site (every site before its first transformation): the
-  // direction modifier is finite (its norms carry kEpsilon), so the factor
-  // exp(-DM * 0) is exactly 1 and the barrier is Q0 - W/2 to the bit; the
-  // square root, two divisions and an exponential per mode are skipped
-  if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
   const double dot = d.pd[0] * d0 + d.pd[1] * d1 + 2 * d.pd[2] * d2;
   const double r1 = f.dnorm[(long long)m * N + s];
   double DM = dire_modifier(kp.sf_scheme, dot, r1, d.r2);
@@ -432,7 +426,36 @@ __device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const
     DM = __dmul_rn(DM, d.ft);
     for (int k = 0; k <= m; k++) soft = __dmul_rn(soft, d.ft);
   }
-  return f.Q0[(long long)m * N + s] * exp_tang(-DM * soft) - DWork / 2;
+  return f.Q0[(long long)m * N + s] * exp_tang(-DM * soft);
+}
+
+__device__ __forceinline__ double r2_Q(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m) {
+  const long long N = kp.N;
+  const double* dd = f.deps + (long long)m * 3 * N;
+  const double d0 = dd[s], d1 = dd[N + s], d2 = dd[2 * N + s];
+  const double DWork = (d.sg[0] * d0 + d.sg[1] * d1 + 2 * d.sg[2] * d2) * kp.V0 * 1e-18 * kJInEv;
+  // an unsoftened site (every site before its first transformation): the
+  // direction modifier is finite (its norms carry kEpsilon), so the factor
+  // exp(-DM * 0) is exactly 1 and the barrier is Q0 - W/2 to the bit; the
+  // square root, two divisions and an exponential per mode are skipped
+  if (d.soft == 0.0) return f.Q0[(long long)m * N + s] - DWork / 2;
+  return r2_soft_q0(kp, f, d, s, m, d0, d1, d2) - DWork / 2;
+}
+
+// The rate argument x = -Q/kT = W V0 1e-18 J / (2 kT) - Q0 e / kT of the rate
+// pass (e the softening factor, 1 at an unsoftened site), the work from the
+// site's stresses scaled once by V0 1e-18 J / (2 kT) (r2_load): three FMAs and
+// the quotient of Q0 e by kT per mode in place of the work sum, its scale
+// factors, the difference and the quotient of Q. Within a few ulps of -Q/kT;
+// x > 0 exactly when Q < 0 unless |Q| is within a few ulps of zero (the
+// avalanche's marking keeps r2_Q).
+__device__ __forceinline__ double r2_arg(const KParams& kp, const Fields& f, const R2Site& d, long long s, int m) {
+  const long long N = kp.N;
+  const double* dd = f.deps + (long long)m * 3 * N;
+  const double d0 = dd[s], d1 = dd[N + s], d2 = dd[2 * N + s];
+  const double hw = __fma_rn(d.sw[2], d2, __fma_rn(d.sw[1], d1, d.sw[0] * d0));
+  const double q = d.soft == 0.0 ? f.Q0[(long long)m * N + s] : r2_soft_q0(kp, f, d, s, m, d0, d1, d2);
+  return hw - over_kT(kp, q);
 }
 
 // GLOBAL3D FP64: Q = dF - W/2 with W = sigma:deps_m
@@ -669,7 +692,7 @@ __device__ __forceinline__ double site_rate(const KParams& kp, const Fields& f, 
                                             long long s, int m) {
   if (MODEL == 0) {
     const R2Site d = r2_load(kp, f, u, totime, s);
-    return rate64(kp, r2_Q(kp, f, d, s, m));
+    return kp.vt * exp_tang(r2_arg(kp, f, d, s, m));
   } else if (MODEL == 1) {
     double sg[6];
     g3_load(kp, f, u, s, sg);
@@ -1013,9 +1036,9 @@ __global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
       const R2Site d = r2_load(kp, f, u, totime, s);
 #pragma unroll 4
       for (int m = 0; m < STZ_MODES; m++) {
-        const double Q = r2_Q(kp, f, d, s, m);
-        neg += Q < 0;
-        acc[m] += rate64(kp, Q);
+        const double x = r2_arg(kp, f, d, s, m);
+        neg += x > 0;
+        acc[m] += kp.vt * exp_tang(x);
       }
     } else {
       double sg[6];

@@ -161,7 +161,7 @@ struct KParams {
   double lambda, mu, young, poisson;
   double kT, vt, V0, dt, gamma0;
   double inv_kT;                   // 1/kT rounded to nearest (rate quotients, over_kT)
-  double w_scale;                  // V0 1e-18 J / (2 kT): work to rate argument (GLOBAL3D FP64)
+  double w_scale;                  // V0 1e-18 J / (2 kT): work to rate argument (FP64 forms)
   double perm_soft, temp_soft, perm_soft_cap, t_temp;
   double perm_soft_mro, temp_soft_mro, xq0amp, random_ratio;  // crystal-like MRO sites (REF2D)
   double end_strain, strain_rate, strain_increment, print_thr;
