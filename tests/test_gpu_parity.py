@@ -114,6 +114,36 @@ def test_ref2d_event_sequence_matches_reference(engine_lib, case):
     eng.close()
 
 
+@pytest.mark.parametrize("no_sf", [1, 0])
+def test_mro_map_matches_oracle(engine_lib, oracle_lib, no_sf):
+    """Crystal-like sites drawn at 15 % (seed 11, 32^2, softening on) with the
+    NO_SF_XTAL_MRO switch as shipped and switched off (the reference's own build
+    only exists with it on, so the oracle's restatement is the pin there): the
+    engine takes the oracle's transformations for 1500 thermal events, fields
+    within 1e-10."""
+    from oracle import pyoracle
+    kw = dict(end="0.5", seed="11", xfrac="0.15", xq0="1.8")
+    p = configs.ref2d(32, 32, **kw)
+    p.no_sf_xtal_mro = no_sf
+    q = configs.ref2d(32, 32, defaults=pyoracle.default_params, from_input=pyoracle.params_from_input, **kw)
+    q.no_sf_xtal_mro = no_sf
+    eng = api.Engine(p)
+    ora = oracle_lib.Model(q)
+    eng.run(max_events=1500)
+    ora.run(max_events=1500)
+    a, b = eng.events(), ora.events()
+    a, b = a[a["kind"] != api.EV_ELASTIC], b[b["kind"] != api.EV_ELASTIC]
+    assert len(a) == len(b)
+    for k in ("step", "kind", "site", "mode"):
+        bad = np.nonzero(a[k] != b[k])[0]
+        assert bad.size == 0, "first mismatch in %s at %d" % (k, bad[0])
+    mro = eng.field(api.FIELD_MRO, 0)
+    assert (mro == 1).sum() > 100 and np.isin(a["site"], np.nonzero(mro)[0]).any()
+    for c in range(3):
+        assert rel_err(eng.field(api.FIELD_SIGMA, c), ora.field(api.FIELD_SIGMA, c)) < FIELD_RTOL
+    eng.close()
+
+
 def test_ref2d_deterministic(engine_lib):
     p = configs.ref2d(32, 32)
     a, b = api.Engine(p), api.Engine(p)
