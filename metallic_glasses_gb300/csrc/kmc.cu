@@ -326,10 +326,10 @@ __device__ __forceinline__ double dire_modifier(int scheme, double dot, double r
 // ---------------------------------------------------------- FP64 rates
 // exp(x) of the FP64 rate kernels by Tang's table-driven method (P. T. P. Tang,
 // "Table-driven implementation of the exponential function in IEEE
-// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (64 m + j) ln2/64 + r
-// with |r| <= ln2/128, exp(x) = 2^m 2^(j/64) e^r; ln2/64 in a 32-bit head (k
+// floating-point arithmetic", ACM TOMS 15(2), 1989): x = (256 m + j) ln2/256 + r
+// with |r| <= ln2/512, exp(x) = 2^m 2^(j/256) e^r; ln2/256 in a 32-bit head (k
 // times it is exact for |k| < 2^21) and a tail; e^r - 1 by its Taylor
-// polynomial of degree 5 (truncation below 2^-54 relative); 2^(j/64) from
+// polynomial of degree 4 (truncation below 2^-54 relative); 2^(j/256) from
 // exp_table.h (generated by exp_table.py) as hi + lo, read through L1 since
 // each lane takes its own entry. Within 1 ulp of the exact value. Arguments
 // outside (-700, 700), and NaN, take the library routine. As written the FP64
@@ -337,6 +337,11 @@ __device__ __forceinline__ double dire_modifier(int scheme, double dot, double r
 // compares the bit pattern of |x|, 2^m enters as an integer add to the
 // exponent field, and hi + lo rounds to hi (|lo| is below half an ulp of hi),
 // so S(J) of Tang's reconstruction is hi.
+// x > 0 for a rate argument (Q < 0, the avalanche trigger), on the integer
+// pipe: the bit patterns of +min subnormal .. +inf, which leaves out NaN
+__device__ __forceinline__ bool arg_positive(double x) {
+  return (unsigned long long)(__double_as_longlong(x) - 1) < 0x7ff0000000000000ULL;
+}
 #define STZ_EXP_TABLE_STORAGE __device__ const
 #include "exp_table.h"
 #undef STZ_EXP_TABLE_STORAGE
@@ -348,11 +353,9 @@ __device__ __forceinline__ double exp_tang(double x) {
   const double r1 = __fma_rn(-kd, STZ_EXP_STEP_HEAD, x);
   const double r2 = -kd * STZ_EXP_STEP_TAIL;
   const double r = r1 + r2;
-  double c = __fma_rn(r, 1.0 / 120, 1.0 / 24);
-  c = __fma_rn(r, c, 1.0 / 6);
-  c = __fma_rn(r, c, 0.5);
+  const double c = __fma_rn(r, __fma_rn(r, 1.0 / 24, 1.0 / 6), 0.5);
   const double p = r1 + __fma_rn(r * r, c, r2);
-  const int j = k & 63, m = (k - j) / 64;
+  const int j = k & 255, m = (k - j) / 256;
   const double hi = __ldg(&kExp2Hi[j]), lo = __ldg(&kExp2Lo[j]);
   return __longlong_as_double(__double_as_longlong(hi + __fma_rn(hi, p, lo)) + ((long long)m << 52));
 }
@@ -1037,7 +1040,7 @@ __global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
 #pragma unroll 4
       for (int m = 0; m < STZ_MODES; m++) {
         const double x = r2_arg(kp, f, d, s, m);
-        neg += x > 0;
+        neg += arg_positive(x);
         acc[m] += kp.vt * exp_tang(x);
       }
     } else {
@@ -1047,7 +1050,7 @@ __global__ void __launch_bounds__(TH) k_rate64(KParams kp, Fields f) {
 #pragma unroll 4
       for (int m = 0; m < STZ_MODES; m++) {
         const double x = g3_arg(kp, a, m);
-        neg += x > 0;
+        neg += arg_positive(x);
         acc[m] += kp.vt * exp_tang(x);
       }
     }
