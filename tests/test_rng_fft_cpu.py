@@ -38,3 +38,16 @@ def test_oracle_fft_matches_numpy(oracle_lib, shape):
     assert np.allclose(f, np.fft.fftn(a), rtol=0, atol=1e-10 * np.abs(a).sum())
     b = oracle_lib.fft3(f, +1)
     assert np.allclose(b / a.size, a, atol=1e-12)
+
+
+def test_exp_table_matches_its_generator():
+    """The FP64 exponential's table (exp_table.h) is what exp_table.py
+    generates: 2^(j/256) as hi + lo and the split of ln2/256."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "metallic_glasses_gb300", "csrc")
+    out = subprocess.run([sys.executable, os.path.join(here, "exp_table.py")], capture_output=True, text=True,
+                         check=True).stdout
+    with open(os.path.join(here, "exp_table.h")) as f:
+        assert f.read() == out
