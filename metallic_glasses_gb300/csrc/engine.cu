@@ -350,9 +350,13 @@ int build_response_table64(stz_ctx* c) {
   if ((st = dalloc(&eps, (size_t)nc * N))) return st;
   if ((st = dalloc(&zero, 6))) { cudaFree(eps); return st; }
   const double one = 1.0;
-  for (int k = 0; k < nc; k++) {
-    CK(cudaMemsetAsync(eps, 0, sizeof(double) * nc * N, c->stream));
-    CK(cudaMemcpyAsync(eps + (size_t)k * N, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  for (int k = 0; k < nc && !st; k++) {
+    if (cudaMemsetAsync(eps, 0, sizeof(double) * nc * N, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(eps + (size_t)k * N, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+      set_error("response table: %s", cudaGetErrorString(cudaGetLastError()));
+      st = STZ_ERR_CUDA;
+      break;
+    }
     SolveArgs a{};
     a.eps = eps;
     a.ebar = zero;
@@ -363,7 +367,10 @@ int build_response_table64(stz_ctx* c) {
     a.msum = c->f.msum;
     a.spec = c->f.spec;
     if ((st = fft_solve(*plan_of(c), a, c->stream, &c->launches))) break;
-    CK(cudaStreamSynchronize(c->stream));
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      set_error("response table: %s", cudaGetErrorString(cudaGetLastError()));
+      st = STZ_ERR_CUDA;
+    }
   }
   cudaFree(eps);
   cudaFree(zero);
