@@ -96,3 +96,6 @@ def test_ensemble_curve_machinery(oracle_lib, monkeypatch):
     assert eps[0] == 0.0 and sig[0] == 0.0 and out["strain_xy_max"] > 0.005
     mu = timing._ensemble_params(8, 0, 0, 250.0, 1e-4, 0.02).mu
     assert abs(sig[1] / eps[1] - 2 * mu) < 1e-6 * 2 * mu
+    inc = timing._ensemble_params(8, 0, 0, 250.0, 1e-4, 0.02, fp64_incremental=True)
+    assert inc.precision == api.PREC_FP64 and inc.solver == api.SOLVER_KERNEL
+    assert timing._ensemble_params(8, 0, 0, 250.0, 1e-4, 0.02).solver == api.SOLVER_FFT
