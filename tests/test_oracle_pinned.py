@@ -68,12 +68,17 @@ def test_mro_fixtures_take_crystal_like_transformations():
 
 def test_mro_structure_file_is_checked():
     """A structure line whose indices do not match its position is refused,
-    as the reference aborts (init.c:412-416)."""
+    as the reference aborts (init.c:412-416); so is a file with fewer lines than
+    sites. Blank lines are skipped and sites are read in row-major order."""
     from metallic_glasses_gb300 import configs
     t, th = configs.read_mro_structure("1 1 0 0.5\n1 2 3 -0.25\n", 1, 2)
     assert t.tolist() == [0, 3] and th.tolist() == [0.5, -0.25]
     with pytest.raises(ValueError):
         configs.read_mro_structure("1 1 0 0.5\n1 3 3 -0.25\n", 1, 2)
+    with pytest.raises(ValueError):
+        configs.read_mro_structure("1 1 0 0.5\n", 1, 2)
+    t, _ = configs.read_mro_structure("1 1 2 0\n\n1 2 1 0\n2 1 0 0\n2 2 3 0\n", 2, 2)
+    assert t.tolist() == [2, 1, 0, 3]
 
 
 def test_shear_instability_stop(oracle_lib, engine_lib):
