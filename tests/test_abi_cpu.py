@@ -90,3 +90,43 @@ def test_timing_commands_parse(cmd):
     r = subprocess.run([sys.executable, "-m", "metallic_glasses_gb300.timing", cmd, "--help"], cwd=ROOT,
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and "usage" in r.stdout, r.stderr[-1000:]
+
+
+def _refused(p):
+    from metallic_glasses_gb300 import api
+    with pytest.raises(api.StzError) as ei:
+        api.Engine(p)
+    return ei.value.code, str(ei.value)
+
+
+def test_create_refuses_bad_parameters_before_any_device_call(engine_lib):
+    """stz_create checks the parameters before it touches a device, so on this
+    host (no GPU) each unsupported or invalid combination is reported with its
+    own status and message, never as a CUDA failure."""
+    from metallic_glasses_gb300 import api, configs
+    p = configs.shear64(0, 16)
+    p.xmro_frac = 0.1
+    code, msg = _refused(p)
+    assert code == api.ERR_UNSUPPORTED and "MRO" in msg
+    p = configs.shear64(0, 16)
+    p.softening = 1
+    assert _refused(p)[0] == api.ERR_UNSUPPORTED
+    p = configs.ref2d(16, 16)
+    p.precision = api.PREC_MIXED
+    code, msg = _refused(p)
+    assert code == api.ERR_UNSUPPORTED and "3D" in msg
+    p = configs.shear64(0, 16)
+    p.precision, p.solver = api.PREC_MIXED, api.SOLVER_FFT
+    assert _refused(p)[0] == api.ERR_UNSUPPORTED
+    p = configs.shear64(0, 16)
+    p.precision, p.solver = api.PREC_MIXED, api.SOLVER_KERNEL
+    p.n[2] = 18
+    code, msg = _refused(p)
+    assert code == api.ERR_UNSUPPORTED and "multiple of 4" in msg
+    p = configs.shear64(0, 16)
+    p.n[2] = 15
+    code, msg = _refused(p)
+    assert code == api.ERR_INVALID and "not supported" in msg
+    p = configs.shear64(0, 16)
+    p.mu = 0.0
+    assert _refused(p)[0] == api.ERR_INVALID
