@@ -5,6 +5,7 @@
   python -m metallic_glasses_gb300.timing batch --replicas 256 --events 32
   python -m metallic_glasses_gb300.timing run --config grf256 --events 20000
   python -m metallic_glasses_gb300.timing ensemble --grid 32 --seeds 8
+  python -m metallic_glasses_gb300.timing ensemble --grid 64 --seeds 4 --max-steps 400000 --chunk 20
 
 `kernel` times one per-event kernel of the mixed form launch by launch with
 CUDA events (which = 0: the full per-site kernel, 1: its stress-update half
@@ -17,8 +18,9 @@ context through stz_run, the single-run path). `run` advances one study
 configuration through stz_run and reports its event rate and the stress error
 of its periodic re-solves. `ensemble` runs the mixed and the FP64 plain form
 on the same seeds through a shear loading at low temperature and compares
-their ensemble-mean stress-strain curves. These are the commands the ncu
-summaries are taken on.
+their ensemble-mean stress-strain curves (--fp64-incremental: the FP64
+side by the incremental update instead of a re-solve per event). These are
+the commands the ncu summaries are taken on.
 """
 import argparse
 import ctypes
