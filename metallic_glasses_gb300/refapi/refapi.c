@@ -77,6 +77,18 @@
 #if !defined(MICRO_MEMORY)
 #error "refapi: builds without MICRO_MEMORY are not implemented by the engine (the direction modifier of init.c:572-640 reads the micro-memory state)"
 #endif
+/* ActEnergy sets its direction modifier under one of six names only
+ * (init.c:590-642); with none of them defined it reads the variable
+ * uninitialised (init.c:563). bmgFlags.h:35 spells the cubic scheme
+ * SF_Cubic_FWD, a name init.c does not test. */
+#if !defined(SF_LINEAR_FWD) && !defined(SF_LINEAR_BWD) && !defined(SF_EVEN) && !defined(SF_SQUARE_FWD) && \
+    !defined(SF_CUBIC_FWD) && !defined(SF_GAUSS_FWD)
+#if defined(SF_Cubic_FWD)
+#error "refapi: SF_Cubic_FWD selects no scheme in ActEnergy (init.c:622 tests SF_CUBIC_FWD); define SF_CUBIC_FWD"
+#else
+#error "refapi: no softening-direction scheme (SF_LINEAR_FWD, SF_LINEAR_BWD, SF_EVEN, SF_SQUARE_FWD, SF_CUBIC_FWD, SF_GAUSS_FWD) is defined; ActEnergy would read its direction modifier uninitialised (init.c:563)"
+#endif
+#endif
 
 static stz_ctx* g_ctx = NULL;
 static stz_params g_p;
@@ -290,18 +302,19 @@ void Alloc(void) {
 #elif defined(COMPRESSION)
   g_p.loading = STZ_LOAD_COMPRESSION;
 #endif
+  /* the first scheme defined in ActEnergy's order wins (init.c:590-642) */
 #if defined(SF_LINEAR_FWD)
   g_p.sf_scheme = STZ_SF_LINEAR_FWD;
 #elif defined(SF_LINEAR_BWD)
   g_p.sf_scheme = STZ_SF_LINEAR_BWD;
 #elif defined(SF_EVEN)
   g_p.sf_scheme = STZ_SF_EVEN;
+#elif defined(SF_SQUARE_FWD)
+  g_p.sf_scheme = STZ_SF_SQUARE_FWD;
 #elif defined(SF_CUBIC_FWD)
   g_p.sf_scheme = STZ_SF_CUBIC_FWD;
 #elif defined(SF_GAUSS_FWD)
   g_p.sf_scheme = STZ_SF_GAUSS_FWD;
-#else
-  g_p.sf_scheme = STZ_SF_SQUARE_FWD;
 #endif
 #ifdef NO_SUBTRACT_ERROR
   g_p.no_subtract_error = 1;

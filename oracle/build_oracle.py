@@ -55,15 +55,18 @@ def ref_available():
     return os.path.isdir(REF_DIR)
 
 
-def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False):
+def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False, sf=None):
     """Compile the reference at an NX x NY grid; returns the binary path.
     full_tensor: also define FULL_TENSOR_RECORD, so that the reference's main
-    writes Eps0 and Sigma of every print as .iout records (bmg.c:269-277)."""
+    writes Eps0 and Sigma of every print as .iout records (bmg.c:269-277).
+    sf: the softening-direction scheme (an STZ_SF_* number) in place of
+    bmgFlags.h's, through the stand-ins' STZ_SHIM_SF."""
     if not ref_available():
         raise FileNotFoundError("reference tree not present")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
-    out = os.path.join(out_dir, "ref2d_%dx%d_%s%s" % (nx, ny, loading, "_ftr" if full_tensor else ""))
+    out = os.path.join(out_dir, "ref2d_%dx%d_%s%s%s" % (nx, ny, loading, "_ftr" if full_tensor else "",
+                                                        "" if sf is None else "_sf%d" % sf))
     mine = [os.path.join(HERE, f) for f in ("ref_wrap.c", "stz_oracle.c", "stz_oracle.h",
                                             "shim/shim.c", "shim/mpi.h", "shim/fftw_mpi.h",
                                             "shim/gsl/gsl_rng.h", "shim/gsl/gsl_randist.h")]
@@ -75,6 +78,8 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False)
         defs.append("-DSTZ_SHIM_LOAD_SHEAR")
     if full_tensor:
         defs.append("-DFULL_TENSOR_RECORD")
+    if sf is not None:
+        defs.append("-DSTZ_SHIM_SF=%d" % sf)
     inc = ["-I", os.path.join(HERE, "shim"), "-I", REF_DIR]
     wraps = ["-Wl,--wrap=VoxelShearTransform", "-Wl,--wrap=KMC",
              "-Wl,--wrap=athermal_plasticity", "-Wl,--wrap=ActEnergy", "-Wl,--wrap=Free"]

@@ -34,7 +34,9 @@ void fftw_free(void* p);
  * build passes -DSTZ_SHIM_NX=.. -DSTZ_SHIM_NY=.., the second inclusion
  * replaces the grid size for the rest of the translation unit, so the
  * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR swaps the
- * loading switch of bmgFlags.h the same way.
+ * loading switch of bmgFlags.h the same way, and STZ_SHIM_SF=k its softening-
+ * direction scheme (k as STZ_SF_*: 0 LINEAR_FWD, 1 LINEAR_BWD, 2 EVEN,
+ * 3 SQUARE_FWD, 4 CUBIC_FWD, 5 GAUSS_FWD; the names ActEnergy tests).
  */
 #if defined(NX) && defined(STZ_SHIM_NX)
 #undef NX
@@ -49,5 +51,28 @@ void fftw_free(void* p);
 #undef COMPRESSION
 #ifndef SHEAR
 #define SHEAR
+#endif
+#endif
+#if defined(H_BMGFLAGS) && defined(STZ_SHIM_SF)
+#undef SF_LINEAR_FWD
+#undef SF_LINEAR_BWD
+#undef SF_EVEN
+#undef SF_SQUARE_FWD
+#undef SF_CUBIC_FWD
+#undef SF_GAUSS_FWD
+#if STZ_SHIM_SF == 0
+#define SF_LINEAR_FWD
+#elif STZ_SHIM_SF == 1
+#define SF_LINEAR_BWD
+#elif STZ_SHIM_SF == 2
+#define SF_EVEN
+#elif STZ_SHIM_SF == 3
+#define SF_SQUARE_FWD
+#elif STZ_SHIM_SF == 4
+#define SF_CUBIC_FWD
+#elif STZ_SHIM_SF == 5
+#define SF_GAUSS_FWD
+#else
+#error "STZ_SHIM_SF must be 0..5"
 #endif
 #endif

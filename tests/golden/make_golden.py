@@ -30,6 +30,8 @@ directory and stores, per case:
                actq       float64 [K, 2] the reference's actQ.out (MRO type of
                                    the chosen site, its Q), one row per thermal event
                structure  (InitMRO 1 cases) the MROstructure.ms the run read
+             cases of another softening-direction scheme (SF_CASES) also:
+               sf         int64      the scheme (STZ_SF_*) the reference was built with
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
@@ -72,6 +74,18 @@ MRO_CASES = {
 }
 
 
+# cases of the other softening-direction schemes of ActEnergy (init.c:590-642;
+# bmgFlags.h ships SF_SQUARE_FWD): (nx, ny, loading, input overrides, thermal
+# events, STZ_SF_* number)
+SF_CASES = {
+    "ref2d_32_sf_linear_fwd_s21": (32, 32, "TENSION", {"end": "0.5", "seed": "21"}, 1500, 0),
+    "ref2d_32_sf_linear_bwd_s22": (32, 32, "TENSION", {"end": "0.5", "seed": "22"}, 1500, 1),
+    "ref2d_32_sf_even_s23": (32, 32, "TENSION", {"end": "0.5", "seed": "23"}, 1500, 2),
+    "ref2d_32_sf_cubic_fwd_s24": (32, 32, "TENSION", {"end": "0.5", "seed": "24"}, 1500, 4),
+    "ref2d_32_sf_gauss_fwd_s25": (32, 32, "TENSION", {"end": "0.5", "seed": "25"}, 1500, 5),
+}
+
+
 def mro_structure(nx, ny, seed=2024):
     """A structure file in the reference's MROstructure.ms layout (one line
     per site in site order: 1-based i, 1-based j, type, angle): types 0/1/2/3
@@ -83,9 +97,9 @@ def mro_structure(nx, ny, seed=2024):
     return "\n".join(lines) + "\n"
 
 
-def run_case(name, nx, ny, loading, overrides, events, mro=False):
+def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None):
     ftr = name in IOUT_CASES
-    exe = build_ref2d(nx, ny, loading, full_tensor=ftr)
+    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
     structure = None
@@ -145,6 +159,8 @@ def run_case(name, nx, ny, loading, overrides, events, mro=False):
                      actq=np.loadtxt(os.path.join(d, "actQ.out"), ndmin=2))
         if structure is not None:
             extra["structure"] = structure
+    if sf is not None:
+        extra["sf"] = np.int64(sf)
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
@@ -219,3 +235,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev) in MRO_CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev, mro=True)
+    for name, (nx, ny, loading, ov, ev, sf) in SF_CASES.items():
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev, sf=sf)

@@ -10,12 +10,19 @@ CASES = ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_
 
 MRO_CASES = ["ref2d_32_mro_s11", "ref2d_32_mrofile_s13"]
 
+# the reference built with each of the other softening-direction schemes
+SF_CASES = ["ref2d_32_sf_linear_fwd_s21", "ref2d_32_sf_linear_bwd_s22", "ref2d_32_sf_even_s23",
+            "ref2d_32_sf_cubic_fwd_s24", "ref2d_32_sf_gauss_fwd_s25"]
+
 
 def params_for(g, **kw):
     ov = ast.literal_eval(str(g["overrides"]))
     loading = api.LOAD_SHEAR if str(g["loading"]) == "SHEAR" else api.LOAD_TENSION
     structure = str(g["structure"]) if "structure" in g.files else None
-    return configs.ref2d(int(g["nx"]), int(g["ny"]), loading=loading, mro_structure=structure, **kw, **ov)
+    p = configs.ref2d(int(g["nx"]), int(g["ny"]), loading=loading, mro_structure=structure, **kw, **ov)
+    if "sf" in g.files:
+        p.sf_scheme = int(g["sf"])
+    return p
 
 
 def check_mro_state(m, g, exact=True):

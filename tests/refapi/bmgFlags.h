@@ -2,7 +2,8 @@
  * 2D fixtures (tension loading, square-forward softening directions, the
  * low-temperature material branch, micro memory, the inhomogeneous-solver
  * entry point, the reduced softening of crystal-like sites). Written for the
- * tests; the names are the reference's. */
+ * tests; the names are the reference's. REFAPI_TEST_NO_SF leaves the
+ * softening-direction scheme to the command line. */
 #ifndef H_BMGFLAGS
 #define H_BMGFLAGS
 #ifdef REFAPI_TEST_SHEAR
@@ -10,7 +11,9 @@
 #else
 #define TENSION
 #endif
+#ifndef REFAPI_TEST_NO_SF
 #define SF_SQUARE_FWD
+#endif
 #define LOW_T
 #ifndef REFAPI_TEST_NO_MICRO_MEMORY
 #define MICRO_MEMORY

@@ -189,6 +189,8 @@ REFUSED_SWITCHES = [
     (["-DXTAL_VARIANTS"], "XTAL_VARIANTS"),
     (["-DSTRESS_FREE_BOUNDARY"], "STRESS_FREE_BOUNDARY"),
     (["-DREFAPI_TEST_NO_MICRO_MEMORY"], "MICRO_MEMORY"),
+    (["-DREFAPI_TEST_NO_SF"], "no softening-direction scheme"),
+    (["-DREFAPI_TEST_NO_SF", "-DSF_Cubic_FWD"], "SF_Cubic_FWD"),
 ]
 
 
@@ -200,9 +202,30 @@ def _syntax_check(defs):
 
 def test_drop_in_compiles_with_the_implemented_switches():
     for defs in ([], ["-DREFAPI_TEST_SHEAR"], ["-DNO_SUBTRACT_ERROR"], ["-DFULL_TENSOR_RECORD"],
-                 ["-DPRE_RELAXATION", "-DUNIFORM_DEFECTS", "-DSTZ_DILATATION"]):
+                 ["-DPRE_RELAXATION", "-DUNIFORM_DEFECTS", "-DSTZ_DILATATION"],
+                 ["-DREFAPI_TEST_NO_SF", "-DSF_CUBIC_FWD"], ["-DREFAPI_TEST_NO_SF", "-DSF_GAUSS_FWD"]):
         r = _syntax_check(defs)
         assert r.returncode == 0, (defs, r.stderr[-2000:])
+
+
+@pytest.mark.parametrize("defs,scheme", [
+    ([], "SQUARE_FWD"),
+    (["-DSF_CUBIC_FWD"], "SQUARE_FWD"),
+    (["-DSF_LINEAR_BWD"], "LINEAR_BWD"),
+    (["-DSF_EVEN"], "EVEN"),
+    (["-DREFAPI_TEST_NO_SF", "-DSF_GAUSS_FWD"], "GAUSS_FWD"),
+    (["-DREFAPI_TEST_NO_SF", "-DSF_CUBIC_FWD", "-DSF_GAUSS_FWD"], "CUBIC_FWD"),
+])
+def test_drop_in_takes_the_scheme_actenergy_takes(defs, scheme):
+    """With several SF_* switches defined, the first in ActEnergy's order
+    (init.c:590-642) is the one the reference runs; the drop-in passes the
+    same scheme to the engine."""
+    cmd = (["gcc", "-E", "-P", "-std=gnu11", *defs, "-DREFAPI_NX=8", "-DREFAPI_NY=8", "-I", TESTHDR,
+            "-I", SHIM, "-I", os.path.join(ROOT, "include"), REFAPI])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = [ln.split("=")[1].strip(" ;") for ln in r.stdout.splitlines() if "g_p.sf_scheme =" in ln]
+    assert got == ["STZ_SF_" + scheme]
 
 
 @pytest.mark.parametrize("defs,name", REFUSED_SWITCHES, ids=[n for _, n in REFUSED_SWITCHES])
