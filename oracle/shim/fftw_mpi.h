@@ -33,8 +33,9 @@ void fftw_free(void* p);
  * includes this header a second time (through my_fft.h) after bmg.h. When the
  * build passes -DSTZ_SHIM_NX=.. -DSTZ_SHIM_NY=.., the second inclusion
  * replaces the grid size for the rest of the translation unit, so the
- * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR swaps the
- * loading switch of bmgFlags.h the same way, and STZ_SHIM_SF=k its softening-
+ * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR and
+ * STZ_SHIM_LOAD_COMPRESSION swap the loading switch of bmgFlags.h the same
+ * way, and STZ_SHIM_SF=k its softening-
  * direction scheme (k as STZ_SF_*: 0 LINEAR_FWD, 1 LINEAR_BWD, 2 EVEN,
  * 3 SQUARE_FWD, 4 CUBIC_FWD, 5 GAUSS_FWD; the names ActEnergy tests).
  */
@@ -51,6 +52,13 @@ void fftw_free(void* p);
 #undef COMPRESSION
 #ifndef SHEAR
 #define SHEAR
+#endif
+#endif
+#if defined(H_BMGFLAGS) && defined(STZ_SHIM_LOAD_COMPRESSION)
+#undef TENSION
+#undef SHEAR
+#ifndef COMPRESSION
+#define COMPRESSION
 #endif
 #endif
 #if defined(H_BMGFLAGS) && defined(STZ_SHIM_SF)

@@ -32,6 +32,8 @@ directory and stores, per case:
                structure  (InitMRO 1 cases) the MROstructure.ms the run read
              cases of another softening-direction scheme (SF_CASES) also:
                sf         int64      the scheme (STZ_SF_*) the reference was built with
+             cases built with NO_SUBTRACT_ERROR (SWITCH_CASES) also:
+               nse        int64      1
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
@@ -86,6 +88,17 @@ SF_CASES = {
 }
 
 
+# the athermal and loading error correction switched off (NO_SUBTRACT_ERROR,
+# evolution.c:91-95, 262-310): (nx, ny, loading, input overrides, thermal
+# events, NO_SUBTRACT_ERROR). The reference's main does not compile under
+# COMPRESSION (its print test, bmg.c:181-187, opens a block under TENSION and
+# SHEAR only), so that switch has no fixture.
+SWITCH_CASES = {
+    "ref2d_32_tension_nse_s32": (32, 32, "TENSION", {"end": "0.5", "seed": "32"}, 1500, True),
+    "ref2d_32_shear_nse_s33": (32, 32, "SHEAR", {"end": "0.5", "seed": "33"}, 1500, True),
+}
+
+
 def mro_structure(nx, ny, seed=2024):
     """A structure file in the reference's MROstructure.ms layout (one line
     per site in site order: 1-based i, 1-based j, type, angle): types 0/1/2/3
@@ -97,9 +110,9 @@ def mro_structure(nx, ny, seed=2024):
     return "\n".join(lines) + "\n"
 
 
-def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None):
+def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=False):
     ftr = name in IOUT_CASES
-    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf)
+    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf, no_subtract_error=nse)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
     structure = None
@@ -161,6 +174,8 @@ def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None):
             extra["structure"] = structure
     if sf is not None:
         extra["sf"] = np.int64(sf)
+    if nse:
+        extra["nse"] = np.int64(1)
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
@@ -238,3 +253,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev, sf) in SF_CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev, sf=sf)
+    for name, (nx, ny, loading, ov, ev, nse) in SWITCH_CASES.items():
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev, nse=nse)

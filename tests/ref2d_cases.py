@@ -14,6 +14,9 @@ MRO_CASES = ["ref2d_32_mro_s11", "ref2d_32_mrofile_s13"]
 SF_CASES = ["ref2d_32_sf_linear_fwd_s21", "ref2d_32_sf_linear_bwd_s22", "ref2d_32_sf_even_s23",
             "ref2d_32_sf_cubic_fwd_s24", "ref2d_32_sf_gauss_fwd_s25"]
 
+# the reference built with NO_SUBTRACT_ERROR, under TENSION and SHEAR
+SWITCH_CASES = ["ref2d_32_tension_nse_s32", "ref2d_32_shear_nse_s33"]
+
 
 def params_for(g, **kw):
     ov = ast.literal_eval(str(g["overrides"]))
@@ -22,6 +25,8 @@ def params_for(g, **kw):
     p = configs.ref2d(int(g["nx"]), int(g["ny"]), loading=loading, mro_structure=structure, **kw, **ov)
     if "sf" in g.files:
         p.sf_scheme = int(g["sf"])
+    if "nse" in g.files:
+        p.no_subtract_error = int(g["nse"])
     return p
 
 

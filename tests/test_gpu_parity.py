@@ -10,7 +10,7 @@ import pytest
 
 from conftest import golden
 from metallic_glasses_gb300 import api, configs
-from ref2d_cases import MRO_CASES, SF_CASES, check_mro_state, params_for
+from ref2d_cases import MRO_CASES, SF_CASES, SWITCH_CASES, check_mro_state, params_for
 
 pytestmark = pytest.mark.gpu
 
@@ -74,7 +74,7 @@ def _shear_prefix_ok(eng, g):
 
 
 @pytest.mark.parametrize("case", ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5"] + MRO_CASES +
-                         SF_CASES)
+                         SF_CASES + SWITCH_CASES)
 def test_ref2d_event_sequence_matches_reference(engine_lib, case):
     g = golden(case)
     p = params_for(g)
