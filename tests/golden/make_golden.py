@@ -34,6 +34,8 @@ directory and stores, per case:
                sf         int64      the scheme (STZ_SF_*) the reference was built with
              cases built with NO_SUBTRACT_ERROR (SWITCH_CASES) also:
                nse        int64      1
+             MRO cases built without NO_SF_XTAL_MRO (MRO_SWITCH_CASES) also:
+               xsf        int64      0
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
@@ -99,6 +101,14 @@ SWITCH_CASES = {
 }
 
 
+# crystal-like sites with bmgFlags.h's NO_SF_XTAL_MRO taken out (ActEnergy
+# then leaves their direction modifier and softening unscaled, init.c:645-668)
+MRO_SWITCH_CASES = {
+    "ref2d_32_mro_xsfoff_s11": (32, 32, "TENSION", {"end": "0.5", "seed": "11", "xfrac": "0.15", "xq0": "1.8"},
+                                3000),
+}
+
+
 def mro_structure(nx, ny, seed=2024):
     """A structure file in the reference's MROstructure.ms layout (one line
     per site in site order: 1-based i, 1-based j, type, angle): types 0/1/2/3
@@ -110,9 +120,9 @@ def mro_structure(nx, ny, seed=2024):
     return "\n".join(lines) + "\n"
 
 
-def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=False):
+def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=False, xsf=True):
     ftr = name in IOUT_CASES
-    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf, no_subtract_error=nse)
+    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf, no_subtract_error=nse, no_sf_xtal_mro=xsf)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
     structure = None
@@ -176,6 +186,8 @@ def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=F
         extra["sf"] = np.int64(sf)
     if nse:
         extra["nse"] = np.int64(1)
+    if not xsf:
+        extra["xsf"] = np.int64(0)
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
@@ -256,3 +268,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev, nse) in SWITCH_CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev, nse=nse)
+    for name, (nx, ny, loading, ov, ev) in MRO_SWITCH_CASES.items():
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev, mro=True, xsf=False)

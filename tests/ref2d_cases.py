@@ -17,6 +17,9 @@ SF_CASES = ["ref2d_32_sf_linear_fwd_s21", "ref2d_32_sf_linear_bwd_s22", "ref2d_3
 # the reference built with NO_SUBTRACT_ERROR, under TENSION and SHEAR
 SWITCH_CASES = ["ref2d_32_tension_nse_s32", "ref2d_32_shear_nse_s33"]
 
+# crystal-like sites with the reference built without NO_SF_XTAL_MRO
+MRO_SWITCH_CASES = ["ref2d_32_mro_xsfoff_s11"]
+
 
 def params_for(g, **kw):
     ov = ast.literal_eval(str(g["overrides"]))
@@ -27,6 +30,8 @@ def params_for(g, **kw):
         p.sf_scheme = int(g["sf"])
     if "nse" in g.files:
         p.no_subtract_error = int(g["nse"])
+    if "xsf" in g.files:
+        p.no_sf_xtal_mro = int(g["xsf"])
     return p
 
 

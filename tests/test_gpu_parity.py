@@ -118,10 +118,10 @@ def test_ref2d_event_sequence_matches_reference(engine_lib, case):
 @pytest.mark.parametrize("no_sf", [1, 0])
 def test_mro_map_matches_oracle(engine_lib, oracle_lib, no_sf):
     """Crystal-like sites drawn at 15 % (seed 11, 32^2, softening on) with the
-    NO_SF_XTAL_MRO switch as shipped and switched off (the reference's own build
-    only exists with it on, so the oracle's restatement is the pin there): the
-    engine takes the oracle's transformations for 1500 thermal events, fields
-    within 1e-10."""
+    NO_SF_XTAL_MRO switch as shipped and switched off: the engine takes the
+    oracle's transformations for 1500 thermal events, fields within 1e-10. The
+    oracle is pinned bit for bit to the reference built either way on the same
+    input (fixtures ref2d_32_mro_s11 and ref2d_32_mro_xsfoff_s11)."""
     from oracle import pyoracle
     kw = dict(end="0.5", seed="11", xfrac="0.15", xq0="1.8")
     p = configs.ref2d(32, 32, **kw)
