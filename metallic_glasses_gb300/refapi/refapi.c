@@ -74,8 +74,12 @@
 #if defined(STRESS_FREE_BOUNDARY)
 #error "refapi: STRESS_FREE_BOUNDARY (elastic.c:220-262) is not implemented by the engine"
 #endif
-#if !defined(MICRO_MEMORY)
-#error "refapi: builds without MICRO_MEMORY are not implemented by the engine (the direction modifier of init.c:572-640 reads the micro-memory state)"
+/* Without MICRO_MEMORY the reference declares no PreDEps0 (bmg.h:236-240), so
+ * its ActEnergy compiles only when the scheme it takes is SF_EVEN, the one
+ * scheme that reads no memory. That build is the engine's SF_EVEN (its memory
+ * then unused); the others are refused, as the reference does not build. */
+#if !defined(MICRO_MEMORY) && (defined(SF_LINEAR_FWD) || defined(SF_LINEAR_BWD) || !defined(SF_EVEN))
+#error "refapi: builds without MICRO_MEMORY need SF_EVEN as the softening-direction scheme (the other schemes read PreDEps0, which the reference declares only under MICRO_MEMORY, bmg.h:236-240)"
 #endif
 /* ActEnergy sets its direction modifier under one of six names only
  * (init.c:590-642); with none of them defined it reads the variable

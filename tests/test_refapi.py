@@ -189,6 +189,7 @@ REFUSED_SWITCHES = [
     (["-DXTAL_VARIANTS"], "XTAL_VARIANTS"),
     (["-DSTRESS_FREE_BOUNDARY"], "STRESS_FREE_BOUNDARY"),
     (["-DREFAPI_TEST_NO_MICRO_MEMORY"], "MICRO_MEMORY"),
+    (["-DREFAPI_TEST_NO_MICRO_MEMORY", "-DSF_EVEN", "-DSF_LINEAR_BWD"], "MICRO_MEMORY"),
     (["-DREFAPI_TEST_NO_SF"], "no softening-direction scheme"),
     (["-DREFAPI_TEST_NO_SF", "-DSF_Cubic_FWD"], "SF_Cubic_FWD"),
 ]
@@ -203,7 +204,8 @@ def _syntax_check(defs):
 def test_drop_in_compiles_with_the_implemented_switches():
     for defs in ([], ["-DREFAPI_TEST_SHEAR"], ["-DNO_SUBTRACT_ERROR"], ["-DFULL_TENSOR_RECORD"],
                  ["-DPRE_RELAXATION", "-DUNIFORM_DEFECTS", "-DSTZ_DILATATION"],
-                 ["-DREFAPI_TEST_NO_SF", "-DSF_CUBIC_FWD"], ["-DREFAPI_TEST_NO_SF", "-DSF_GAUSS_FWD"]):
+                 ["-DREFAPI_TEST_NO_SF", "-DSF_CUBIC_FWD"], ["-DREFAPI_TEST_NO_SF", "-DSF_GAUSS_FWD"],
+                 ["-DREFAPI_TEST_NO_MICRO_MEMORY", "-DREFAPI_TEST_NO_SF", "-DSF_EVEN"]):
         r = _syntax_check(defs)
         assert r.returncode == 0, (defs, r.stderr[-2000:])
 
@@ -215,6 +217,7 @@ def test_drop_in_compiles_with_the_implemented_switches():
     (["-DSF_EVEN"], "EVEN"),
     (["-DREFAPI_TEST_NO_SF", "-DSF_GAUSS_FWD"], "GAUSS_FWD"),
     (["-DREFAPI_TEST_NO_SF", "-DSF_CUBIC_FWD", "-DSF_GAUSS_FWD"], "CUBIC_FWD"),
+    (["-DREFAPI_TEST_NO_MICRO_MEMORY", "-DREFAPI_TEST_NO_SF", "-DSF_EVEN"], "EVEN"),
 ])
 def test_drop_in_takes_the_scheme_actenergy_takes(defs, scheme):
     """With several SF_* switches defined, the first in ActEnergy's order
