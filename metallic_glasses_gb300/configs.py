@@ -87,6 +87,30 @@ def read_mro_structure(text, nx, ny):
     return types, theta
 
 
+def high_t_material(p, branch):
+    """The moduli and barrier amplitude of the reference's high-temperature
+    material branches of Init() (bmgFlags.h HIGH_T_Vit1 / HIGH_T_PdNiP,
+    init.c:28-42, with bmg.h:36-48's constants), in place of what the input
+    file's LOW_T derivation gave (init.c:18-27): Vit1 follows the glass /
+    supercooled-liquid interpolation in tanh((T - Tg)/DeltaE), PdNiP fixed
+    values; lambda as in init.c:44. Returns p."""
+    T = p.temperature
+    if branch == "HIGH_T_Vit1":
+        Tg = 623.
+        E = (80.7 + 30.0) / 2. - (80.7 - 30.0) * math.tanh((T - Tg) / 24.0) / 2. - 39.0E-3 * (T - Tg)
+        nu = (0.360 + 0.447) / 2. - (0.360 - 0.447) * math.tanh((T - Tg) / 24.0) / 2.
+        q0 = 2.2
+    elif branch == "HIGH_T_PdNiP":
+        E, nu, q0 = 96., 0.36, 3.0
+    else:
+        raise ValueError("material branch %r" % branch)
+    p.young, p.poisson = E, nu
+    p.mu = E / (2 + 2 * nu)
+    p.lambda_ = E * nu / (1 - nu * nu)
+    p.q0_mean = q0
+    return p
+
+
 def ref2d(nx=64, ny=64, input_path=None, loading=api.LOAD_TENSION, defaults=None, from_input=None,
           mro_structure=None, solver=None, **overrides):
     p = (defaults or api.default_params)(api.MODEL_REF2D)

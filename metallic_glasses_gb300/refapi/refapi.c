@@ -170,13 +170,30 @@ void ReadInput(FILE* in) {
   memcpy(ResStressDataFile, res, sizeof(res));
 }
 
-/* init.c:6-75: derived constants (the 2D LOW_T branch and the common part) */
+/* init.c:6-75: derived constants. The 2D material branch in Init()'s order
+ * (XTAL_VARIANTS is refused above): LOW_T from the input's moduli, or a
+ * high-temperature alloy whose moduli and barrier amplitude replace the
+ * input's, from the constants of the caller's bmg.h (bmg.h:36-48); then the
+ * common part. */
 void Init(void) {
 #if defined(LOW_T)
   nu *= 2;
   mu = E / (2 + 2 * nu);
-#elif defined(XTAL_VARIANTS) || defined(HIGH_T_Vit1) || defined(HIGH_T_PdNiP)
-#error "refapi: only the LOW_T material branch of Init() is provided"
+#elif defined(HIGH_T_Vit1)
+  {
+    const double glass = tanh((T__K - Tg__K) / DeltaE);
+    E = (E_gl + E_sc) / 2. - (E_gl - E_sc) * glass / 2. - k_E * (T__K - Tg__K);
+    nu = (nu_gl + nu_sc) / 2. - (nu_gl - nu_sc) * glass / 2.;
+  }
+  mu = E / (2 + 2 * nu);
+  Q0amp = 2.2;
+#elif defined(HIGH_T_PdNiP)
+  E = 96;
+  nu = 0.36;
+  mu = E / (2 + 2 * nu);
+  Q0amp = 3.0;
+#else
+#error "refapi: no material branch of Init() (LOW_T, HIGH_T_Vit1 or HIGH_T_PdNiP) is defined"
 #endif
   lambda = E * nu / (1 - nu * nu);
   alpha = (1 + nu) / 2;
@@ -601,6 +618,9 @@ void PrintFlags(void) {
 #endif
 #ifdef LOW_T
   printf("#define LOW_T\n");
+#endif
+#ifdef HIGH_T_Vit1
+  printf("#define HIGH_T_Vit1\n");
 #endif
 }
 

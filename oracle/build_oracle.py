@@ -56,7 +56,7 @@ def ref_available():
 
 
 def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False, sf=None,
-                no_subtract_error=False, no_sf_xtal_mro=True):
+                no_subtract_error=False, no_sf_xtal_mro=True, material=None):
     """Compile the reference at an NX x NY grid; returns the binary path.
     full_tensor: also define FULL_TENSOR_RECORD, so that the reference's main
     writes Eps0 and Sigma of every print as .iout records (bmg.c:269-277).
@@ -64,14 +64,16 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False,
     bmgFlags.h's, through the stand-ins' STZ_SHIM_SF. loading: TENSION,
     SHEAR or COMPRESSION. no_subtract_error: also define NO_SUBTRACT_ERROR
     (commented out in bmgFlags.h). no_sf_xtal_mro False: take bmgFlags.h's
-    NO_SF_XTAL_MRO out (STZ_SHIM_XTAL_SF_OFF)."""
+    NO_SF_XTAL_MRO out (STZ_SHIM_XTAL_SF_OFF). material: HIGH_T_Vit1 or
+    HIGH_T_PdNiP in place of bmgFlags.h's LOW_T (STZ_SHIM_NO_LOW_T)."""
     if not ref_available():
         raise FileNotFoundError("reference tree not present")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "ref2d_%dx%d_%s%s%s" % (nx, ny, loading, "_ftr" if full_tensor else "",
                                                         "" if sf is None else "_sf%d" % sf) +
-                       ("_nse" if no_subtract_error else "") + ("" if no_sf_xtal_mro else "_xsfoff"))
+                       ("_nse" if no_subtract_error else "") + ("" if no_sf_xtal_mro else "_xsfoff") +
+                       ("" if material is None else "_" + material))
     mine = [os.path.join(HERE, f) for f in ("ref_wrap.c", "stz_oracle.c", "stz_oracle.h",
                                             "shim/shim.c", "shim/mpi.h", "shim/fftw_mpi.h",
                                             "shim/gsl/gsl_rng.h", "shim/gsl/gsl_randist.h")]
@@ -93,6 +95,10 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False,
         defs.append("-DNO_SUBTRACT_ERROR")
     if not no_sf_xtal_mro:
         defs.append("-DSTZ_SHIM_XTAL_SF_OFF")
+    if material is not None:
+        if material not in ("HIGH_T_Vit1", "HIGH_T_PdNiP"):
+            raise ValueError("material %r" % material)
+        defs += ["-D" + material, "-DSTZ_SHIM_NO_LOW_T"]
     inc = ["-I", os.path.join(HERE, "shim"), "-I", REF_DIR]
     wraps = ["-Wl,--wrap=VoxelShearTransform", "-Wl,--wrap=KMC",
              "-Wl,--wrap=athermal_plasticity", "-Wl,--wrap=ActEnergy", "-Wl,--wrap=Free"]

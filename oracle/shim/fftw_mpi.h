@@ -35,7 +35,9 @@ void fftw_free(void* p);
  * replaces the grid size for the rest of the translation unit, so the
  * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR and
  * STZ_SHIM_LOAD_COMPRESSION swap the loading switch of bmgFlags.h the same
- * way, STZ_SHIM_XTAL_SF_OFF takes NO_SF_XTAL_MRO out, and STZ_SHIM_SF=k its
+ * way, STZ_SHIM_XTAL_SF_OFF takes NO_SF_XTAL_MRO out, STZ_SHIM_NO_LOW_T takes
+ * LOW_T out (for a HIGH_T_* material branch defined on the command line, which
+ * bmg.h's Tg__K needs before this point), and STZ_SHIM_SF=k the
  * softening-
  * direction scheme (k as STZ_SF_*: 0 LINEAR_FWD, 1 LINEAR_BWD, 2 EVEN,
  * 3 SQUARE_FWD, 4 CUBIC_FWD, 5 GAUSS_FWD; the names ActEnergy tests).
@@ -61,6 +63,9 @@ void fftw_free(void* p);
 #ifndef COMPRESSION
 #define COMPRESSION
 #endif
+#endif
+#if defined(H_BMGFLAGS) && defined(STZ_SHIM_NO_LOW_T)
+#undef LOW_T
 #endif
 #if defined(H_BMGFLAGS) && defined(STZ_SHIM_XTAL_SF_OFF)
 #undef NO_SF_XTAL_MRO

@@ -36,6 +36,8 @@ directory and stores, per case:
                nse        int64      1
              MRO cases built without NO_SF_XTAL_MRO (MRO_SWITCH_CASES) also:
                xsf        int64      0
+             cases of a high-temperature material branch (MATERIAL_CASES) also:
+               material   str        HIGH_T_Vit1 or HIGH_T_PdNiP
 and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
@@ -109,6 +111,14 @@ MRO_SWITCH_CASES = {
 }
 
 
+# the high-temperature material branches of Init() in place of LOW_T
+# (init.c:28-42): (nx, ny, loading, input overrides, thermal events, branch)
+MATERIAL_CASES = {
+    "ref2d_32_vit1_s41": (32, 32, "TENSION", {"end": "0.5", "seed": "41"}, 1500, "HIGH_T_Vit1"),
+    "ref2d_32_pdnip_s42": (32, 32, "TENSION", {"end": "0.5", "seed": "42"}, 1500, "HIGH_T_PdNiP"),
+}
+
+
 def mro_structure(nx, ny, seed=2024):
     """A structure file in the reference's MROstructure.ms layout (one line
     per site in site order: 1-based i, 1-based j, type, angle): types 0/1/2/3
@@ -120,9 +130,10 @@ def mro_structure(nx, ny, seed=2024):
     return "\n".join(lines) + "\n"
 
 
-def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=False, xsf=True):
+def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=False, xsf=True, material=None):
     ftr = name in IOUT_CASES
-    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf, no_subtract_error=nse, no_sf_xtal_mro=xsf)
+    exe = build_ref2d(nx, ny, loading, full_tensor=ftr, sf=sf, no_subtract_error=nse, no_sf_xtal_mro=xsf,
+                      material=material)
     d = tempfile.mkdtemp(prefix="stz_ref_")
     configs.write_input(os.path.join(d, "input"), **overrides)
     structure = None
@@ -188,6 +199,8 @@ def run_case(name, nx, ny, loading, overrides, events, mro=False, sf=None, nse=F
         extra["nse"] = np.int64(1)
     if not xsf:
         extra["xsf"] = np.int64(0)
+    if material is not None:
+        extra["material"] = material
     out = os.path.join(HERE, name + ".npz")
     S = np.array(S, np.float64)
     # per-step time for every step; mean strain and stress for every 10th
@@ -271,3 +284,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev) in MRO_SWITCH_CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev, mro=True, xsf=False)
+    for name, (nx, ny, loading, ov, ev, mat) in MATERIAL_CASES.items():
+        if not only or name in only:
+            run_case(name, nx, ny, loading, ov, ev, material=mat)

@@ -20,8 +20,14 @@ SWITCH_CASES = ["ref2d_32_tension_nse_s32", "ref2d_32_shear_nse_s33"]
 # crystal-like sites with the reference built without NO_SF_XTAL_MRO
 MRO_SWITCH_CASES = ["ref2d_32_mro_xsfoff_s11"]
 
+# the reference built with a high-temperature material branch of Init()
+MATERIAL_CASES = ["ref2d_32_vit1_s41", "ref2d_32_pdnip_s42"]
 
-def params_for(g, **kw):
+
+def params_for(g, material=None, **kw):
+    """The engine parameters of fixture g (its input overrides, loading and
+    switches); material "LOW_T" keeps the input file's derivation in place of
+    the fixture's high-temperature branch."""
     ov = ast.literal_eval(str(g["overrides"]))
     loading = api.LOAD_SHEAR if str(g["loading"]) == "SHEAR" else api.LOAD_TENSION
     structure = str(g["structure"]) if "structure" in g.files else None
@@ -32,6 +38,9 @@ def params_for(g, **kw):
         p.no_subtract_error = int(g["nse"])
     if "xsf" in g.files:
         p.no_sf_xtal_mro = int(g["xsf"])
+    material = material or (str(g["material"]) if "material" in g.files else "LOW_T")
+    if material != "LOW_T":
+        configs.high_t_material(p, material)
     return p
 
 

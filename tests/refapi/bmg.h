@@ -28,7 +28,18 @@ typedef double real;
 #define DE 3
 #define MODES 20
 #define T__K 300.
+#if defined(HIGH_T_Vit1)
+#define Tg__K 623.
+#elif defined(HIGH_T_PdNiP)
+#define Tg__K 587.5
+#endif
 #define TRIAL_FREQUENCY 1e13
+#define E_gl 80.7
+#define E_sc 30.0
+#define k_E 39.0E-3
+#define DeltaE 24.0
+#define nu_gl 0.360
+#define nu_sc 0.447
 #define EV_IN_J 1.60217733e-19
 #define J_IN_EV (1 / EV_IN_J)
 #define EPSILON 1e-17

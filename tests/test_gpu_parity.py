@@ -10,7 +10,7 @@ import pytest
 
 from conftest import golden
 from metallic_glasses_gb300 import api, configs
-from ref2d_cases import MRO_CASES, SF_CASES, SWITCH_CASES, check_mro_state, params_for
+from ref2d_cases import MATERIAL_CASES, MRO_CASES, MRO_SWITCH_CASES, SF_CASES, SWITCH_CASES, check_mro_state, params_for
 
 pytestmark = pytest.mark.gpu
 
@@ -74,7 +74,7 @@ def _shear_prefix_ok(eng, g):
 
 
 @pytest.mark.parametrize("case", ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5"] + MRO_CASES +
-                         SF_CASES + SWITCH_CASES)
+                         SF_CASES + SWITCH_CASES + MRO_SWITCH_CASES + MATERIAL_CASES)
 def test_ref2d_event_sequence_matches_reference(engine_lib, case):
     g = golden(case)
     p = params_for(g)
@@ -107,7 +107,7 @@ def test_ref2d_event_sequence_matches_reference(engine_lib, case):
     assert rel_err(eng.field(api.FIELD_TEMP_SOFT), g["temp_soft"]) < FIELD_RTOL
     assert np.allclose(sc["eps_avg"][:3], g["sc"][1:4], rtol=FIELD_RTOL, atol=1e-14)
     assert np.allclose(sc["stress"][:3], g["sc"][4:7], rtol=1e-9, atol=1e-12)
-    if case in MRO_CASES:
+    if case in MRO_CASES + MRO_SWITCH_CASES:
         # the map bit for bit; the modes through the host's cos/sin (glibc of
         # the machine that runs the engine, not the one that made the fixture)
         # and the device-drawn barriers to an ulp

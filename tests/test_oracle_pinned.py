@@ -5,10 +5,11 @@ import pytest
 
 from conftest import golden
 from metallic_glasses_gb300 import api
-from ref2d_cases import CASES, MRO_CASES, MRO_SWITCH_CASES, SF_CASES, SWITCH_CASES, check_mro_state, params_for
+from ref2d_cases import (CASES, MATERIAL_CASES, MRO_CASES, MRO_SWITCH_CASES, SF_CASES, SWITCH_CASES, check_mro_state,
+                         params_for)
 
 
-@pytest.mark.parametrize("case", CASES + MRO_CASES + SF_CASES + SWITCH_CASES + MRO_SWITCH_CASES)
+@pytest.mark.parametrize("case", CASES + MRO_CASES + SF_CASES + SWITCH_CASES + MRO_SWITCH_CASES + MATERIAL_CASES)
 def test_oracle_matches_reference_bitwise(oracle_lib, engine_lib, case):
     g = golden(case)
     p = params_for(g)
@@ -67,6 +68,8 @@ def test_mro_fixtures_take_crystal_like_transformations():
 
 
 def _shipped(g):
+    if "material" in g.files:
+        return params_for(g, material="LOW_T")
     p = params_for(g)
     if "sf" in g.files:
         assert p.sf_scheme == int(g["sf"]) != api.SF_SQUARE_FWD
@@ -80,10 +83,10 @@ def _shipped(g):
     return p
 
 
-@pytest.mark.parametrize("case", SF_CASES + SWITCH_CASES + MRO_SWITCH_CASES)
+@pytest.mark.parametrize("case", SF_CASES + SWITCH_CASES + MRO_SWITCH_CASES + MATERIAL_CASES)
 def test_switch_fixtures_depend_on_their_switch(oracle_lib, engine_lib, case):
-    """Each scheme, NO_SUBTRACT_ERROR or NO_SF_XTAL_MRO fixture is a run of
-    its own switch: the oracle with the switch as shipped leaves the fixture's
+    """Each scheme, NO_SUBTRACT_ERROR, NO_SF_XTAL_MRO or material-branch
+    fixture is a run of its own switch: the oracle with the switch as shipped leaves the fixture's
     transformation sequence within the first quarter of it (within ten
     transformations for the schemes; 23 for NO_SUBTRACT_ERROR under SHEAR,
     which acts through the small normal stresses and after avalanches; 219 of

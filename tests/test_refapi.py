@@ -177,6 +177,30 @@ def test_iout_records_are_the_raw_fields(engine_lib):
         assert np.array_equal(g, 7 * s - 11)
 
 
+@pytest.mark.parametrize("material", ["LOW_T", "HIGH_T_Vit1", "HIGH_T_PdNiP"])
+def test_drop_in_init_material_branches(engine_lib, material):
+    """Init() of the drop-in under each material branch (CPU, no device): the
+    moduli and barrier amplitude the oracle reproduces the reference's own
+    runs with (configs.high_t_material for the high-temperature branches,
+    pinned by the ref2d_32_vit1/pdnip fixtures; the input derivation for
+    LOW_T), to the last bit."""
+    defs = [] if material == "LOW_T" else ["-DREFAPI_TEST_HIGH_T", "-D" + material]
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "init_check")
+        cmd = (["gcc", *CFLAGS, *defs, "-DREFAPI_NX=8", "-DREFAPI_NY=6", "-I", TESTHDR, "-I", SHIM,
+                "-I", os.path.join(ROOT, "include"), os.path.join(TESTHDR, "init_check.c"), REFAPI] + _support() +
+               ["-o", exe] + _lib_args())
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr[-2000:]
+        got = [float(v) for v in r.stdout.split()]
+    p = configs.ref2d(8, 6, E="69.46", nu="0.365", q0amp="2.0")
+    if material != "LOW_T":
+        configs.high_t_material(p, material)
+    assert got == [p.young, p.poisson, p.mu, p.lambda_, p.q0_mean]
+
+
 REFUSED_SWITCHES = [
     (["-DSTRAIN_RATE_SENSITIVITY"], "STRAIN_RATE_SENSITIVITY"),
     (["-DSTRAIN_RATE_SENSITIVITY", "-DLOCAL_RATE_V2"], "LOCAL_RATE_V2"),
@@ -192,6 +216,7 @@ REFUSED_SWITCHES = [
     (["-DREFAPI_TEST_NO_MICRO_MEMORY", "-DSF_EVEN", "-DSF_LINEAR_BWD"], "MICRO_MEMORY"),
     (["-DREFAPI_TEST_NO_SF"], "no softening-direction scheme"),
     (["-DREFAPI_TEST_NO_SF", "-DSF_Cubic_FWD"], "SF_Cubic_FWD"),
+    (["-DREFAPI_TEST_HIGH_T"], "no material branch"),
 ]
 
 
