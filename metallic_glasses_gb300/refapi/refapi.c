@@ -59,8 +59,13 @@
 #if defined(STRAIN_RATE_SENSITIVITY) || defined(LOCAL_RATE_V2)
 #error "refapi: STRAIN_RATE_SENSITIVITY / LOCAL_RATE_V2 (rate-sensitive barriers, init.c:670-682) are not implemented by the engine"
 #endif
-#if defined(RELX_BIMOLE_FLAG) || defined(RELX_FVT_FLAG) || defined(AVG_PERMSOFTENING)
-#error "refapi: RELX_BIMOLE_FLAG / RELX_FVT_FLAG / AVG_PERMSOFTENING (softening relaxation laws, init.c:717-729) are not implemented by the engine"
+/* The two relaxation laws divide by tPerm, which the reference never assigns
+ * (0.0 from bmg.h:177; init.c:50,53 are commented out). */
+#if defined(RELX_BIMOLE_FLAG) || defined(RELX_FVT_FLAG)
+#error "refapi: RELX_BIMOLE_FLAG / RELX_FVT_FLAG (softening relaxation laws, init.c:717-724) are not implemented by the engine; in the reference they divide by tPerm, which is never assigned (0.0)"
+#endif
+#if defined(AVG_PERMSOFTENING)
+#error "refapi: AVG_PERMSOFTENING (the grid-mean permanent softening, init.c:692-709, 725-729) is not implemented by the engine"
 #endif
 #if defined(HEAT_CONDUCT)
 #error "refapi: HEAT_CONDUCT (local heating and conduction, elastic.c:549-582, evolution.c:247-249) is not implemented by the engine"
