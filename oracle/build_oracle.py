@@ -62,7 +62,9 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False,
     writes Eps0 and Sigma of every print as .iout records (bmg.c:269-277).
     sf: the softening-direction scheme (an STZ_SF_* number) in place of
     bmgFlags.h's, through the stand-ins' STZ_SHIM_SF. loading: TENSION,
-    SHEAR or COMPRESSION. no_subtract_error: also define NO_SUBTRACT_ERROR
+    SHEAR (the reference's main does not compile under COMPRESSION: its print
+    test, bmg.c:181-187, opens a block under TENSION and SHEAR only).
+    no_subtract_error: also define NO_SUBTRACT_ERROR
     (commented out in bmgFlags.h). no_sf_xtal_mro False: take bmgFlags.h's
     NO_SF_XTAL_MRO out (STZ_SHIM_XTAL_SF_OFF). material: HIGH_T_Vit1 or
     HIGH_T_PdNiP in place of bmgFlags.h's LOW_T (STZ_SHIM_NO_LOW_T)."""
@@ -83,8 +85,6 @@ def build_ref2d(nx=64, ny=64, loading="TENSION", force=False, full_tensor=False,
     defs = ["-DSTZ_SHIM_NX=%d" % nx, "-DSTZ_SHIM_NY=%d" % ny]
     if loading == "SHEAR":
         defs.append("-DSTZ_SHIM_LOAD_SHEAR")
-    elif loading == "COMPRESSION":
-        defs.append("-DSTZ_SHIM_LOAD_COMPRESSION")
     elif loading != "TENSION":
         raise ValueError("loading %r" % loading)
     if full_tensor:

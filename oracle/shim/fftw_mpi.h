@@ -33,14 +33,19 @@ void fftw_free(void* p);
  * includes this header a second time (through my_fft.h) after bmg.h. When the
  * build passes -DSTZ_SHIM_NX=.. -DSTZ_SHIM_NY=.., the second inclusion
  * replaces the grid size for the rest of the translation unit, so the
- * unmodified sources run at a test-sized grid. STZ_SHIM_LOAD_SHEAR and
- * STZ_SHIM_LOAD_COMPRESSION swap the loading switch of bmgFlags.h the same
- * way, STZ_SHIM_XTAL_SF_OFF takes NO_SF_XTAL_MRO out, STZ_SHIM_NO_LOW_T takes
- * LOW_T out (for a HIGH_T_* material branch defined on the command line, which
- * bmg.h's Tg__K needs before this point), and STZ_SHIM_SF=k the
- * softening-
- * direction scheme (k as STZ_SF_*: 0 LINEAR_FWD, 1 LINEAR_BWD, 2 EVEN,
- * 3 SQUARE_FWD, 4 CUBIC_FWD, 5 GAUSS_FWD; the names ActEnergy tests).
+ * unmodified sources run at a test-sized grid. bmgFlags.h switches change
+ * the same way:
+ *   STZ_SHIM_LOAD_SHEAR   SHEAR in place of TENSION;
+ *   STZ_SHIM_XTAL_SF_OFF  NO_SF_XTAL_MRO taken out;
+ *   STZ_SHIM_NO_LOW_T     LOW_T taken out, for a HIGH_T_* material branch
+ *                         defined on the command line (bmg.h's Tg__K needs it
+ *                         before this point);
+ *   STZ_SHIM_SF=k         the softening-direction scheme, k as STZ_SF_*
+ *                         (0 LINEAR_FWD, 1 LINEAR_BWD, 2 EVEN, 3 SQUARE_FWD,
+ *                         4 CUBIC_FWD, 5 GAUSS_FWD: the names ActEnergy tests).
+ * Every unit includes my_fft.h after bmg.h, so its code sees the changed
+ * switches; only bmg.h's own declarations were made before this point, which
+ * is why a switch that bmg.h reads (MICRO_MEMORY) cannot change here.
  */
 #if defined(NX) && defined(STZ_SHIM_NX)
 #undef NX
@@ -55,13 +60,6 @@ void fftw_free(void* p);
 #undef COMPRESSION
 #ifndef SHEAR
 #define SHEAR
-#endif
-#endif
-#if defined(H_BMGFLAGS) && defined(STZ_SHIM_LOAD_COMPRESSION)
-#undef TENSION
-#undef SHEAR
-#ifndef COMPRESSION
-#define COMPRESSION
 #endif
 #endif
 #if defined(H_BMGFLAGS) && defined(STZ_SHIM_NO_LOW_T)
