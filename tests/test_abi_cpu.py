@@ -33,6 +33,22 @@ def test_library_exports_every_declared_symbol(engine_lib):
     assert not missing, "declared but not exported: %s" % missing
 
 
+@pytest.mark.parametrize("compiler", [["gcc", "-x", "c", "-std=c99"], ["gcc", "-x", "c", "-std=c11"],
+                                      ["g++", "-x", "c++", "-std=c++11"]])
+def test_headers_compile_standalone(compiler, tmp_path):
+    """Each public header is self-contained plain C (and C++) with no warnings
+    under -Wall -Wextra -pedantic: what a C, cgo or FFI binding includes."""
+    import subprocess
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            src = tmp_path / ("use_" + f + ".src")
+            src.write_text('#include "%s"\nint main(void) { return 0; }\n' % f)
+            r = subprocess.run(compiler + ["-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-I", inc,
+                                           str(src)], capture_output=True, text=True)
+            assert r.returncode == 0, (f, r.stderr[-2000:])
+
+
 def test_struct_sizes_match(engine_lib):
     from metallic_glasses_gb300 import api
     assert engine_lib.stz_sizeof(0) == C.sizeof(api.Params)
