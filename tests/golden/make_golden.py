@@ -66,6 +66,8 @@ CASES = {
     # runs into the reference's SHEAR instability stop after its first avalanche
     "ref2d_32_shear_stop_s7": (32, 32, "SHEAR", {"end": "0.5", "seed": "7"}, 100000),
     "ref2d_32_tension_nosoft_s5": (32, 32, "TENSION", {"end": "0.5", "seed": "5", "soft": "0"}, 3000),
+    # a non-square grid: site index i*NY + j and the FFT over unequal axes
+    "ref2d_32x48_tension_s51": (32, 48, "TENSION", {"end": "0.5", "seed": "51"}, 1500),
 }
 
 

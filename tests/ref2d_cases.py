@@ -5,7 +5,8 @@ import numpy as np
 
 from metallic_glasses_gb300 import api, configs
 
-CASES = ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5", "ref2d_32_shear_stop_s7"]
+CASES = ["ref2d_64_tension_s123", "ref2d_32_shear_s7", "ref2d_32_tension_nosoft_s5", "ref2d_32_shear_stop_s7",
+         "ref2d_32x48_tension_s51"]
 
 
 MRO_CASES = ["ref2d_32_mro_s11", "ref2d_32_mrofile_s13"]
