@@ -593,33 +593,53 @@ void WriteScalarMPI_INT(int* field, char* s, int step) { write_record(field, siz
 void WriteMROMPI_INT(int* field, char* s, int step) { write_record(field, sizeof(int), s, step); }
 
 void ParameterPrint(void) {
+  /* the reference's text, byte for byte (io.c:349-372), so that logs of a
+   * drop-in build compare with the reference's */
   printf("\nSimulation Geometry:\n");
   printf("System size:\t[%d x %d]\n", NX, NY);
+  printf("Voxel size:\t[%.3fnm x %.3fnm]\n", (double)LX, (double)LY);
   printf("\nMaterial Properties at T=%f\n", (double)T__K);
-  printf("Activation energy barrier amplitude: \t%.3f\n", Q0amp);
+  printf("Activation energy barrier amplituide: \t%.3f\n", Q0amp);
   printf("Young's modulus:\t%.3f\n", E);
   printf("Shear modulus:\t%.3f\n", mu);
   printf("Poisson's ratio:\t%.3f\n", nu);
+  printf("\nPEL Parameters:\n");
   printf("# of STZ modes:\t%d\n", MODES);
-  printf("Engine: GB300 (stz_api)\n");
+  printf("Stress-free energy barrier prefactor:\t%.3f\n", Q0amp);
+  printf("\nSoftening Parameters:\n");
+  printf("Permanent softening prefactor:\t%.3f\n", PermSoft);
+  printf("Temporary softening prefactor:\t%.3f\n", TempSoft);
+  printf("PermSoftening cap:\t%.3f\n", PermSofteningCap);
+  printf("\nSimulation Environment:\n");
+  printf("Applied strain rate:\t%.3e\n", strainrate);
+  printf("Strain increment in recording data:\t%.3e\n", strainincrement);
+  printf("End Strain:\t%.3f\n", EndStrain);
+  printf("Softening model: %s\n", softening_FLAG == 0 ? "OFF" : "ON");
+  printf("Relaxation time:\t%.3e\n", RelxTime);
+  printf("Ratio for generating residual stress:\t%.3f\n", ResiRatio);
 }
 
 void PrintFlags(void) {
+  /* the reference's list and order (io.c:374-434); the switches it also
+   * lists that this layer refuses cannot be defined here */
   printf("Active flags in bmgFlags.h:\n");
+#ifdef COMPRESSION
+  printf("#define COMPRESSION\n");
+#endif
 #ifdef TENSION
   printf("#define TENSION\n");
 #endif
 #ifdef SHEAR
   printf("#define SHEAR\n");
 #endif
-#ifdef COMPRESSION
-  printf("#define COMPRESSION\n");
+#ifdef PRE_RELAXATION
+  printf("#define PRE_RELAXATION\n");
 #endif
-#ifdef MICRO_MEMORY
-  printf("#define MICRO_MEMORY\n");
+#ifdef RESIDUAL_STRESS
+  printf("#define RESIDUAL_STRESS\n");
 #endif
-#ifdef INHOM_ELAST
-  printf("#define INHOM_ELAST\n");
+#ifdef UNIFORM_DEFECTS
+  printf("#define UNIFORM_DEFECTS\n");
 #endif
 #ifdef LOW_T
   printf("#define LOW_T\n");

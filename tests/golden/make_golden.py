@@ -38,7 +38,9 @@ directory and stores, per case:
                xsf        int64      0
              cases of a high-temperature material branch (MATERIAL_CASES) also:
                material   str        HIGH_T_Vit1 or HIGH_T_PdNiP
-and the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
+the reference's start-up printout under a few switch and input combinations
+(print_*.txt: its PrintFlags and ParameterPrint blocks), and
+the MT19937 known answers of the GSL conventions (mt19937_kat.npz), and
 the reference's InhomogeneousStressSolver on a spatially varying medium
 (inhom_32.npz, from inhom_ref.c: eps0, lam, mu, epsavg, sigma, stress).
 
@@ -119,6 +121,37 @@ MATERIAL_CASES = {
     "ref2d_32_vit1_s41": (32, 32, "TENSION", {"end": "0.5", "seed": "41"}, 1500, "HIGH_T_Vit1"),
     "ref2d_32_pdnip_s42": (32, 32, "TENSION", {"end": "0.5", "seed": "42"}, 1500, "HIGH_T_PdNiP"),
 }
+
+
+# the reference's start-up printout (PrintFlags, ParameterPrint; io.c:349-434)
+# under a few switch and input combinations: (loading, material, input overrides)
+PRINT_CASES = {
+    "print_tension": ("TENSION", None, {}),
+    "print_shear_nosoft": ("SHEAR", None, {"soft": "0", "end": "0.1"}),
+    "print_vit1": ("TENSION", "HIGH_T_Vit1", {"rate": "5e-5"}),
+}
+
+
+def print_case(name, loading, material, overrides):
+    """Runs the reference for one thermal event and keeps its flag block and
+    parameter block as <name>.txt."""
+    exe = build_ref2d(32, 32, loading, material=material)
+    d = tempfile.mkdtemp(prefix="stz_ref_print_")
+    configs.write_input(os.path.join(d, "input"), **overrides)
+    env = dict(os.environ, STZ_REF_LOG=os.path.join(d, "log.txt"), STZ_REF_MAX_EVENTS="1",
+               STZ_REF_DUMP=os.path.join(d, "dump.bin"))
+    out = subprocess.run([exe], cwd=d, env=env, capture_output=True, text=True, check=True).stdout
+    lines = out.split("\n")
+    i = lines.index("Active flags in bmgFlags.h:")
+    j = i + 1
+    while lines[j].startswith("#define"):
+        j += 1
+    k = lines.index("Simulation Geometry:") - 1
+    m = next(n for n in range(k, len(lines)) if lines[n].startswith("Ratio for generating residual stress:"))
+    text = "\n".join(lines[i:j] + lines[k:m + 1]) + "\n"
+    with open(os.path.join(HERE, name + ".txt"), "w") as f:
+        f.write(text)
+    print(name, "->", name + ".txt")
 
 
 def mro_structure(nx, ny, seed=2024):
@@ -289,3 +322,6 @@ if __name__ == "__main__":
     for name, (nx, ny, loading, ov, ev, mat) in MATERIAL_CASES.items():
         if not only or name in only:
             run_case(name, nx, ny, loading, ov, ev, material=mat)
+    for name, (loading, mat, ov) in PRINT_CASES.items():
+        if not only or name in only:
+            print_case(name, loading, mat, ov)

@@ -201,6 +201,29 @@ def test_drop_in_init_material_branches(engine_lib, material):
     assert got == [p.young, p.poisson, p.mu, p.lambda_, p.q0_mean]
 
 
+@pytest.mark.parametrize("case,defs,overrides", [
+    ("print_tension", [], {}),
+    ("print_shear_nosoft", ["-DREFAPI_TEST_SHEAR"], {"soft": "0", "end": "0.1"}),
+    ("print_vit1", ["-DREFAPI_TEST_HIGH_T", "-DHIGH_T_Vit1"], {"rate": "5e-5"}),
+])
+def test_drop_in_startup_printout_matches_reference(engine_lib, case, defs, overrides):
+    """The flag block and the parameter block the drop-in prints at start-up
+    (CPU, no device) are the reference's own, byte for byte
+    (tests/golden/print_*.txt, written by the reference's build)."""
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "print_check")
+        cmd = (["gcc", *CFLAGS, *defs, "-DREFAPI_NX=32", "-DREFAPI_NY=32", "-I", TESTHDR, "-I", SHIM,
+                "-I", os.path.join(ROOT, "include"), os.path.join(TESTHDR, "print_check.c"), REFAPI] + _support() +
+               ["-o", exe] + _lib_args())
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        configs.write_input(os.path.join(d, "input"), **overrides)
+        r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr[-2000:]
+    want = open(os.path.join(ROOT, "tests", "golden", case + ".txt")).read()
+    assert r.stdout == want
+
+
 REFUSED_SWITCHES = [
     (["-DSTRAIN_RATE_SENSITIVITY"], "STRAIN_RATE_SENSITIVITY"),
     (["-DSTRAIN_RATE_SENSITIVITY", "-DLOCAL_RATE_V2"], "LOCAL_RATE_V2"),
