@@ -593,7 +593,7 @@ void WriteScalarMPI_INT(int* field, char* s, int step) { write_record(field, siz
 void WriteMROMPI_INT(int* field, char* s, int step) { write_record(field, sizeof(int), s, step); }
 
 void ParameterPrint(void) {
-  /* the reference's text, byte for byte (io.c:349-372), so that logs of a
+  /* the reference's text, byte for byte (io.c:103-135), so that logs of a
    * drop-in build compare with the reference's */
   printf("\nSimulation Geometry:\n");
   printf("System size:\t[%d x %d]\n", NX, NY);

@@ -123,7 +123,7 @@ MATERIAL_CASES = {
 }
 
 
-# the reference's start-up printout (PrintFlags, ParameterPrint; io.c:349-434)
+# the reference's start-up printout (PrintFlags, ParameterPrint; io.c:103-135, 374-434)
 # under a few switch and input combinations: (loading, material, input overrides)
 PRINT_CASES = {
     "print_tension": ("TENSION", None, {}),
